@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Benchmark: candidate literals scored per second on one GB300.
+
+Workload (default ``batched_step``): one refinement step of 256 candidate
+literals over a 32M x 6 binding set (10% positive) and 32 relations of arity
+1-3 (log-uniform 1K-8M tuples, Zipf s=1.1 keys over a 2M domain); seeded
+synthetic data.  ``--workload single_literal`` runs the 16M x 4 binding set /
+4M-tuple relation single-literal operator bench instead.
+
+A step = one batched evaluation of all the step's literals (exact counts).
+``value`` is literals/s with the binding set resident in HBM; ``e2e`` is the
+same metric through the C ABI from pinned host buffers (binding-set upload
+and count download inside the timed region); the plain per-literal GPU path
+is timed beside it (``per_literal``).  Inputs (768 MB of binding columns)
+are larger than the 129 MB L2, so no flush is needed between steps.
+
+``--impl reference`` times the CPU restatement of the reference's operator
+chain (the oracle; the reference itself cannot be built on the GPU host) on
+all host cores over a bounded sample of the same step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["batched_step", "single_literal", "single_literal_zipf"],
+                    default="batched_step")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="fraction of the binding-set size (for quick checks only)")
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="literals in the CPU-baseline sample (0 = automatic)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-per-literal", action="store_true")
+    return ap.parse_args()
+
+
+def make_workload(args, rank: int):
+    from quickfoil_gb300 import workloads
+    if args.workload == "batched_step":
+        return workloads.batched_step(n_bindings=int(32_000_000 * args.scale), seed=3 + rank)
+    return workloads.single_literal(n_bindings=int(16_000_000 * args.scale),
+                                    zipf=args.workload.endswith("zipf"), seed=2 + rank)
+
+
+def workload_config(args, w):
+    cfg = {"workload": w.name, "binding_rows": w.num_bindings,
+           "binding_columns": len(w.binding_columns), "positive_rows": w.num_positive,
+           "relations": len(w.relations), "relation_tuples": w.relation_tuples(),
+           "literals": len(w.literals), "key_domain": w.domain,
+           "l2_policy": "inputs larger than L2 (binding columns %d MB > 129 MB)"
+                        % (w.num_bindings * len(w.binding_columns) * 4 // 2**20)}
+    if args.scale != 1.0:
+        cfg["scale"] = args.scale
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+            self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.fh,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, flags in rows for i, f in enumerate(flags)
+                          if f.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(w, nthreads: int, sample: int, budget_s: float = 20.0):
+    """The oracle (CPU restatement of the reference chain) on a bounded
+    sample of the step's literals; returns (literals/s, sample description)."""
+    import oracle
+    o = oracle.Oracle(w.relations)
+    lits = [l.as_tuple() for l in w.literals]
+    if sample <= 0:
+        # grow the sample until the run takes a few seconds, within the budget
+        sample = 2
+        t0 = time.perf_counter()
+        o.evaluate(w.binding_columns, w.num_positive, lits[:sample], 5, nthreads)
+        dt = time.perf_counter() - t0
+        sample = int(max(2, min(len(lits), sample * budget_s / max(dt, 1e-3) / 2)))
+    o.evaluate(w.binding_columns, w.num_positive, lits[:sample], 5, nthreads)  # warm relation cache
+    t0 = time.perf_counter()
+    o.evaluate(w.binding_columns, w.num_positive, lits[:sample], 5, nthreads)
+    dt = time.perf_counter() - t0
+    o.close()
+    return sample / dt, dt, sample
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    w = make_workload(args, 0)
+    threads = os.cpu_count() or 1
+    import oracle
+    o = oracle.Oracle(w.relations)
+    lits = [l.as_tuple() for l in w.literals]
+    sample = args.cpu_sample if args.cpu_sample > 0 else min(len(lits), 16)
+    step_lits = lits[:sample]
+    for _ in range(args.warmup):
+        o.evaluate(w.binding_columns, w.num_positive, step_lits, 5, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.evaluate(w.binding_columns, w.num_positive, step_lits, 5, threads)
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    o.close()
+    value = sample / dt
+    line = {"impl": "reference", "metric": "candidate literals scored/s (exact counts)",
+            "value": value, "unit": "literals/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64",
+            "data": "synthetic (seeded)", "config": workload_config(args, w),
+            "cpu_baseline": {"value": value, "unit": "literals/s", "cores": threads,
+                             "kind": "port",
+                             "sample": f"first {sample} of {len(lits)} literals of the step, "
+                                       "oracle (C restatement of the reference operator chain), "
+                                       f"{threads} threads"},
+            "e2e": {"value": value, "unit": "literals/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    from quickfoil_gb300 import Engine
+    from quickfoil_gb300 import _capi as C
+    w = make_workload(args, rank)
+    eng = Engine(local_rank)
+    stream = torch.cuda.current_stream(dev)
+    eng.set_stream(stream.cuda_stream)
+    for rid, cols in enumerate(w.relations):
+        eng.register_relation(rid, cols)
+    dev_cols = [torch.from_numpy(c).to(dev) for c in w.binding_columns]
+    b = eng.bindings(dev_cols, w.num_positive)
+    n = len(w.literals)
+    lits_c = (C.QfgLiteral * n)(*[l.to_c() for l in w.literals])
+    counts = torch.zeros((n, 4), dtype=torch.int64, device=dev)
+
+    # First touch: relation key tables (cached for the run, like the
+    # reference's relation partitions).
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.evaluate_step_device(b, lits_c, n, counts.data_ptr())
+    torch.cuda.synchronize()
+    first_touch_ms = (time.perf_counter() - t0) * 1e3
+    traffic = eng.step_traffic(b, w.literals)
+
+    for _ in range(args.warmup):
+        eng.evaluate_step_device(b, lits_c, n, counts.data_ptr())
+    torch.cuda.synchronize()
+    eng.set_option(C.QFG_OPT_STAGE_TIMING, 1)
+    eng.stage_times(reset=True)
+    launches0 = eng.kernel_launches()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        eng.evaluate_step_device(b, lits_c, n, counts.data_ptr())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = eng.kernel_launches() - launches0
+    stages = eng.stage_times(reset=True)
+    eng.set_option(C.QFG_OPT_STAGE_TIMING, 0)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    batched_counts = counts.cpu().numpy().copy()
+
+    # Plain per-literal GPU path (one operator chain per literal).
+    per_lit = None
+    if not args.no_per_literal:
+        host_counts = np.zeros((n, 4), dtype=np.int64)
+        eng.evaluate_per_literal(b, w.literals)  # warm relation partitions
+        eng.set_option(C.QFG_OPT_STAGE_TIMING, 1)
+        eng.stage_times(reset=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_counts = eng.evaluate_per_literal(b, w.literals)
+        pl_s = time.perf_counter() - t0
+        pl_stage = eng.stage_times(reset=True)
+        eng.set_option(C.QFG_OPT_STAGE_TIMING, 0)
+        per_lit = {"value": n / pl_s, "unit": "literals/s", "ms_per_step": pl_s * 1e3,
+                   "join_count_kernel_ms": pl_stage["per_literal"][0],
+                   "counts_equal_batched": bool(np.array_equal(host_counts, batched_counts))}
+
+    # End to end through the C ABI from pinned host buffers.
+    pinned = [torch.from_numpy(c).pin_memory() for c in w.binding_columns]
+    h2d = sum(c.numel() * 4 for c in pinned)
+    d2h = n * 4 * 8
+    for _ in range(max(1, min(args.warmup, 2))):
+        be = eng.bindings(pinned, w.num_positive)
+        eng.evaluate_step(be, w.literals)
+        be.close()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    e2e_counts = None
+    for _ in range(args.steps):
+        be = eng.bindings(pinned, w.num_positive)
+        e2e_counts = eng.evaluate_step(be, w.literals)
+        be.close()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    if rank == 0:
+        peak, peak_kind = measured_peak_hbm()
+        st_ms = {k: v[0] / max(v[1], 1) * (v[1] / args.steps) for k, v in stages.items()}
+        dominant = max(("bind_partition", "evaluate"), key=lambda k: st_ms[k])
+        kernel_ms = stages[dominant][0] / args.steps
+        achieved = traffic[dominant] / (kernel_ms * 1e-3) / 1e9 if kernel_ms > 0 else 0.0
+        line = {
+            "metric": "candidate literals scored/s (batched persistent evaluation, exact counts)",
+            "value": n * world / (ms * 1e-3), "unit": "literals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32 keys / int64 counts", "data": "synthetic (seeded)",
+            "config": workload_config(args, w),
+            "e2e": {"value": n * world / e2e_s, "unit": "literals/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_s * 1e3,
+                    "counts_equal_device_path": bool(np.array_equal(e2e_counts, batched_counts))},
+            "gpu_launches": launches,
+            "stages_ms_per_step": {k: round(v, 4) for k, v in st_ms.items() if v > 0},
+            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "algorithmic_bytes": traffic[dominant],
+                         "peak_source": peak_kind},
+            "first_touch_ms": first_touch_ms,
+            "algorithmic_bytes_per_step": traffic,
+        }
+        if per_lit is not None:
+            line["per_literal"] = per_lit
+            line["batched_over_per_literal"] = line["value"] / (per_lit["value"] * world)
+        if clk is not None:
+            line["clocks"] = clk
+        if not args.no_cpu:
+            sample = args.cpu_sample
+            v, dt, s = cpu_baseline(w, 1, sample)
+            line["cpu_baseline"] = {"value": v, "unit": "literals/s", "cores": 1, "kind": "port",
+                                    "sample": f"first {s} of {n} literals of the step "
+                                              f"({dt:.1f} s), oracle = C restatement of the "
+                                              "reference operator chain, 1 thread like the "
+                                              "reference"}
+        print(json.dumps(line), flush=True)
+    b.close()
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,238 @@
+/*
+ * qfgpu.h -- C ABI of the GB300 candidate-literal engine (libqfgpu.so).
+ *
+ * Plain C: pointers, sizes and status codes, no C++ or CUDA types.  Every
+ * call returns a status (QFG_OK == 0); none aborts.  qfg_status_string()
+ * names a status and qfg_ctx_last_error() gives the detail of the last
+ * failure on a context.
+ *
+ * Each entry point names the reference (jbalint/quickfoil) interface it
+ * replaces.  The reference's operators are single-threaded C++ over host
+ * int32 columns; this library keeps the same data model (int32 columns,
+ * positives-first binding sets, four exact counts per candidate literal)
+ * with columns resident in GPU memory.
+ *
+ * Threading: a context is used by one host thread at a time; different
+ * contexts may be used concurrently.  Work is issued on the context's
+ * stream (qfg_ctx_set_stream); calls that return host data synchronize it.
+ */
+#ifndef QFGPU_H_
+#define QFGPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QFG_MAX_ARITY 8
+#define QFG_MAX_RADIX_BITS 15
+
+/* Status codes. */
+enum {
+  QFG_OK = 0,
+  QFG_ERR_INVALID = 1,     /* bad argument or descriptor (rejected before any launch) */
+  QFG_ERR_OOM = 2,         /* device allocation failed */
+  QFG_ERR_BUDGET = 3,      /* allocation would exceed the context's HBM budget */
+  QFG_ERR_CUDA = 4,        /* a CUDA call failed (message in qfg_ctx_last_error) */
+  QFG_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  QFG_ERR_NOT_FOUND = 6,   /* unknown relation id */
+  QFG_ERR_MISMATCH = 7     /* produced row counts differ from the announced ones */
+};
+
+/* Flags describing where caller columns live. */
+enum {
+  QFG_HOST = 0,            /* host memory: copied to the device */
+  QFG_DEVICE_COPY = 1,     /* device memory: copied into engine-owned memory */
+  QFG_DEVICE_BORROW = 2    /* device memory: used in place, caller keeps it alive */
+};
+
+/* Flags for the evaluation calls. */
+enum {
+  QFG_COUNTS_HOST = 0,     /* counts written to host memory, call synchronizes */
+  QFG_COUNTS_DEVICE = 1    /* counts written to device memory, call is asynchronous */
+};
+
+/* Context options (qfg_ctx_set_option). */
+enum {
+  QFG_OPT_NUM_RADIX_BITS = 1,   /* FLAGS_num_radix_bits for qfg_radix_partition defaults (5) */
+  QFG_OPT_EVAL_BITS = 2,        /* 0 = autotuned partition bits of the evaluation kernels */
+  QFG_OPT_WAIT_LIMIT = 3,       /* iteration limit of bounded device-side waits */
+  QFG_OPT_USE_GRAPHS = 4,       /* 1 = replay batched steps from captured CUDA graphs */
+  QFG_OPT_STAGE_TIMING = 5      /* 1 = time each evaluation stage with CUDA events */
+};
+
+/* Evaluation stages timed under QFG_OPT_STAGE_TIMING (the GPU counterpart of
+ * the reference's QuickFoilTimer stages, learner/QuickFoilTimer.hpp:25-38). */
+enum {
+  QFG_STAGE_KEY_TABLES = 0,     /* relation partitions / key tables (first touch only) */
+  QFG_STAGE_BIND_PARTITION = 1, /* binding-set partitioning */
+  QFG_STAGE_EVALUATE = 2,       /* build + probe + count */
+  QFG_STAGE_PER_LITERAL = 3,    /* plain per-literal join-count kernels */
+  QFG_NUM_STAGES = 4
+};
+
+typedef struct qfg_ctx qfg_ctx;
+typedef struct qfg_bindings qfg_bindings;
+
+/* A candidate literal (reference schema/FoilLiteral.hpp:21-164).
+ * vars[i] >= 0: argument i is bound to clause variable vars[i], i.e. to
+ * binding-set column vars[i]; vars[i] == -1: unbound (a new variable).
+ * join_pos is FoilLiteral::join_key() (schema/FoilLiteral.hpp:133-144): the
+ * bound argument with the largest variable type id, the first on ties. */
+typedef struct {
+  int32_t relation_id;
+  int32_t num_args;
+  int32_t join_pos;
+  int32_t vars[QFG_MAX_ARITY];
+} qfg_literal;
+
+/* ---- library / context ------------------------------------------------ */
+int qfg_version(void);
+const char* qfg_status_string(int status);
+
+/* Creates a context on CUDA device `device`.  hbm_budget_bytes bounds the
+ * device memory the context may hold (0 = 90% of the free memory).  No
+ * reference counterpart: the reference allocates with malloc and an
+ * optional byte quota (memory/MemoryUsage.hpp:33-66). */
+int qfg_ctx_create(int device, int64_t hbm_budget_bytes, qfg_ctx** out);
+int qfg_ctx_destroy(qfg_ctx* ctx);
+const char* qfg_ctx_last_error(const qfg_ctx* ctx);
+/* stream is a cudaStream_t passed as void*; NULL selects the legacy stream. */
+int qfg_ctx_set_stream(qfg_ctx* ctx, void* stream);
+int qfg_ctx_synchronize(qfg_ctx* ctx);
+int qfg_ctx_set_option(qfg_ctx* ctx, int option, int64_t value);
+/* Bytes held and budget. */
+int qfg_ctx_memory(const qfg_ctx* ctx, int64_t* used_bytes, int64_t* budget_bytes);
+/* Number of kernels this context has launched (for launch accounting). */
+int qfg_ctx_kernel_launches(const qfg_ctx* ctx, int64_t* launches);
+/* Accumulated milliseconds and call counts per stage (QFG_NUM_STAGES
+ * entries each; synchronizes the stream); reset_after != 0 clears them. */
+int qfg_ctx_stage_times(qfg_ctx* ctx, double* ms, int64_t* calls, int reset_after);
+
+/* ---- background relations --------------------------------------------- */
+/* Replaces FoilPredicate's fact table (schema/FoilPredicate.hpp:21-68):
+ * num_columns int32 columns of num_tuples rows, registered once per run.
+ * Derived per-column partitions and key tables are cached on the device,
+ * as TableView caches partitions (storage/TableView.hpp:62-80). */
+int qfg_relation_register(qfg_ctx* ctx, int32_t relation_id, int32_t num_columns,
+                          const int32_t* const* columns, int64_t num_tuples, int flags);
+int qfg_relation_release(qfg_ctx* ctx, int32_t relation_id);
+
+/* ---- binding sets ------------------------------------------------------ */
+/* Replaces FoilClause's binding blocks (schema/FoilClause.hpp:72-109):
+ * consecutive layout, rows [0, num_positive) positive then num_negative
+ * negative rows (integral_blocks). */
+int qfg_bindings_create(qfg_ctx* ctx, int32_t num_columns, const int32_t* const* columns,
+                        int64_t num_positive, int64_t num_negative, int flags,
+                        qfg_bindings** out);
+/* Split layout (positive_blocks / negative_blocks, schema/FoilClause.hpp:
+ * 152-161); stored consecutively on the device. */
+int qfg_bindings_create_split(qfg_ctx* ctx, int32_t num_columns,
+                              const int32_t* const* positive_columns, int64_t num_positive,
+                              const int32_t* const* negative_columns, int64_t num_negative,
+                              int flags, qfg_bindings** out);
+int qfg_bindings_destroy(qfg_ctx* ctx, qfg_bindings* bindings);
+int qfg_bindings_info(const qfg_bindings* bindings, int32_t* num_columns,
+                      int64_t* num_positive, int64_t* num_negative);
+/* Device pointer of one column (rows positives first). */
+int qfg_bindings_column(const qfg_bindings* bindings, int32_t column, const int32_t** device_ptr);
+/* Copies all columns to host arrays of num_positive + num_negative rows. */
+int qfg_bindings_download(qfg_ctx* ctx, const qfg_bindings* bindings,
+                          int32_t* const* host_columns);
+
+/* ---- candidate-literal evaluation (the hot path) ----------------------- */
+/* counts receives 4 int64 per literal in CandidateLiteralInfo field order
+ * (learner/CandidateLiteralInfo.hpp:15-26): num_covered_positive,
+ * num_covered_negative, num_binding_positive, num_binding_negative.
+ * covered = distinct binding rows of the label with at least one matching
+ * relation tuple; binding = matching (relation tuple, binding row) pairs. */
+
+/* CandidateLiteralEvaluator::Evaluate (learner/CandidateLiteralEvaluator.hpp:
+ * 28-31, .cpp:264-406): every literal joins on clause variable
+ * clause_join_key_id (vars[join_pos] == clause_join_key_id). */
+int qfg_evaluate_group(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t clause_join_key_id,
+                       int32_t num_literals, const qfg_literal* literals, int64_t* counts,
+                       int flags);
+
+/* All candidate literals of one refinement step at once, any join variable
+ * (the loop of QuickFoil::EvaluateAllCandidateLiterals,
+ * learner/QuickFoil.cpp:418-440, in one batched evaluation). */
+int qfg_evaluate_step(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
+                      const qfg_literal* literals, int64_t* counts, int flags);
+
+/* The plain per-literal GPU path: one RadixPartition -> BuildHashTable ->
+ * HashJoin -> Filter -> CountAggregator chain per literal, as the
+ * reference runs it (operations/*), with the binding side re-partitioned
+ * for every literal. */
+int qfg_evaluate_per_literal(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
+                             const qfg_literal* literals, int64_t* counts, int flags);
+
+/* Algorithmic bytes per stage (QFG_NUM_STAGES entries) that a batched step
+ * over these literals moves: what each stage must read and write at least
+ * once, the numerator of its HBM roofline.  Builds the relation key tables
+ * when they are not cached yet.  No reference counterpart. */
+int qfg_step_traffic(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
+                     const qfg_literal* literals, int64_t* bytes);
+
+/* ---- API-kept operators (device pointers, context stream) -------------- */
+/* RadixPartition (operations/RadixPartition.hpp:13-14, .cpp:56-186):
+ * stable partition of n int32 values by ((uint32)v) & (2^bits - 1) into
+ * PartitionTuple{int32 value, int32 tuple_id} (storage/PartitionTuple.hpp:
+ * 20-42).  d_out_tuples holds 2*n int32; d_offsets 2^bits + 1 int64
+ * (partition p = tuples [offsets[p], offsets[p+1])).  1 <= bits <= 15. */
+int qfg_radix_partition(qfg_ctx* ctx, const int32_t* d_values, int64_t n, int bits,
+                        int32_t* d_out_tuples, int64_t* d_offsets);
+
+/* BuildHashTableOnPartitions (operations/BuildHashTable.cpp:54-93) with the
+ * FoilHashTable layout (storage/FoilHashTable.cpp:34-49): for each non-empty
+ * partition p, buckets[next_pow2(n_p)] of 1-based chain heads and next[n_p]
+ * links, chains in descending position order, byte-identical to the
+ * reference's.  Input is qfg_radix_partition's output.  d_bucket_offsets
+ * (2^bits + 1 int64) receives where partition p's buckets start inside
+ * d_buckets, which must hold at least 2*n + 2^bits int32; d_masks (2^bits
+ * uint32) receives FoilHashTable::mask(); d_next holds n int32. */
+int qfg_build_hash_table_on_partitions(qfg_ctx* ctx, const int32_t* d_tuples,
+                                       const int64_t* d_offsets, int64_t n, int bits,
+                                       int32_t* d_buckets, int64_t* d_bucket_offsets,
+                                       uint32_t* d_masks, int32_t* d_next);
+
+/* BuildHashTableOnTable (operations/BuildHashTable.cpp:97-125,193-210):
+ * whole-table chained table over num_keys key columns, hash = the
+ * reference's Hash<k> HashCombine chain (utility/Hash.hpp:35-55).
+ * d_buckets holds next_pow2(n) int32, d_next n int32; *mask_out receives
+ * the mask.  Byte-identical to the reference's. */
+int qfg_build_hash_table_on_table(qfg_ctx* ctx, const int32_t* const* d_keys, int32_t num_keys,
+                                  int64_t n, int32_t* d_buckets, int32_t* d_next,
+                                  uint32_t* mask_out);
+
+/* LeftSemiJoin<k> (operations/LeftSemiJoin.hpp:55-141): bit i of d_bits
+ * (64-bit little-endian blocks, the BitVector layout of utility/BitVector.hpp)
+ * is set when probe row i matches some build row on all num_keys keys.
+ * *num_ones receives the set-bit count (SemiJoinChunk::num_ones). */
+int qfg_left_semijoin(qfg_ctx* ctx, const int32_t* const* d_probe_keys, int64_t num_probe,
+                      const int32_t* const* d_build_keys, int64_t num_build, int32_t num_keys,
+                      uint64_t* d_bits, int64_t* num_ones);
+
+/* RightSemiJoin<k> (operations/RightSemiJoin.hpp:44-82): bit j set when
+ * build row j is matched by some probe row. */
+int qfg_right_semijoin(qfg_ctx* ctx, const int32_t* const* d_probe_keys, int64_t num_probe,
+                       const int32_t* const* d_build_keys, int64_t num_build, int32_t num_keys,
+                       uint64_t* d_bits, int64_t* num_ones);
+
+/* CreateLabelAwareBindingTables (operations/MultiColumnHashJoin.cpp:117-256):
+ * the binding set extended by `literal`: every (binding row, relation
+ * tuple) pair matching on the literal's bound arguments, projecting the
+ * binding columns then one column per unbound argument, positives first,
+ * in the reference's row order.  num_out_positive / num_out_negative are
+ * the literal's binding counts; a different produced count returns
+ * QFG_ERR_MISMATCH.  The new binding set stays on the device. */
+int qfg_extend_bindings(qfg_ctx* ctx, const qfg_bindings* bindings, const qfg_literal* literal,
+                        int64_t num_out_positive, int64_t num_out_negative,
+                        qfg_bindings** out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QFGPU_H_ */

@@ -1,0 +1,246 @@
+"""CPU oracle for the QuickFOIL candidate-literal hot path.
+
+TEST INFRASTRUCTURE ONLY: imported by ``tests/``, by ``__graft_entry__.smoke``
+and by the CPU-baseline leg of ``bench.py`` as the checker.  The product
+package (``quickfoil_gb300``) never imports this module.
+
+``qf_oracle.c`` restates the reference operator chain in plain C; this module
+compiles it with gcc (``build()``) and exposes it through ctypes.  The
+restatement is pinned against the reference's own RadixPartition test cases
+and against count fixtures produced by the reference's own sources
+(``tests/golden``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_DIR = os.path.join(_HERE, "_lib")
+_LIB_PATH = os.path.join(_LIB_DIR, "libqforacle.so")
+MAX_ARITY = 8
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile ``qf_oracle.c`` into ``oracle/_lib/libqforacle.so``."""
+    src = os.path.join(_HERE, "qf_oracle.c")
+    hdr = os.path.join(_HERE, "qf_oracle.h")
+    if (not force and os.path.exists(_LIB_PATH)
+            and os.path.getmtime(_LIB_PATH) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+        return _LIB_PATH
+    os.makedirs(_LIB_DIR, exist_ok=True)
+    tmp = _LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-pthread",
+                           "-Wall", "-o", tmp, src])
+    os.replace(tmp, _LIB_PATH)
+    return _LIB_PATH
+
+
+class _Table(ctypes.Structure):
+    _fields_ = [("num_columns", ctypes.c_int32),
+                ("num_tuples", ctypes.c_int64),
+                ("columns", ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)))]
+
+
+class _Literal(ctypes.Structure):
+    _fields_ = [("relation", ctypes.c_int32),
+                ("num_args", ctypes.c_int32),
+                ("join_pos", ctypes.c_int32),
+                ("vars", ctypes.c_int32 * MAX_ARITY)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        L.qfo_radix_partition.argtypes = [i32p, ctypes.c_int64, ctypes.c_int, i32p, i64p]
+        L.qfo_radix_partition.restype = None
+        L.qfo_num_buckets.argtypes = [ctypes.c_int32]
+        L.qfo_num_buckets.restype = ctypes.c_int32
+        L.qfo_build_partition_hash_table.argtypes = [i32p, ctypes.c_int32, ctypes.c_int, i32p, i32p]
+        L.qfo_build_partition_hash_table.restype = ctypes.c_uint32
+        L.qfo_build_table_hash_table.argtypes = [ctypes.POINTER(i32p), ctypes.c_int, ctypes.c_int64,
+                                                 i32p, i32p]
+        L.qfo_build_table_hash_table.restype = ctypes.c_uint32
+        L.qfo_relcache_create.argtypes = []
+        L.qfo_relcache_create.restype = ctypes.c_void_p
+        L.qfo_relcache_destroy.argtypes = [ctypes.c_void_p]
+        L.qfo_relcache_destroy.restype = None
+        L.qfo_evaluate.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Table), ctypes.c_int,
+                                   ctypes.POINTER(_Table), ctypes.c_int64,
+                                   ctypes.POINTER(_Literal), ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, i64p]
+        L.qfo_evaluate.restype = ctypes.c_int
+        u64p = ctypes.POINTER(ctypes.c_uint64)
+        for name in ("qfo_left_semijoin", "qfo_right_semijoin"):
+            f = getattr(L, name)
+            f.argtypes = [ctypes.POINTER(i32p), ctypes.c_int64, ctypes.POINTER(i32p),
+                          ctypes.c_int64, ctypes.c_int, u64p]
+            f.restype = ctypes.c_int64
+        L.qfo_extend_bindings.argtypes = [ctypes.POINTER(_Table), ctypes.c_int64,
+                                          ctypes.POINTER(_Table), ctypes.POINTER(_Literal),
+                                          ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(i32p)]
+        L.qfo_extend_bindings.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _i32ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def _colptrs(cols: Sequence[np.ndarray]):
+    arr = (ctypes.POINTER(ctypes.c_int32) * max(1, len(cols)))()
+    for i, c in enumerate(cols):
+        arr[i] = _i32ptr(c)
+    return arr
+
+
+def _as_cols(cols) -> list:
+    return [np.ascontiguousarray(c, dtype=np.int32) for c in cols]
+
+
+class _TableHandle:
+    """Keeps the numpy columns alive while C holds pointers into them."""
+
+    def __init__(self, cols):
+        self.cols = _as_cols(cols)
+        self.ptrs = _colptrs(self.cols)
+        n = len(self.cols[0]) if self.cols else 0
+        self.struct = _Table(len(self.cols), n, self.ptrs)
+
+
+def _literal_struct(lit) -> _Literal:
+    relation, vars_, join_pos = lit
+    s = _Literal()
+    s.relation = relation
+    s.num_args = len(vars_)
+    s.join_pos = join_pos
+    for i in range(MAX_ARITY):
+        s.vars[i] = vars_[i] if i < len(vars_) else -1
+    return s
+
+
+def radix_partition(values: np.ndarray, bits: int):
+    """Returns (tuples[n,2] int32 (value, tuple_id), offsets[2^bits+1] int64)."""
+    values = np.ascontiguousarray(values, dtype=np.int32)
+    n = len(values)
+    out = np.empty((max(n, 1), 2), dtype=np.int32)
+    offsets = np.empty((1 << bits) + 1, dtype=np.int64)
+    lib().qfo_radix_partition(_i32ptr(values), n, bits, _i32ptr(out),
+                              offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    return out[:n], offsets
+
+
+def build_partition_hash_table(part_tuples: np.ndarray, bits: int):
+    """FoilHashTable over one partition: (buckets, next, mask)."""
+    part_tuples = np.ascontiguousarray(part_tuples, dtype=np.int32)
+    n = len(part_tuples)
+    nb = lib().qfo_num_buckets(n)
+    buckets = np.empty(nb, dtype=np.int32)
+    nxt = np.empty(n, dtype=np.int32)
+    mask = lib().qfo_build_partition_hash_table(_i32ptr(part_tuples), n, bits,
+                                                _i32ptr(buckets), _i32ptr(nxt))
+    return buckets, nxt, mask
+
+
+def build_table_hash_table(keys):
+    keys = _as_cols(keys)
+    n = len(keys[0])
+    nb = lib().qfo_num_buckets(n)
+    buckets = np.empty(nb, dtype=np.int32)
+    nxt = np.empty(max(n, 1), dtype=np.int32)
+    mask = lib().qfo_build_table_hash_table(_colptrs(keys), len(keys), n,
+                                            _i32ptr(buckets), _i32ptr(nxt))
+    return buckets, nxt[:n], mask
+
+
+class Oracle:
+    """Holds a relation-partition cache across evaluations, like the
+    reference's per-predicate TableView (partitions persist for the run)."""
+
+    def __init__(self, relations):
+        self._rels = [_TableHandle(r) for r in relations]
+        self._rel_structs = (_Table * max(1, len(self._rels)))(*[h.struct for h in self._rels])
+        self._cache = lib().qfo_relcache_create()
+
+    def close(self):
+        if self._cache:
+            lib().qfo_relcache_destroy(self._cache)
+            self._cache = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def evaluate(self, binding_columns, num_positive: int, literals, bits: int = 5,
+                 nthreads: int = 1) -> np.ndarray:
+        """Counts [n_literals, 4] int64: covered_pos, covered_neg, binding_pos,
+        binding_neg.  ``literals`` is a list of (relation, vars, join_pos)."""
+        b = _TableHandle(binding_columns)
+        lits = (_Literal * max(1, len(literals)))(*[_literal_struct(l) for l in literals])
+        counts = np.zeros((max(1, len(literals)), 4), dtype=np.int64)
+        rc = lib().qfo_evaluate(self._cache, self._rel_structs, len(self._rels),
+                                ctypes.byref(b.struct), num_positive, lits, len(literals),
+                                bits, nthreads,
+                                counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+        if rc != 0:
+            raise ValueError(f"oracle rejected the literal list (status {rc})")
+        return counts[:len(literals)]
+
+
+def evaluate(relations, binding_columns, num_positive, literals, bits=5, nthreads=1):
+    o = Oracle(relations)
+    try:
+        return o.evaluate(binding_columns, num_positive, literals, bits, nthreads)
+    finally:
+        o.close()
+
+
+def _semijoin(name, probe_keys, build_keys, nbits_rows):
+    probe_keys = _as_cols(probe_keys)
+    build_keys = _as_cols(build_keys)
+    out = np.zeros(max(1, (nbits_rows + 63) // 64), dtype=np.uint64)
+    ones = getattr(lib(), name)(_colptrs(probe_keys), len(probe_keys[0]), _colptrs(build_keys),
+                                len(build_keys[0]), len(probe_keys),
+                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    return out[:(nbits_rows + 63) // 64], int(ones)
+
+
+def left_semijoin(probe_keys, build_keys):
+    """Bit per probe row (uint64 blocks), number of set bits."""
+    return _semijoin("qfo_left_semijoin", probe_keys, build_keys, len(probe_keys[0]))
+
+
+def right_semijoin(probe_keys, build_keys):
+    """Bit per build row (uint64 blocks), number of set bits."""
+    return _semijoin("qfo_right_semijoin", probe_keys, build_keys, len(build_keys[0]))
+
+
+def extend_bindings(binding_columns, num_positive, relation_columns, literal,
+                    num_out_positive, num_out_negative):
+    """Label-aware binding-set extension; returns the list of new columns."""
+    b = _TableHandle(binding_columns)
+    r = _TableHandle(relation_columns)
+    _, vars_, _ = literal
+    n_unbound = sum(1 for v in vars_ if v < 0)
+    total = num_out_positive + num_out_negative
+    outs = [np.zeros(max(total, 1), dtype=np.int32) for _ in range(len(b.cols) + n_unbound)]
+    lit = _literal_struct(literal)
+    rc = lib().qfo_extend_bindings(ctypes.byref(b.struct), num_positive, ctypes.byref(r.struct),
+                                   ctypes.byref(lit), num_out_positive, num_out_negative,
+                                   _colptrs(outs))
+    if rc != 0:
+        raise ValueError(f"extension produced row counts different from the given ones ({rc})")
+    return [o[:total] for o in outs]

@@ -1,0 +1,130 @@
+/*
+ * qf_oracle.h -- CPU oracle for the QuickFOIL candidate-literal hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * operator chain (jbalint/quickfoil), used by tests/, by the smoke check and
+ * by the CPU-baseline leg of bench.py as the checker.  Nothing in the product
+ * library links, loads or calls it; the product path fails loudly when its
+ * CUDA library is missing instead of falling back to this code.
+ *
+ * Parity pinning: the radix partition restatement is checked against the
+ * reference's own RadixPartition_test cases (operations/RadixPartition_test.cpp
+ * :106-168); the count restatement is checked against fixtures produced by the
+ * reference's own CandidateLiteralEvaluator compiled from its sources (see
+ * oracle/build_ref.sh and tests/golden/make_golden.py).
+ *
+ * Every function names the reference file:line it follows.
+ */
+#ifndef QF_ORACLE_H_
+#define QF_ORACLE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QFO_MAX_ARITY 8
+
+/* storage/PartitionTuple.hpp:20-42: {int32 value; int32 tuple_id} (8 bytes). */
+typedef struct {
+  int32_t value;
+  int32_t tuple_id;
+} qfo_partition_tuple;
+
+/* A column store: num_columns int32 columns of num_tuples rows. */
+typedef struct {
+  int32_t num_columns;
+  int64_t num_tuples;
+  const int32_t* const* columns;
+} qfo_table;
+
+/* A candidate literal (schema/FoilLiteral.hpp): vars[i] >= 0 is the clause
+ * variable bound at argument i (a binding-set column), -1 is unbound.
+ * join_pos is FoilLiteral::join_key() (schema/FoilLiteral.hpp:133-144). */
+typedef struct {
+  int32_t relation;
+  int32_t num_args;
+  int32_t join_pos;
+  int32_t vars[QFO_MAX_ARITY];
+} qfo_literal;
+
+/* operations/RadixPartition.cpp:56-155.  Partition id of v is
+ * ((uint32_t)v) & (2^bits - 1) (utility/Hash.hpp:18-23, identity hash).
+ * Output tuples are grouped by partition and keep input order inside a
+ * partition.  offsets[p] .. offsets[p+1] delimit partition p
+ * (2^bits + 1 entries). */
+void qfo_radix_partition(const int32_t* values, int64_t n, int bits,
+                         qfo_partition_tuple* out, int64_t* offsets);
+
+/* storage/FoilHashTable.cpp:34-49: number of buckets = next power of two. */
+int32_t qfo_num_buckets(int32_t n);
+
+/* operations/BuildHashTable.cpp:54-93 for one partition of n > 0 tuples:
+ * buckets[next_pow2(n)] (1-based chain heads, 0 = empty) and next[n].
+ * Returns the FoilHashTable mask ((num_buckets - 1) << bits). */
+uint32_t qfo_build_partition_hash_table(const qfo_partition_tuple* part, int32_t n,
+                                        int bits, int32_t* buckets, int32_t* next);
+
+/* utility/Hash.hpp:25-55: HashCombine chain over num_keys int32 keys of row
+ * tid. */
+uint32_t qfo_hash_keys(const int32_t* const* keys, int num_keys, int64_t tid);
+
+/* operations/BuildHashTable.cpp:97-125: whole-table multi-key chained table
+ * (radix bits 0).  buckets has next_pow2(n) entries, next has n. */
+uint32_t qfo_build_table_hash_table(const int32_t* const* keys, int num_keys, int64_t n,
+                                    int32_t* buckets, int32_t* next);
+
+/* Relation-partition cache, the analogue of TableView::partitions_
+ * (storage/TableView.hpp:62-80): a relation column is partitioned once and
+ * reused by every later evaluation (learner/CandidateLiteralEvaluator.cpp:296-299). */
+typedef struct qfo_relcache qfo_relcache;
+qfo_relcache* qfo_relcache_create(void);
+void qfo_relcache_destroy(qfo_relcache* cache);
+
+/* CandidateLiteralEvaluator::Evaluate (learner/CandidateLiteralEvaluator.cpp:
+ * 264-406) over one binding set whose first num_positive rows are positive
+ * (consecutive layout, :316-343).  For each literal writes four counts to
+ * counts[4*i + 0..3] in CandidateLiteralInfo field order
+ * (learner/CandidateLiteralInfo.hpp:15-26): num_covered_positive,
+ * num_covered_negative, num_binding_positive, num_binding_negative.
+ * bits is FLAGS_num_radix_bits; nthreads > 1 evaluates (literal, partition)
+ * pairs on that many POSIX threads (the reference is single threaded; the
+ * counts do not depend on the thread count).
+ * Returns 0 on success, nonzero on an invalid literal. */
+int qfo_evaluate(qfo_relcache* cache, const qfo_table* relations, int num_relations,
+                 const qfo_table* bindings, int64_t num_positive,
+                 const qfo_literal* literals, int num_literals, int bits, int nthreads,
+                 int64_t* counts);
+
+/* LeftSemiJoin<k>::DoSemiJoin (operations/LeftSemiJoin.hpp:55-141): one bit
+ * per probe row, set when some build row matches on all k keys.  Bits are
+ * packed little-endian into 64-bit blocks (utility/BitVector.hpp:25-26).
+ * Returns the number of set bits. */
+int64_t qfo_left_semijoin(const int32_t* const* probe_keys, int64_t num_probe,
+                          const int32_t* const* build_keys, int64_t num_build, int num_keys,
+                          uint64_t* out_bits);
+
+/* RightSemiJoin<k>::Next (operations/RightSemiJoin.hpp:44-82): one bit per
+ * build row, set when some probe row matches.  Returns the set-bit count. */
+int64_t qfo_right_semijoin(const int32_t* const* probe_keys, int64_t num_probe,
+                           const int32_t* const* build_keys, int64_t num_build, int num_keys,
+                           uint64_t* out_bits);
+
+/* CreateLabelAwareBindingTables (operations/MultiColumnHashJoin.cpp:117-256)
+ * for a consecutive binding set.  Output columns: the binding columns then
+ * one column per unbound literal argument, positives first.  Rows are
+ * produced in the reference's order for the side it would build on.
+ * out_columns[c] must hold num_out_positive + num_out_negative rows; the
+ * caller takes those counts from the literal's binding counts.  Returns 0,
+ * or nonzero when the produced row counts differ from the given ones. */
+int qfo_extend_bindings(const qfo_table* bindings, int64_t num_positive,
+                        const qfo_table* relation, const qfo_literal* literal,
+                        int64_t num_out_positive, int64_t num_out_negative,
+                        int32_t* const* out_columns);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QF_ORACLE_H_ */

@@ -1,0 +1,26 @@
+// eval_common.cuh -- declarations shared by the evaluation paths.
+#pragma once
+
+#include "qfg_common.cuh"
+
+namespace qfg {
+
+// Checks every literal against the registered relations and the binding
+// set (arity, bound join key, variable range) before anything is launched.
+int validate_literals(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits);
+
+// Zeroes the 4*n count words; for QFG_COUNTS_HOST they live in scratch.
+int counts_begin(Ctx* ctx, int32_t n, int64_t* counts, int flags, unsigned long long** dev);
+// Copies counts back (QFG_COUNTS_HOST, synchronizing) and reports a device
+// wait that gave up.
+int counts_end(Ctx* ctx, int32_t n, int64_t* counts, int flags, unsigned long long* dev);
+
+// One literal through the plain per-literal chain; counts[0..3] accumulate.
+int evaluate_plain_one(Ctx* ctx, const qfg_bindings* b, const qfg_literal& l,
+                       unsigned long long* counts);
+
+// All literals through the batched engine; counts[4*i..] accumulate.
+int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
+                     unsigned long long* counts);
+
+}  // namespace qfg

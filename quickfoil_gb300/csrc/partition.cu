@@ -1,0 +1,410 @@
+// partition.cu -- stable radix partitioning and chained hash-table builds in
+// the reference's exact layouts.
+//
+// RadixPartition (operations/RadixPartition.cpp:56-155) produces, per radix
+// partition of the identity hash's low bits, the (value, tuple_id) pairs in
+// input order.  Here a warp owns a contiguous chunk of rows; a histogram pass
+// counts digits per (digit, warp chunk) with warp-aggregated updates
+// (__match_any_sync: one shared-memory add per distinct digit per 32 rows),
+// an exclusive scan in digit-major order turns the counts into output
+// cursors, and a scatter pass re-reads the chunk and writes each row at its
+// cursor plus its rank among same-digit lanes below it.  Chunks are disjoint
+// and scanned in row order, so the result is stable.
+//
+// The same stable pass, applied LSD-style to bucket ids, rebuilds the
+// reference's chained FoilHashTable byte for byte: a chain lists the
+// partition positions of one bucket in descending order, so after a stable
+// sort by (partition, bucket) each element's `next` is its predecessor in the
+// sorted order and the bucket head is the last one.
+#include "qfg_common.cuh"
+
+namespace qfg {
+
+namespace {
+
+constexpr int kMaxSmemPerBlock = 200 * 1024;
+
+// RadixPartition API input/output: digit source = the value, payload = the
+// row index, output = PartitionTuple{value, tuple_id} (8 bytes).
+struct RefTupleIO {
+  const int32_t* values;
+  int2* out;
+  __device__ __forceinline__ uint32_t key(int64_t i) const { return (uint32_t)values[i]; }
+  __device__ __forceinline__ void write(int64_t pos, int64_t i, uint32_t k) const {
+    out[pos] = make_int2((int32_t)k, (int32_t)i);
+  }
+};
+
+// One LSD pass over (u32 key, int32 payload) in structure-of-arrays form.
+struct SortIO {
+  const uint32_t* keys_in;
+  const int32_t* payload_in;  // null: payload is the row index
+  uint32_t* keys_out;
+  int32_t* payload_out;
+  __device__ __forceinline__ uint32_t key(int64_t i) const { return keys_in[i]; }
+  __device__ __forceinline__ void write(int64_t pos, int64_t i, uint32_t k) const {
+    keys_out[pos] = k;
+    payload_out[pos] = payload_in != nullptr ? payload_in[i] : (int32_t)i;
+  }
+};
+
+template <class IO>
+__global__ void stable_hist_kernel(IO io, int64_t n, int shift, int bits, int64_t chunk,
+                                   int64_t num_chunks, uint32_t* __restrict__ hist) {
+  extern __shared__ uint32_t sh_hist[];
+  const uint32_t P = 1u << bits, mask = P - 1u;
+  const int warps = blockDim.x >> 5, lane = lane_id();
+  uint32_t* h = sh_hist + (size_t)warp_id() * P;
+  for (uint32_t d = lane; d < P; d += 32) h[d] = 0;
+  __syncwarp();
+  const int64_t wc = (int64_t)blockIdx.x * warps + warp_id();
+  if (wc >= num_chunks) return;
+  const int64_t start = wc * chunk, end = min(n, start + chunk);
+  for (int64_t base = start; base < end; base += 32) {
+    const int64_t i = base + lane;
+    const bool valid = i < end;
+    const uint32_t d = valid ? (io.key(i) >> shift) & mask : 0u;
+    const unsigned act = __ballot_sync(kFullMask, valid);
+    if (valid) {
+      const unsigned peers = __match_any_sync(act, d);
+      if (lane == __ffs(peers) - 1) h[d] += __popc(peers);
+    }
+    __syncwarp();
+  }
+  for (uint32_t d = lane; d < P; d += 32) hist[(int64_t)d * num_chunks + wc] = h[d];
+}
+
+template <class IO>
+__global__ void stable_scatter_kernel(IO io, int64_t n, int shift, int bits, int64_t chunk,
+                                      int64_t num_chunks, const uint32_t* __restrict__ cursors) {
+  extern __shared__ uint32_t sh_cur[];
+  const uint32_t P = 1u << bits, mask = P - 1u;
+  const int warps = blockDim.x >> 5, lane = lane_id();
+  uint32_t* cur = sh_cur + (size_t)warp_id() * P;
+  const int64_t wc = (int64_t)blockIdx.x * warps + warp_id();
+  if (wc >= num_chunks) return;
+  for (uint32_t d = lane; d < P; d += 32) cur[d] = cursors[(int64_t)d * num_chunks + wc];
+  __syncwarp();
+  const int64_t start = wc * chunk, end = min(n, start + chunk);
+  const unsigned lt = lanemask_lt();
+  for (int64_t base = start; base < end; base += 32) {
+    const int64_t i = base + lane;
+    const bool valid = i < end;
+    const uint32_t k = valid ? io.key(i) : 0u;
+    const uint32_t d = (k >> shift) & mask;
+    const unsigned act = __ballot_sync(kFullMask, valid);
+    unsigned peers = 0;
+    uint32_t pos = 0;
+    if (valid) {
+      peers = __match_any_sync(act, d);
+      pos = cur[d] + __popc(peers & lt);
+    }
+    __syncwarp();
+    if (valid) {
+      io.write(pos, i, k);
+      if (lane == __ffs(peers) - 1) cur[d] += __popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+// offsets[d] = cursor of digit d in chunk 0; offsets[P] = n.
+__global__ void digit_offsets_kernel(const uint32_t* __restrict__ scanned, int64_t num_chunks,
+                                     int bits, int64_t n, int64_t* __restrict__ offsets) {
+  const uint32_t P = 1u << bits;
+  for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d <= P; d += gridDim.x * blockDim.x)
+    offsets[d] = d == P ? n : (int64_t)scanned[(int64_t)d * num_chunks];
+}
+
+struct PassShape {
+  int64_t chunk, num_chunks;
+  int warps;
+  size_t smem;
+  unsigned grid;
+};
+
+PassShape pass_shape(int64_t n, int bits) {
+  PassShape s;
+  const int64_t P = int64_t(1) << bits;
+  // Rows per warp chunk: large enough that the (digit, chunk) count table
+  // stays at most n/8 entries, and a multiple of 32.
+  s.chunk = std::max<int64_t>(1024, 8 * P);
+  s.num_chunks = std::max<int64_t>(1, (n + s.chunk - 1) / s.chunk);
+  const int64_t per_warp = 4 * P;
+  s.warps = (int)std::min<int64_t>(8, std::max<int64_t>(1, kMaxSmemPerBlock / per_warp));
+  s.smem = (size_t)(per_warp * s.warps);
+  s.grid = (unsigned)((s.num_chunks + s.warps - 1) / s.warps);
+  return s;
+}
+
+template <class IO>
+int stable_pass(Ctx* ctx, IO io, int64_t n, int shift, int bits, int64_t* digit_offsets) {
+  const PassShape s = pass_shape(n, bits);
+  const int64_t entries = s.num_chunks * (int64_t(1) << bits);
+  QFG_TRY(ctx->scratch[kScrHist].reserve(ctx, sizeof(uint32_t) * (size_t)entries));
+  uint32_t* hist = ctx->scratch[kScrHist].as<uint32_t>();
+  if (s.smem > 48 * 1024) {
+    QFG_CUDA(ctx, cudaFuncSetAttribute(stable_hist_kernel<IO>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem));
+    QFG_CUDA(ctx, cudaFuncSetAttribute(stable_scatter_kernel<IO>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem));
+  }
+  stable_hist_kernel<IO><<<s.grid, 32 * s.warps, s.smem, ctx->stream>>>(io, n, shift, bits, s.chunk,
+                                                                        s.num_chunks, hist);
+  QFG_LAUNCHED(ctx);
+  QFG_TRY(exclusive_scan_u32(ctx, hist, hist, entries, nullptr));
+  if (digit_offsets != nullptr) {
+    const uint32_t P = 1u << bits;
+    digit_offsets_kernel<<<(P + 256) / 256, 256, 0, ctx->stream>>>(hist, s.num_chunks, bits, n,
+                                                                   digit_offsets);
+    QFG_LAUNCHED(ctx);
+  }
+  stable_scatter_kernel<IO><<<s.grid, 32 * s.warps, s.smem, ctx->stream>>>(
+      io, n, shift, bits, s.chunk, s.num_chunks, hist);
+  QFG_LAUNCHED(ctx);
+  return QFG_OK;
+}
+
+// Stable LSD sort of n (u32 key < 2^key_bits, int32 payload) pairs.  The
+// first pass reads keys from k0 and takes the row index as payload; passes
+// then ping-pong between (k0, p0) and (k1, p1).  The result ends in
+// (*k_out, *p_out).
+int stable_sort_pairs(Ctx* ctx, uint32_t* k0, int32_t* p0, uint32_t* k1, int32_t* p1, int64_t n,
+                      int key_bits, uint32_t** k_out, int32_t** p_out) {
+  uint32_t* kin = k0;
+  int32_t* pin = p0;
+  uint32_t* kout = k1;
+  int32_t* pout = p1;
+  const int passes = std::max(1, (key_bits + 11) / 12);
+  const int step = (key_bits + passes - 1) / passes;
+  int shift = 0;
+  for (int pass = 0; pass < passes; ++pass) {
+    const int bits = std::max(1, std::min(step, key_bits - shift));
+    SortIO io{kin, pass == 0 ? nullptr : pin, kout, pout};
+    QFG_TRY(stable_pass(ctx, io, n, shift, bits, nullptr));
+    shift += bits;
+    std::swap(kin, kout);
+    std::swap(pin, pout);
+  }
+  *k_out = kin;
+  *p_out = pin;
+  return QFG_OK;
+}
+
+__device__ __forceinline__ int64_t find_partition(const int64_t* __restrict__ offsets, int P,
+                                                  int64_t i) {
+  int lo = 0, hi = P - 1;  // largest p with offsets[p] <= i
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (offsets[mid] <= i) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void bucket_counts_kernel(const int64_t* __restrict__ offsets, int P,
+                                     uint32_t* __restrict__ nb) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+    const int64_t c = offsets[p + 1] - offsets[p];
+    uint32_t v = 0;
+    if (c > 0) {  // NEXT_POW_2 (storage/FoilHashTable.cpp:17-31)
+      v = (uint32_t)c - 1u;
+      v |= v >> 1; v |= v >> 2; v |= v >> 4; v |= v >> 8; v |= v >> 16;
+      v += 1u;
+    }
+    nb[p] = v;
+  }
+}
+
+__global__ void bucket_meta_kernel(const uint32_t* __restrict__ nb, const uint32_t* __restrict__ nb_scan,
+                                   const uint32_t* __restrict__ total, int P, int bits,
+                                   int64_t* __restrict__ bucket_offsets, uint32_t* __restrict__ masks) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p <= P; p += gridDim.x * blockDim.x) {
+    if (p == P) {
+      bucket_offsets[P] = *total;
+    } else {
+      bucket_offsets[p] = nb_scan[p];
+      masks[p] = nb[p] > 0 ? ((nb[p] - 1u) << bits) : 0u;
+    }
+  }
+}
+
+// Global bucket id of every partition position: bucket_offsets[p] +
+// ((uint32)v & mask_p) >> bits (operations/BuildHashTable.cpp:81-84).
+__global__ void partition_bucket_ids_kernel(const int2* __restrict__ tuples, int64_t n,
+                                            const int64_t* __restrict__ offsets, int P, int bits,
+                                            const int64_t* __restrict__ bucket_offsets,
+                                            const uint32_t* __restrict__ masks,
+                                            uint32_t* __restrict__ gid) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = find_partition(offsets, P, i);
+    const uint32_t b = (ref_hash(tuples[i].x) & masks[p]) >> bits;
+    gid[i] = (uint32_t)bucket_offsets[p] + b;
+  }
+}
+
+// After a stable sort by global bucket id: link each position to its
+// predecessor in the same bucket and make the last one the bucket head.
+// Positions are relative to the segment that row i belongs to.
+__global__ void chain_links_kernel(const uint32_t* __restrict__ sorted_gid,
+                                   const int32_t* __restrict__ sorted_row, int64_t n,
+                                   const int64_t* __restrict__ offsets, int P,
+                                   int32_t* __restrict__ buckets, int32_t* __restrict__ next) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t g = sorted_gid[s];
+    const int64_t i = sorted_row[s];
+    const int64_t base = offsets != nullptr ? offsets[find_partition(offsets, P, i)] : 0;
+    int32_t link = 0;
+    if (s > 0 && sorted_gid[s - 1] == g) link = (int32_t)(sorted_row[s - 1] - base + 1);
+    next[i] = link;
+    if (s == n - 1 || sorted_gid[s + 1] != g) buckets[g] = (int32_t)(i - base + 1);
+  }
+}
+
+// Hash<k> (utility/Hash.hpp:35-55) bucket of every row, mask = nb - 1.
+__global__ void table_bucket_ids_kernel(const int32_t* const* __restrict__ keys, int num_keys,
+                                        int64_t n, uint32_t mask, uint32_t* __restrict__ gid) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t h = ref_hash(keys[0][i]);
+    for (int k = 1; k < num_keys; ++k) h = ref_hash_combine(h, keys[k][i]);
+    gid[i] = h & mask;
+  }
+}
+
+int bits_for(uint64_t x) {  // smallest b with 2^b > x - 1, at least 1
+  int b = 1;
+  while (b < 32 && (uint64_t(1) << b) < x) ++b;
+  return b;
+}
+
+unsigned grid_for(Ctx* ctx, int64_t n, int threads) {
+  int64_t blocks = (n + threads - 1) / threads;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)ctx->num_sms * 16));
+}
+
+}  // namespace
+
+int radix_partition_ref(Ctx* ctx, const int32_t* values, int64_t n, int bits, int32_t* out_tuples,
+                        int64_t* out_offsets) {
+  if (n == 0) {
+    const uint32_t P = 1u << bits;
+    QFG_CUDA(ctx, cudaMemsetAsync(out_offsets, 0, sizeof(int64_t) * (P + 1), ctx->stream));
+    return QFG_OK;
+  }
+  RefTupleIO io{values, reinterpret_cast<int2*>(out_tuples)};
+  return stable_pass(ctx, io, n, 0, bits, out_offsets);
+}
+
+int relation_partitions(Ctx* ctx, Relation* rel, int column, int bits, PartitionedColumn** out) {
+  auto key = std::make_pair(column, bits);
+  auto it = rel->partitions.find(key);
+  if (it != rel->partitions.end()) {
+    *out = it->second.get();
+    return QFG_OK;
+  }
+  auto pc = std::make_unique<PartitionedColumn>();
+  pc->bits = bits;
+  pc->n = rel->num_tuples;
+  QFG_TRY(pc->tuples.reserve(ctx, sizeof(int32_t) * 2 * (size_t)std::max<int64_t>(pc->n, 1)));
+  QFG_TRY(pc->offsets.reserve(ctx, sizeof(int64_t) * ((size_t(1) << bits) + 1)));
+  QFG_TRY(radix_partition_ref(ctx, rel->columns[column], pc->n, bits, pc->tuples.as<int32_t>(),
+                              pc->offsets.as<int64_t>()));
+  *out = pc.get();
+  rel->partitions[key] = std::move(pc);
+  return QFG_OK;
+}
+
+}  // namespace qfg
+
+using namespace qfg;
+
+extern "C" int qfg_radix_partition(qfg_ctx* c, const int32_t* d_values, int64_t n, int bits,
+                                   int32_t* d_out_tuples, int64_t* d_offsets) {
+  if (c == nullptr) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  if (bits < 1 || bits > QFG_MAX_RADIX_BITS || n < 0 || n > INT32_MAX || d_offsets == nullptr ||
+      (n > 0 && (d_values == nullptr || d_out_tuples == nullptr)))
+    return set_error(ctx, QFG_ERR_INVALID, "qfg_radix_partition: invalid arguments");
+  return radix_partition_ref(ctx, d_values, n, bits, d_out_tuples, d_offsets);
+}
+
+extern "C" int qfg_build_hash_table_on_partitions(qfg_ctx* c, const int32_t* d_tuples,
+                                                  const int64_t* d_offsets, int64_t n, int bits,
+                                                  int32_t* d_buckets, int64_t* d_bucket_offsets,
+                                                  uint32_t* d_masks, int32_t* d_next) {
+  if (c == nullptr) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  if (bits < 1 || bits > QFG_MAX_RADIX_BITS || n < 0 || n > INT32_MAX / 2 ||
+      d_offsets == nullptr || d_bucket_offsets == nullptr || d_masks == nullptr ||
+      (n > 0 && (d_tuples == nullptr || d_buckets == nullptr || d_next == nullptr)))
+    return set_error(ctx, QFG_ERR_INVALID, "qfg_build_hash_table_on_partitions: invalid arguments");
+  const int P = 1 << bits;
+  QFG_TRY(ctx->scratch[kScrTmpA].reserve(ctx, sizeof(uint32_t) * (size_t)(2 * P + 2)));
+  uint32_t* nb = ctx->scratch[kScrTmpA].as<uint32_t>();
+  uint32_t* nb_scan = nb + P;
+  uint32_t* total = nb + 2 * P;
+  bucket_counts_kernel<<<(P + 255) / 256, 256, 0, ctx->stream>>>(d_offsets, P, nb);
+  QFG_LAUNCHED(ctx);
+  QFG_TRY(exclusive_scan_u32(ctx, nb, nb_scan, P, total));
+  bucket_meta_kernel<<<(P + 256) / 256, 256, 0, ctx->stream>>>(nb, nb_scan, total, P, bits,
+                                                              d_bucket_offsets, d_masks);
+  QFG_LAUNCHED(ctx);
+  if (n == 0) return QFG_OK;
+  // Buckets start empty (calloc in storage/FoilHashTable.cpp:44).
+  QFG_CUDA(ctx, cudaMemsetAsync(d_buckets, 0, sizeof(int32_t) * (size_t)(2 * n), ctx->stream));
+  QFG_TRY(ctx->scratch[kScrSortA].reserve(ctx, 2 * sizeof(uint32_t) * (size_t)n));
+  QFG_TRY(ctx->scratch[kScrSortB].reserve(ctx, 2 * sizeof(uint32_t) * (size_t)n));
+  uint32_t* k0 = ctx->scratch[kScrSortA].as<uint32_t>();
+  int32_t* p0 = reinterpret_cast<int32_t*>(k0 + n);
+  uint32_t* k1 = ctx->scratch[kScrSortB].as<uint32_t>();
+  int32_t* p1 = reinterpret_cast<int32_t*>(k1 + n);
+  partition_bucket_ids_kernel<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(
+      reinterpret_cast<const int2*>(d_tuples), n, d_offsets, P, bits, d_bucket_offsets, d_masks, k0);
+  QFG_LAUNCHED(ctx);
+  uint32_t* ks;
+  int32_t* ps;
+  QFG_TRY(stable_sort_pairs(ctx, k0, p0, k1, p1, n, bits_for((uint64_t)(2 * n + 1)), &ks, &ps));
+  chain_links_kernel<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(ks, ps, n, d_offsets, P,
+                                                                     d_buckets, d_next);
+  QFG_LAUNCHED(ctx);
+  return QFG_OK;
+}
+
+extern "C" int qfg_build_hash_table_on_table(qfg_ctx* c, const int32_t* const* d_keys,
+                                             int32_t num_keys, int64_t n, int32_t* d_buckets,
+                                             int32_t* d_next, uint32_t* mask_out) {
+  if (c == nullptr) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  if (num_keys < 1 || num_keys > QFG_MAX_ARITY || n < 1 || n > INT32_MAX / 2 ||
+      d_keys == nullptr || d_buckets == nullptr || d_next == nullptr || mask_out == nullptr)
+    return set_error(ctx, QFG_ERR_INVALID, "qfg_build_hash_table_on_table: invalid arguments");
+  uint32_t nb = (uint32_t)n - 1u;
+  nb |= nb >> 1; nb |= nb >> 2; nb |= nb >> 4; nb |= nb >> 8; nb |= nb >> 16;
+  nb += 1u;
+  const uint32_t mask = nb - 1u;
+  *mask_out = mask;
+  QFG_TRY(ctx->scratch[kScrTmpB].reserve(ctx, sizeof(const int32_t*) * QFG_MAX_ARITY));
+  const int32_t** keys_dev = ctx->scratch[kScrTmpB].as<const int32_t*>();
+  QFG_CUDA(ctx, cudaMemcpyAsync(keys_dev, d_keys, sizeof(const int32_t*) * num_keys,
+                                cudaMemcpyHostToDevice, ctx->stream));
+  QFG_CUDA(ctx, cudaMemsetAsync(d_buckets, 0, sizeof(int32_t) * nb, ctx->stream));
+  QFG_TRY(ctx->scratch[kScrSortA].reserve(ctx, 2 * sizeof(uint32_t) * (size_t)n));
+  QFG_TRY(ctx->scratch[kScrSortB].reserve(ctx, 2 * sizeof(uint32_t) * (size_t)n));
+  uint32_t* k0 = ctx->scratch[kScrSortA].as<uint32_t>();
+  int32_t* p0 = reinterpret_cast<int32_t*>(k0 + n);
+  uint32_t* k1 = ctx->scratch[kScrSortB].as<uint32_t>();
+  int32_t* p1 = reinterpret_cast<int32_t*>(k1 + n);
+  table_bucket_ids_kernel<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(keys_dev, num_keys, n,
+                                                                          mask, k0);
+  QFG_LAUNCHED(ctx);
+  uint32_t* ks;
+  int32_t* ps;
+  QFG_TRY(stable_sort_pairs(ctx, k0, p0, k1, p1, n, bits_for((uint64_t)nb), &ks, &ps));
+  chain_links_kernel<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(ks, ps, n, nullptr, 1,
+                                                                     d_buckets, d_next);
+  QFG_LAUNCHED(ctx);
+  QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return QFG_OK;
+}

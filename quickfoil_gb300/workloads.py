@@ -1,0 +1,131 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+No external dataset is involved; every array is generated from a fixed seed
+so the GPU engine and the CPU oracle see identical int32 columns.
+
+* ``single_literal``  -- one candidate literal over a 16M x 4 binding set
+  (10% positive) and a 4M-tuple relation r(A, B) with A uniform over
+  [0, 1M) (or Zipf s=1.1); the literal binds binding column 2 to A.
+* ``batched_step``    -- one refinement step: a 32M x 6 binding set (10%
+  positive, uniform over a 2M domain), 32 relations of arity 1-3 with
+  log-uniform tuple counts in [1K, 8M] and Zipf s=1.1 keys over the 2M
+  domain, and 256 candidate literals with random bound/unbound arguments.
+
+Binding columns are uniform over the key domain, which keeps every count
+below 2^31 (the reference counts in int32).  Zipf keys are drawn by inverse
+CDF of P(k) ~ k^-s over k = 1..D followed by a seeded permutation of the
+domain, so frequent keys are scattered over the value range.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import List
+
+import numpy as np
+
+from .engine import Literal
+
+
+class Zipf:
+    """Finite-domain Zipf sampler: values in [0, domain)."""
+
+    def __init__(self, domain: int, s: float, rng: np.random.Generator):
+        k = np.arange(1, domain + 1, dtype=np.float64)
+        w = k ** (-s)
+        self.cdf = np.cumsum(w)
+        self.cdf /= self.cdf[-1]
+        self.perm = rng.permutation(domain).astype(np.int32)
+
+    def sample(self, n: int, rng: np.random.Generator) -> np.ndarray:
+        u = rng.random(n)
+        idx = np.searchsorted(self.cdf, u, side="left")
+        np.minimum(idx, len(self.cdf) - 1, out=idx)
+        return self.perm[idx]
+
+
+@dataclass
+class Workload:
+    name: str
+    binding_columns: List[np.ndarray]
+    num_positive: int
+    relations: List[List[np.ndarray]]   # relation id = index
+    literals: List[Literal]
+    domain: int
+
+    @property
+    def num_bindings(self) -> int:
+        return len(self.binding_columns[0])
+
+    def relation_tuples(self) -> int:
+        return sum(len(r[0]) for r in self.relations)
+
+
+def uniform_bindings(n: int, ncols: int, domain: int, rng) -> List[np.ndarray]:
+    return [rng.integers(0, domain, n, dtype=np.int32) for _ in range(ncols)]
+
+
+def single_literal(n_bindings: int = 16_000_000, n_relation: int = 4_000_000,
+                   domain: int = 1_000_000, zipf: bool = False, seed: int = 2) -> Workload:
+    rng = np.random.default_rng(seed)
+    B = uniform_bindings(n_bindings, 4, domain, rng)
+    if zipf:
+        A = Zipf(domain, 1.1, rng).sample(n_relation, rng)
+    else:
+        A = rng.integers(0, domain, n_relation, dtype=np.int32)
+    Bcol = rng.integers(0, domain, n_relation, dtype=np.int32)
+    lit = Literal(0, (2, -1), 0)
+    return Workload("single_literal" + ("_zipf" if zipf else ""), B, n_bindings // 10, [[A, Bcol]],
+                    [lit], domain)
+
+
+def random_literals(num: int, relations, ncols: int, rng) -> List[Literal]:
+    """Random relation, random bound/unbound arguments with at least one bound
+    argument (learner/CandidateLiteralEnumerator.cpp:75,151 never emits an
+    all-unbound literal); bound arguments get random clause variables.  All
+    arguments share one type, so the join key is the first bound argument."""
+    out = []
+    for _ in range(num):
+        rid = int(rng.integers(0, len(relations)))
+        arity = len(relations[rid])
+        while True:
+            bound = rng.random(arity) < 0.5
+            if bound.any():
+                break
+        vars_ = tuple(int(rng.integers(0, ncols)) if b else -1 for b in bound)
+        out.append(Literal(rid, vars_))
+    return out
+
+
+def batched_step(n_bindings: int = 32_000_000, ncols: int = 6, num_relations: int = 32,
+                 min_tuples: int = 1_000, max_tuples: int = 8_000_000, num_literals: int = 256,
+                 domain: int = 2_000_000, seed: int = 3) -> Workload:
+    rng = np.random.default_rng(seed)
+    B = uniform_bindings(n_bindings, ncols, domain, rng)
+    relations = []
+    for _ in range(num_relations):
+        arity = int(rng.integers(1, 4))
+        n = int(np.exp(rng.uniform(np.log(min_tuples), np.log(max_tuples))))
+        z = Zipf(domain, 1.1, rng)
+        relations.append([z.sample(n, rng) for _ in range(arity)])
+    lits = random_literals(num_literals, relations, ncols, rng)
+    return Workload("batched_step", B, n_bindings // 10, relations, lits, domain)
+
+
+def small_random(seed: int, n_bindings: int = 3000, ncols: int = 4, num_relations: int = 5,
+                 max_tuples: int = 2000, num_literals: int = 40, domain: int = 300,
+                 zipf: bool = True) -> Workload:
+    """Small mixed case for parity tests (runs through the oracle in ms)."""
+    rng = np.random.default_rng(seed)
+    B = uniform_bindings(n_bindings, ncols, domain, rng)
+    relations = []
+    for _ in range(num_relations):
+        arity = int(rng.integers(1, 4))
+        n = int(rng.integers(1, max_tuples + 1))
+        if zipf:
+            z = Zipf(domain, 1.1, rng)
+            relations.append([z.sample(n, rng) for _ in range(arity)])
+        else:
+            relations.append([rng.integers(0, domain, n, dtype=np.int32) for _ in range(arity)])
+    lits = random_literals(num_literals, relations, ncols, rng)
+    P = int(rng.integers(0, n_bindings + 1))
+    return Workload(f"small_random_{seed}", B, P, relations, lits, domain)
