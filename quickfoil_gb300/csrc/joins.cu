@@ -1,22 +1,363 @@
 // joins.cu -- semi-joins and the label-aware binding-set extension.
+//
+// Both rest on a device key set: the distinct key tuples of one side in an
+// open-addressing table whose slots hold the row that first claimed the
+// tuple (atomicCAS), every row of that side mapping to that representative.
+//
+// LeftSemiJoin / RightSemiJoin (operations/LeftSemiJoin.hpp:55-141,
+// operations/RightSemiJoin.hpp:44-82) only need membership: the rows of the
+// other side look their tuple up and a warp turns 32 answers into one 32-bit
+// word with __ballot_sync.  Two consecutive words form one 64-bit block of
+// the reference's BitVector (dynamic_bitset<unsigned long>, little-endian
+// bit order), so the output is byte-identical; bits past the last row stay
+// zero as the reference requires (utility/BitVectorBuilder.hpp:46-54).
+//
+// CreateLabelAwareBindingTables (operations/MultiColumnHashJoin.cpp:117-256)
+// must also reproduce the row order.  In the reference every probe row emits
+// its matches in chain order, and a chain built by head insertion lists
+// equal-key build rows in descending row order (MultiColumnHashJoin.cpp:
+// 496-528, BuildHashTable.cpp:97-125).  Here the build rows are sorted
+// stably by representative, each probe row counts its matches, an exclusive
+// scan gives every probe row its output offset, and the probe row writes its
+// matches walking its build segment from the end.  The side that is built on
+// follows the reference: the binding set when both label sides are smaller
+// than the relation (CollaborateJoin, :172-207), else the relation (:208-250).
+#include <cstring>
+
 #include "qfg_common.cuh"
+
+namespace qfg {
+
+namespace {
+
+struct KeyCols {
+  const int32_t* c[QFG_MAX_ARITY];
+  int nk;
+};
+
+__device__ __forceinline__ uint32_t keys_hash(const KeyCols& k, int64_t r) {
+  uint32_t h = mix32((uint32_t)k.c[0][r]);
+  for (int q = 1; q < k.nk; ++q) h = mix32(h + 0x9e3779b9u + (uint32_t)k.c[q][r]);
+  return h;
+}
+
+__device__ __forceinline__ bool keys_eq(const KeyCols& a, int64_t x, const KeyCols& b, int64_t y) {
+  for (int q = 0; q < a.nk; ++q)
+    if (a.c[q][x] != b.c[q][y]) return false;
+  return true;
+}
+
+__global__ void keyset_insert_kernel(KeyCols build, int64_t n, int32_t* __restrict__ owner,
+                                     uint32_t mask, int32_t* __restrict__ rep) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t slot = keys_hash(build, r) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+      const int32_t o = atomicCAS(&owner[slot], -1, (int32_t)r);
+      if (o == -1) {
+        if (rep != nullptr) rep[r] = (int32_t)r;
+        break;
+      }
+      if (keys_eq(build, o, build, r)) {
+        if (rep != nullptr) rep[r] = o;
+        break;
+      }
+      slot = (slot + 1) & mask;
+    }
+  }
+}
+
+__device__ __forceinline__ int32_t keyset_find(const KeyCols& build, const int32_t* __restrict__ owner,
+                                               uint32_t mask, const KeyCols& probe, int64_t i) {
+  uint32_t slot = keys_hash(probe, i) & mask;
+  for (uint32_t p = 0; p <= mask; ++p) {
+    const int32_t o = owner[slot];
+    if (o < 0) return -1;
+    if (keys_eq(build, o, probe, i)) return o;
+    slot = (slot + 1) & mask;
+  }
+  return -1;
+}
+
+__global__ void semijoin_bits_kernel(KeyCols build, const int32_t* __restrict__ owner, uint32_t mask,
+                                     KeyCols probe, int64_t n, uint32_t* __restrict__ words,
+                                     int64_t nwords, unsigned long long* __restrict__ ones) {
+  const int64_t warps_total = (int64_t)gridDim.x * blockDim.x / 32;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = lane_id();
+  for (int64_t w = gw; w < nwords; w += warps_total) {
+    const int64_t i = w * 32 + lane;
+    const bool hit = i < n && keyset_find(build, owner, mask, probe, i) >= 0;
+    const unsigned ball = __ballot_sync(kFullMask, hit);
+    if (lane == 0) {
+      words[w] = ball;
+      if (ball != 0u) atomicAdd(ones, (unsigned long long)__popc(ball));
+    }
+  }
+}
+
+// After a stable sort of build rows by representative: first and last
+// sorted position of every representative's segment.
+__global__ void segments_kernel(const uint32_t* __restrict__ skey, int64_t n,
+                                int32_t* __restrict__ seg_first, int32_t* __restrict__ seg_last) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t r = skey[s];
+    if (s == 0 || skey[s - 1] != r) seg_first[r] = (int32_t)s;
+    if (s == n - 1 || skey[s + 1] != r) seg_last[r] = (int32_t)s;
+  }
+}
+
+__global__ void match_count_kernel(KeyCols build, const int32_t* __restrict__ owner, uint32_t mask,
+                                   KeyCols probe, int64_t n, const int32_t* __restrict__ seg_first,
+                                   const int32_t* __restrict__ seg_last, int32_t* __restrict__ prep,
+                                   uint32_t* __restrict__ cnt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t r = keyset_find(build, owner, mask, probe, i);
+    prep[i] = r;
+    cnt[i] = r < 0 ? 0u : (uint32_t)(seg_last[r] - seg_first[r] + 1);
+  }
+}
+
+struct ExtendArgs {
+  const int32_t* const* bind_cols;  // nc device pointers (full binding set)
+  int nc;
+  const int32_t* unbound[QFG_MAX_ARITY];  // relation columns of the unbound arguments
+  int nu;
+  int64_t label_lo;        // first binding row of this label
+  int relation_is_probe;   // probe rows are relation rows (else binding rows)
+  int64_t out_rows;        // rows of every output column
+  int64_t out_base;        // first output row of this label
+  int32_t* out;            // (nc + nu) columns of out_rows
+};
+
+__global__ void extend_write_kernel(ExtendArgs a, int64_t n_probe, const int32_t* __restrict__ prep,
+                                    const uint32_t* __restrict__ pos,
+                                    const int32_t* __restrict__ seg_first,
+                                    const int32_t* __restrict__ seg_last,
+                                    const int32_t* __restrict__ sorted_rows) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_probe;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t r = prep[i];
+    if (r < 0) continue;
+    int64_t o = a.out_base + pos[i];
+    // The build segment in descending row order = the reference's chain order.
+    for (int32_t s = seg_last[r]; s >= seg_first[r]; --s, ++o) {
+      const int32_t brow = sorted_rows[s];
+      const int64_t b = a.label_lo + (a.relation_is_probe ? (int64_t)brow : i);
+      const int64_t rr = a.relation_is_probe ? i : (int64_t)brow;
+      for (int c = 0; c < a.nc; ++c) a.out[(int64_t)c * a.out_rows + o] = a.bind_cols[c][b];
+      for (int u = 0; u < a.nu; ++u) a.out[(int64_t)(a.nc + u) * a.out_rows + o] = a.unbound[u][rr];
+    }
+  }
+}
+
+unsigned rows_grid(Ctx* ctx, int64_t n) {
+  const int64_t blocks = (n + 255) / 256;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)ctx->num_sms * 8));
+}
+
+uint32_t table_mask(int64_t n) {
+  uint32_t cap = 64;
+  while (cap < (uint64_t)(2 * n)) cap <<= 1;
+  return cap - 1;
+}
+
+int make_keycols(Ctx* ctx, const int32_t* const* host_ptrs, int nk, KeyCols* out) {
+  if (nk < 1 || nk > QFG_MAX_ARITY || host_ptrs == nullptr)
+    return set_error(ctx, QFG_ERR_INVALID, "key column count must be in [1, 8]");
+  out->nk = nk;
+  for (int q = 0; q < nk; ++q) out->c[q] = host_ptrs[q];
+  return QFG_OK;
+}
+
+int semijoin(Ctx* ctx, const KeyCols& set_side, int64_t n_set, const KeyCols& bit_side,
+             int64_t n_bits, uint64_t* d_bits, int64_t* num_ones) {
+  const int64_t nwords = 2 * ((n_bits + 63) / 64);
+  QFG_TRY(ctx->scratch[kScrTmpC].reserve(ctx, sizeof(unsigned long long)));
+  unsigned long long* ones = ctx->scratch[kScrTmpC].as<unsigned long long>();
+  QFG_CUDA(ctx, cudaMemsetAsync(ones, 0, sizeof(unsigned long long), ctx->stream));
+  if (n_set == 0 || n_bits == 0) {
+    if (nwords > 0)
+      QFG_CUDA(ctx, cudaMemsetAsync(d_bits, 0, sizeof(uint32_t) * nwords, ctx->stream));
+  } else {
+    const uint32_t mask = table_mask(n_set);
+    QFG_TRY(ctx->scratch[kScrJoin].reserve(ctx, sizeof(int32_t) * ((size_t)mask + 1)));
+    int32_t* owner = ctx->scratch[kScrJoin].as<int32_t>();
+    QFG_CUDA(ctx, cudaMemsetAsync(owner, 0xff, sizeof(int32_t) * ((size_t)mask + 1), ctx->stream));
+    keyset_insert_kernel<<<rows_grid(ctx, n_set), 256, 0, ctx->stream>>>(set_side, n_set, owner,
+                                                                         mask, nullptr);
+    QFG_LAUNCHED(ctx);
+    const unsigned grid = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((nwords + 7) / 8, (int64_t)ctx->num_sms * 8));
+    semijoin_bits_kernel<<<grid, 256, 0, ctx->stream>>>(set_side, owner, mask, bit_side, n_bits,
+                                                        reinterpret_cast<uint32_t*>(d_bits), nwords,
+                                                        ones);
+    QFG_LAUNCHED(ctx);
+  }
+  unsigned long long h = 0;
+  QFG_CUDA(ctx, cudaMemcpyAsync(&h, ones, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (num_ones != nullptr) *num_ones = (int64_t)h;
+  return QFG_OK;
+}
+
+// One label of the extension: joins `probe` rows against `build` rows and
+// writes the matches in the reference's order at output rows
+// [out_base, out_base + expected).
+int extend_label(Ctx* ctx, const KeyCols& build, int64_t n_build, const KeyCols& probe,
+                 int64_t n_probe, int64_t expected, ExtendArgs args) {
+  if (n_build == 0 || n_probe == 0) {
+    return expected == 0 ? QFG_OK
+                         : set_error(ctx, QFG_ERR_MISMATCH, "extension produced 0 rows for a label");
+  }
+  const uint32_t mask = table_mask(n_build);
+  const size_t cap = (size_t)mask + 1;
+  QFG_TRY(ctx->scratch[kScrJoin].reserve(ctx, sizeof(int32_t) * (cap + 3 * (size_t)n_build)));
+  int32_t* owner = ctx->scratch[kScrJoin].as<int32_t>();
+  int32_t* rep = owner + cap;
+  int32_t* seg_first = rep + n_build;
+  int32_t* seg_last = seg_first + n_build;
+  QFG_CUDA(ctx, cudaMemsetAsync(owner, 0xff, sizeof(int32_t) * cap, ctx->stream));
+  keyset_insert_kernel<<<rows_grid(ctx, n_build), 256, 0, ctx->stream>>>(build, n_build, owner,
+                                                                         mask, rep);
+  QFG_LAUNCHED(ctx);
+  QFG_TRY(ctx->scratch[kScrSortA].reserve(ctx, 2 * sizeof(uint32_t) * (size_t)n_build));
+  QFG_TRY(ctx->scratch[kScrSortB].reserve(ctx, 2 * sizeof(uint32_t) * (size_t)n_build));
+  uint32_t* k0 = ctx->scratch[kScrSortA].as<uint32_t>();
+  int32_t* p0 = reinterpret_cast<int32_t*>(k0 + n_build);
+  uint32_t* k1 = ctx->scratch[kScrSortB].as<uint32_t>();
+  int32_t* p1 = reinterpret_cast<int32_t*>(k1 + n_build);
+  QFG_CUDA(ctx, cudaMemcpyAsync(k0, rep, sizeof(int32_t) * (size_t)n_build,
+                                cudaMemcpyDeviceToDevice, ctx->stream));
+  int bits = 1;
+  while (bits < 31 && ((int64_t)1 << bits) < n_build) ++bits;
+  uint32_t* skey;
+  int32_t* srow;
+  QFG_TRY(sort_pairs_u32(ctx, k0, p0, k1, p1, n_build, bits, &skey, &srow));
+  segments_kernel<<<rows_grid(ctx, n_build), 256, 0, ctx->stream>>>(skey, n_build, seg_first,
+                                                                    seg_last);
+  QFG_LAUNCHED(ctx);
+  QFG_TRY(ctx->scratch[kScrJoin2].reserve(ctx, sizeof(int32_t) * (2 * (size_t)n_probe + 2)));
+  int32_t* prep = ctx->scratch[kScrJoin2].as<int32_t>();
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(prep + n_probe);
+  uint32_t* total = cnt + n_probe;
+  match_count_kernel<<<rows_grid(ctx, n_probe), 256, 0, ctx->stream>>>(
+      build, owner, mask, probe, n_probe, seg_first, seg_last, prep, cnt);
+  QFG_LAUNCHED(ctx);
+  QFG_TRY(exclusive_scan_u32(ctx, cnt, cnt, n_probe, total));
+  uint32_t produced = 0;
+  QFG_CUDA(ctx, cudaMemcpyAsync(&produced, total, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if ((int64_t)produced != expected)
+    return set_error(ctx, QFG_ERR_MISMATCH,
+                     "extension produced " + std::to_string(produced) + " rows for a label, " +
+                         std::to_string(expected) + " announced");
+  extend_write_kernel<<<rows_grid(ctx, n_probe), 256, 0, ctx->stream>>>(
+      args, n_probe, prep, cnt, seg_first, seg_last, srow);
+  QFG_LAUNCHED(ctx);
+  // The next label reuses (and may regrow) the same scratch.
+  QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return QFG_OK;
+}
+
+}  // namespace
+
+}  // namespace qfg
 
 using namespace qfg;
 
-extern "C" int qfg_left_semijoin(qfg_ctx* c, const int32_t* const*, int64_t, const int32_t* const*,
-                                 int64_t, int32_t, uint64_t*, int64_t*) {
-  if (c == nullptr) return QFG_ERR_INVALID;
-  return set_error(&c->impl, QFG_ERR_INVALID, "qfg_left_semijoin: not available in this build");
+extern "C" int qfg_extend_bindings(qfg_ctx* c, const qfg_bindings* b, const qfg_literal* lit,
+                                   int64_t num_out_positive, int64_t num_out_negative,
+                                   qfg_bindings** out) {
+  if (c == nullptr || b == nullptr || lit == nullptr || out == nullptr) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  *out = nullptr;
+  Relation* rel = nullptr;
+  QFG_TRY(find_relation(ctx, lit->relation_id, &rel));
+  if (lit->num_args != rel->num_columns || num_out_positive < 0 || num_out_negative < 0 ||
+      num_out_positive + num_out_negative > INT32_MAX)
+    return set_error(ctx, QFG_ERR_INVALID, "qfg_extend_bindings: invalid literal or counts");
+  KeyCols rel_keys, pos_keys, neg_keys;
+  rel_keys.nk = pos_keys.nk = neg_keys.nk = 0;
+  ExtendArgs args;
+  memset(&args, 0, sizeof(args));
+  const int64_t P = b->num_positive, N = b->num_negative, R = rel->num_tuples;
+  for (int k = 0; k < lit->num_args; ++k) {
+    const int v = lit->vars[k];
+    if (v >= b->num_columns || v < -1)
+      return set_error(ctx, QFG_ERR_INVALID, "qfg_extend_bindings: variable out of range");
+    if (v >= 0) {
+      rel_keys.c[rel_keys.nk++] = rel->columns[k];
+      pos_keys.c[pos_keys.nk++] = b->columns[v];
+      neg_keys.c[neg_keys.nk++] = b->columns[v] + P;
+    } else {
+      args.unbound[args.nu++] = rel->columns[k];
+    }
+  }
+  if (rel_keys.nk == 0)
+    return set_error(ctx, QFG_ERR_INVALID, "qfg_extend_bindings: literal has no bound argument");
+  const int nc = b->num_columns;
+  const int64_t total = num_out_positive + num_out_negative;
+  auto nb = std::make_unique<qfg_bindings>();
+  nb->num_columns = nc + args.nu;
+  nb->num_positive = num_out_positive;
+  nb->num_negative = num_out_negative;
+  QFG_TRY(nb->storage.reserve(ctx, sizeof(int32_t) * (size_t)nb->num_columns *
+                                       (size_t)std::max<int64_t>(total, 1)));
+  nb->columns.resize(nb->num_columns);
+  for (int i = 0; i < nb->num_columns; ++i) nb->columns[i] = nb->storage.as<int32_t>() + i * total;
+  // Device copy of the binding column pointers (any number of columns).
+  QFG_TRY(ctx->scratch[kScrTmpB].reserve(ctx, sizeof(const int32_t*) * (size_t)nc));
+  const int32_t** dcols = ctx->scratch[kScrTmpB].as<const int32_t*>();
+  QFG_TRY(upload_small(ctx, dcols, b->columns.data(), sizeof(const int32_t*) * (size_t)nc));
+  args.bind_cols = dcols;
+  args.nc = nc;
+  args.out_rows = total;
+  args.out = nb->storage.as<int32_t>();
+  args.relation_is_probe = (P < R && N < R) ? 1 : 0;
+  for (int label = 0; label < 2; ++label) {
+    const KeyCols& bind_keys = label == 0 ? pos_keys : neg_keys;
+    const int64_t n_label = label == 0 ? P : N;
+    args.label_lo = label == 0 ? 0 : P;
+    args.out_base = label == 0 ? 0 : num_out_positive;
+    const int64_t expected = label == 0 ? num_out_positive : num_out_negative;
+    if (args.relation_is_probe)
+      QFG_TRY(extend_label(ctx, bind_keys, n_label, rel_keys, R, expected, args));
+    else
+      QFG_TRY(extend_label(ctx, rel_keys, R, bind_keys, n_label, expected, args));
+  }
+  QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = nb.release();
+  return QFG_OK;
 }
 
-extern "C" int qfg_right_semijoin(qfg_ctx* c, const int32_t* const*, int64_t, const int32_t* const*,
-                                  int64_t, int32_t, uint64_t*, int64_t*) {
+extern "C" int qfg_left_semijoin(qfg_ctx* c, const int32_t* const* d_probe_keys, int64_t num_probe,
+                                 const int32_t* const* d_build_keys, int64_t num_build,
+                                 int32_t num_keys, uint64_t* d_bits, int64_t* num_ones) {
   if (c == nullptr) return QFG_ERR_INVALID;
-  return set_error(&c->impl, QFG_ERR_INVALID, "qfg_right_semijoin: not available in this build");
+  Ctx* ctx = &c->impl;
+  if (num_probe < 0 || num_build < 0 || num_probe > INT32_MAX || num_build > INT32_MAX ||
+      (num_probe > 0 && d_bits == nullptr))
+    return set_error(ctx, QFG_ERR_INVALID, "qfg_left_semijoin: invalid arguments");
+  KeyCols probe, build;
+  QFG_TRY(make_keycols(ctx, d_probe_keys, num_keys, &probe));
+  QFG_TRY(make_keycols(ctx, d_build_keys, num_keys, &build));
+  return semijoin(ctx, build, num_build, probe, num_probe, d_bits, num_ones);
 }
 
-extern "C" int qfg_extend_bindings(qfg_ctx* c, const qfg_bindings*, const qfg_literal*, int64_t,
-                                   int64_t, qfg_bindings**) {
+extern "C" int qfg_right_semijoin(qfg_ctx* c, const int32_t* const* d_probe_keys, int64_t num_probe,
+                                  const int32_t* const* d_build_keys, int64_t num_build,
+                                  int32_t num_keys, uint64_t* d_bits, int64_t* num_ones) {
   if (c == nullptr) return QFG_ERR_INVALID;
-  return set_error(&c->impl, QFG_ERR_INVALID, "qfg_extend_bindings: not available in this build");
+  Ctx* ctx = &c->impl;
+  if (num_probe < 0 || num_build < 0 || num_probe > INT32_MAX || num_build > INT32_MAX ||
+      (num_build > 0 && d_bits == nullptr))
+    return set_error(ctx, QFG_ERR_INVALID, "qfg_right_semijoin: invalid arguments");
+  KeyCols probe, build;
+  QFG_TRY(make_keycols(ctx, d_probe_keys, num_keys, &probe));
+  QFG_TRY(make_keycols(ctx, d_build_keys, num_keys, &build));
+  return semijoin(ctx, probe, num_probe, build, num_build, d_bits, num_ones);
 }

@@ -286,6 +286,11 @@ unsigned grid_for(Ctx* ctx, int64_t n, int threads) {
 
 }  // namespace
 
+int sort_pairs_u32(Ctx* ctx, uint32_t* k0, int32_t* p0, uint32_t* k1, int32_t* p1, int64_t n,
+                   int key_bits, uint32_t** k_out, int32_t** p_out) {
+  return stable_sort_pairs(ctx, k0, p0, k1, p1, n, key_bits, k_out, p_out);
+}
+
 int radix_partition_ref(Ctx* ctx, const int32_t* values, int64_t n, int bits, int32_t* out_tuples,
                         int64_t* out_offsets) {
   if (n == 0) {

@@ -217,6 +217,12 @@ int exclusive_scan_u32(Ctx* ctx, const uint32_t* in, uint32_t* out, int64_t n,
 int radix_partition_ref(Ctx* ctx, const int32_t* values, int64_t n, int bits,
                         int32_t* out_tuples, int64_t* out_offsets);
 
+// Stable LSD sort of n (key < 2^key_bits, payload) pairs; the first pass
+// takes the row index as payload.  Buffers ping-pong; the result is returned
+// through k_out / p_out.
+int sort_pairs_u32(Ctx* ctx, uint32_t* k0, int32_t* p0, uint32_t* k1, int32_t* p1, int64_t n,
+                   int key_bits, uint32_t** k_out, int32_t** p_out);
+
 // Cached reference-layout partitions of a relation column.
 int relation_partitions(Ctx* ctx, Relation* rel, int column, int bits,
                         PartitionedColumn** out);

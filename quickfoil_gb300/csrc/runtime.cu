@@ -42,6 +42,8 @@ DevBuf& DevBuf::operator=(DevBuf&& o) noexcept {
 
 void DevBuf::release() {
   if (ptr_ != nullptr) {
+    // Work queued on the context stream may still read this buffer.
+    if (ctx_ != nullptr) cudaStreamSynchronize(ctx_->stream);
     cudaFree(ptr_);
     if (ctx_ != nullptr) ctx_->used -= (int64_t)bytes_;
   }
