@@ -50,6 +50,8 @@ def parse_args():
                     help="literals in the CPU-baseline sample (0 = automatic)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-per-literal", action="store_true")
+    ap.add_argument("--eval-bits", type=int, default=0,
+                    help="binding partition bits of the batched engine (0 = autotuned)")
     return ap.parse_args()
 
 
@@ -211,6 +213,8 @@ def run_gb300(args):
     from quickfoil_gb300 import _capi as C
     w = make_workload(args, rank)
     eng = Engine(local_rank)
+    if args.eval_bits:
+        eng.set_option(C.QFG_OPT_EVAL_BITS, args.eval_bits)
     stream = torch.cuda.current_stream(dev)
     eng.set_stream(stream.cuda_stream)
     for rid, cols in enumerate(w.relations):

@@ -29,6 +29,7 @@
 // range through it.  Counts are reduced with warp shuffles into per-CTA
 // int64 accumulators and flushed to global memory once per CTA.
 #include <algorithm>
+#include <cstring>
 #include <unordered_map>
 
 #include "eval_common.cuh"
@@ -37,12 +38,19 @@ namespace qfg {
 
 namespace {
 
-constexpr int kTile = 2560;            // binding rows per shared-memory tile
-constexpr int kSlots = 4096;           // key-table slots (power of two > kTile)
-constexpr int kEvalThreads = 1024;
+constexpr int kTile = 1536;            // binding rows per shared-memory tile
+constexpr int kSlots = 2048;           // key-table slots (power of two > kTile)
+constexpr int kEvalThreads = 256;
 constexpr int kGroupCols = QFG_MAX_ARITY;  // join column + up to 7 atom columns
 constexpr int kMaxLitsPerLaunch = 512;
-constexpr int kMaxPartitionBits = 14;
+constexpr int kMaxGroupLits = kEvalThreads;  // one thread per literal in the per-item prefix
+constexpr int kRound = 2048;           // rows staged per partition round
+constexpr int kPartThreads = 512;
+constexpr int kMaxCoarseBits = 7;      // pass 1 fan-out: 2 << 7 = 256 bins
+constexpr int kMaxSubBits = 9;         // pass 2 fan-out: up to 512 sub-bins
+constexpr int kMaxPartitionBits = kMaxCoarseBits + kMaxSubBits;
+static_assert(kMaxPartitionBits <= kRelPartitionBits, "relation bins must refine binding bins");
+static_assert(kSlots % kEvalThreads == 0 && kSlots > kTile, "slot table shape");
 
 // ----------------------------------------------------------------------------
 // Relation key tables.
@@ -115,72 +123,317 @@ unsigned grid_for_rows(Ctx* ctx, int64_t n, int threads) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)ctx->num_sms * 8));
 }
 
+// Exclusive scan of one value per thread (blockDim.x <= 1024); every thread
+// must call it.  *total receives the sum.
+__device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+  const int lane = lane_id(), warp = warp_id();
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFullMask, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    const uint32_t t = lane < nw ? s_warp[lane] : 0u;
+    uint32_t s = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFullMask, s, o);
+      if (lane >= o) s += y;
+    }
+    s_warp[lane] = s - t;
+    if (lane == 31) *total = s;
+  }
+  __syncthreads();
+  const uint32_t r = x - v + s_warp[warp];
+  __syncthreads();
+  return r;
+}
+
 // ----------------------------------------------------------------------------
 // Binding-set partitioning per group.
+//
+// Partition p of a group holds the binding rows whose join key has
+// top_bits(mix32(key), bits) == p, positives and negatives in two separate
+// segments.  A fan-out of 2^15 partitions is far too wide for coalesced
+// stores, so the scatter runs in two passes of modest fan-out: pass 1 sends
+// rows to (top cbits bits, label) coarse bins, pass 2 splits every coarse
+// bin, inside its own range, into its 2^(bits - cbits) partitions.  Both
+// passes stage rounds of kRound rows in shared memory, counting-sort them by
+// destination bin there and write each bin's run with consecutive threads on
+// consecutive addresses.  A histogram pass counts the coarse bins per CTA
+// (one atomicAdd per bin and CTA gives the CTA its cursor); pass 2 counts its
+// own sub-bins, so no global fine histogram exists.  With bits <= 8 a single
+// pass writes the partitions directly.
 
 struct BPartArgs {
   const int32_t* cols[kGroupCols];  // cols[0] = join column
   int ncols;
   int64_t n, npos;
-  int bits;
-  uint32_t* tot;   // 2 << bits bin totals (zeroed)
-  uint32_t* base;  // gridDim.x * (2 << bits) per-CTA bases
-  int32_t* out;    // ncols SoA columns of n rows
+  int bits;                 // partition bits
+  int cbits;                // pass-1 bits (== bits: single pass)
+  uint32_t* p1_tot;         // 2 << cbits bin totals (zeroed)
+  uint32_t* p1_base;        // gridDim.x * (2 << cbits) per-CTA bases
 };
 
-__device__ __forceinline__ void cta_range(int64_t n, int64_t* r0, int64_t* r1) {
-  const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+// Rows [r0, r1) of this CTA; r0 is a multiple of 4 so that 16-byte loads
+// stay aligned when the column base pointers are.
+__device__ __forceinline__ void cta_range4(int64_t n, int64_t* r0, int64_t* r1) {
+  int64_t per = (n + gridDim.x - 1) / gridDim.x;
+  per = (per + 3) & ~int64_t(3);
   *r0 = min(n, (int64_t)blockIdx.x * per);
   *r1 = min(n, *r0 + per);
 }
 
-__device__ __forceinline__ uint32_t bind_bin(int32_t key, int bits, bool neg) {
-  return ((mix32((uint32_t)key) >> (32 - bits)) << 1) | (neg ? 1u : 0u);
+__device__ __forceinline__ uint32_t top_bits(int32_t key, int bits) {
+  return mix32((uint32_t)key) >> (32 - bits);
 }
 
-__global__ void __launch_bounds__(1024) bpart_hist_kernel(BPartArgs a) {
-  extern __shared__ uint32_t sh_bins[];
-  const int nbins = 2 << a.bits;
-  for (int i = threadIdx.x; i < nbins; i += blockDim.x) sh_bins[i] = 0;
+__device__ __forceinline__ int lane_of(const int4& v, int k) {
+  return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+}
+
+template <bool kVec>
+__global__ void __launch_bounds__(kPartThreads, 2) bpart_hist_kernel(BPartArgs a) {
+  __shared__ uint32_t p1[2 << (kMaxCoarseBits + 1)];
+  const int np1 = 2 << a.cbits;
+  for (int i = threadIdx.x; i < np1; i += blockDim.x) p1[i] = 0;
   __syncthreads();
   int64_t r0, r1;
-  cta_range(a.n, &r0, &r1);
+  cta_range4(a.n, &r0, &r1);
   const int32_t* __restrict__ key = a.cols[0];
-  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
-    atomicAdd(&sh_bins[bind_bin(key[r], a.bits, r >= a.npos)], 1u);
+  auto count = [&](int32_t k, int64_t r) {
+    atomicAdd(&p1[(top_bits(k, a.cbits) << 1) | (r >= a.npos ? 1u : 0u)], 1u);
+  };
+  int64_t rs = r0;
+  if (kVec) {
+    const int64_t nv = (r1 - r0) >> 2;
+    const int4* __restrict__ kv = reinterpret_cast<const int4*>(key + r0);
+    const int64_t step = blockDim.x;
+    int64_t v = threadIdx.x;
+    for (; v + step < nv; v += 2 * step) {
+      const int4 k0 = __ldg(kv + v), k1 = __ldg(kv + v + step);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) count(lane_of(k0, k), r0 + 4 * v + k);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) count(lane_of(k1, k), r0 + 4 * (v + step) + k);
+    }
+    if (v < nv) {
+      const int4 k0 = __ldg(kv + v);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) count(lane_of(k0, k), r0 + 4 * v + k);
+    }
+    rs = r0 + 4 * nv;
+  }
+  for (int64_t r = rs + threadIdx.x; r < r1; r += blockDim.x) count(key[r], r);
   __syncthreads();
-  for (int i = threadIdx.x; i < nbins; i += blockDim.x) {
-    const uint32_t c = sh_bins[i];
-    a.base[(int64_t)blockIdx.x * nbins + i] = c ? atomicAdd(&a.tot[i], c) : 0u;
+  for (int i = threadIdx.x; i < np1; i += blockDim.x) {
+    const uint32_t c = p1[i];
+    a.p1_base[(int64_t)blockIdx.x * np1 + i] = c ? atomicAdd(&a.p1_tot[i], c) : 0u;
   }
 }
 
-__global__ void __launch_bounds__(1024)
-bpart_scatter_kernel(BPartArgs a, const uint32_t* __restrict__ start) {
-  extern __shared__ uint32_t sh_cur[];
-  const int nbins = 2 << a.bits;
-  for (int i = threadIdx.x; i < nbins; i += blockDim.x)
-    sh_cur[i] = start[i] + a.base[(int64_t)blockIdx.x * nbins + i];
+// Shared-memory staging for one round of up to kRound rows of ncols columns.
+struct RoundSmem {
+  int32_t* rows;      // ncols * kRound
+  uint16_t* bin;      // kRound
+  uint16_t* rank;     // kRound
+  uint16_t* perm;     // kRound
+  uint32_t* lcount;   // nbins
+  uint32_t* lstart;   // nbins
+  uint32_t* cursor;   // nbins (global output cursor of each bin)
+};
+
+__device__ __forceinline__ RoundSmem carve_round(unsigned char* smem, int ncols, int nbins) {
+  RoundSmem S;
+  S.rows = reinterpret_cast<int32_t*>(smem);
+  S.bin = reinterpret_cast<uint16_t*>(S.rows + ncols * kRound);
+  S.rank = S.bin + kRound;
+  S.perm = S.rank + kRound;
+  S.lcount = reinterpret_cast<uint32_t*>(S.perm + kRound);
+  S.lstart = S.lcount + nbins;
+  S.cursor = S.lstart + nbins;
+  return S;
+}
+
+size_t round_smem_bytes(int ncols, int nbins) {
+  return sizeof(int32_t) * (size_t)ncols * kRound + 3 * sizeof(uint16_t) * kRound +
+         3 * sizeof(uint32_t) * (size_t)nbins;
+}
+
+// Counting-sorts the staged round by bin (nbins <= blockDim.x; lcount zero on
+// entry) and writes it out: sorted position k goes to cursor[bin] +
+// (k - lstart[bin]), so the threads writing one bin's run write consecutive
+// addresses.
+__device__ __forceinline__ void write_round(const RoundSmem& S, int nt, int nbins, int ncols,
+                                            int32_t* __restrict__ out, int64_t out_stride,
+                                            uint32_t* s_warp, uint32_t* s_total) {
+  for (int i = threadIdx.x; i < nt; i += blockDim.x)
+    S.rank[i] = (uint16_t)atomicAdd(&S.lcount[S.bin[i]], 1u);
+  __syncthreads();
+  const uint32_t c = (int)threadIdx.x < nbins ? S.lcount[threadIdx.x] : 0u;
+  const uint32_t ex = block_scan_excl(c, s_warp, s_total);
+  if ((int)threadIdx.x < nbins) S.lstart[threadIdx.x] = ex;
+  __syncthreads();
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) S.perm[S.lstart[S.bin[i]] + S.rank[i]] = (uint16_t)i;
+  __syncthreads();
+  for (int k = threadIdx.x; k < nt; k += blockDim.x) {
+    const int i = S.perm[k];
+    const int b = S.bin[i];
+    const int64_t g = (int64_t)S.cursor[b] + (k - (int)S.lstart[b]);
+    for (int q = 0; q < ncols; ++q) out[(int64_t)q * out_stride + g] = S.rows[q * kRound + i];
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < nbins) {
+    S.cursor[threadIdx.x] += S.lcount[threadIdx.x];
+    S.lcount[threadIdx.x] = 0u;
+  }
+  __syncthreads();
+}
+
+// Stages rows [0, nt) of up to kGroupCols columns (column q starts at
+// src[q]) into S.rows.  All loads of a thread are issued before any store so
+// that they are in flight together.
+constexpr int kRowsPerThread = kRound / kPartThreads;
+
+__device__ __forceinline__ void load_round(const int32_t* const* src, int ncols, int nt,
+                                           int32_t* rows) {
+  int32_t v[kGroupCols][kRowsPerThread];
+#pragma unroll
+  for (int q = 0; q < kGroupCols; ++q) {
+    if (q < ncols) {
+#pragma unroll
+      for (int k = 0; k < kRowsPerThread; ++k) {
+        const int i = threadIdx.x + k * kPartThreads;
+        v[q][k] = i < nt ? __ldg(src[q] + i) : 0;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kGroupCols; ++q) {
+    if (q < ncols) {
+#pragma unroll
+      for (int k = 0; k < kRowsPerThread; ++k) {
+        const int i = threadIdx.x + k * kPartThreads;
+        if (i < nt) rows[q * kRound + i] = v[q][k];
+      }
+    }
+  }
+}
+
+// Pass 1: the CTA's chunk of the original columns into pass-1 bins.
+__global__ void __launch_bounds__(kPartThreads, 2)
+bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
+  const int np1 = 2 << a.cbits;
+  const RoundSmem S = carve_round(smem, a.ncols, np1);
+  for (int i = threadIdx.x; i < np1; i += blockDim.x) {
+    S.cursor[i] = p1_start[i] + a.p1_base[(int64_t)blockIdx.x * np1 + i];
+    S.lcount[i] = 0u;
+  }
   __syncthreads();
   int64_t r0, r1;
-  cta_range(a.n, &r0, &r1);
-  const int32_t* __restrict__ key = a.cols[0];
-  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-    const int32_t k = key[r];
-    const uint32_t pos = atomicAdd(&sh_cur[bind_bin(k, a.bits, r >= a.npos)], 1u);
-    a.out[pos] = k;
-    for (int c = 1; c < a.ncols; ++c) a.out[(int64_t)c * a.n + pos] = a.cols[c][r];
+  cta_range4(a.n, &r0, &r1);
+  for (int64_t rr = r0; rr < r1; rr += kRound) {
+    const int nt = (int)(r1 - rr < kRound ? r1 - rr : (int64_t)kRound);
+    {
+      const int32_t* src[kGroupCols];
+#pragma unroll
+      for (int q = 0; q < kGroupCols; ++q) src[q] = q < a.ncols ? a.cols[q] + rr : nullptr;
+      load_round(src, a.ncols, nt, S.rows);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nt; i += blockDim.x)
+      S.bin[i] = (uint16_t)((top_bits(S.rows[i], a.cbits) << 1) | (rr + i >= a.npos ? 1u : 0u));
+    __syncthreads();
+    write_round(S, nt, np1, a.ncols, out, a.n, s_warp, &s_total);
+  }
+}
+
+// Pass 2: CTA b splits pass-1 bin b = (hash prefix c, label) inside its own
+// range into sub-bins 0 .. 2^sbits - 1 and records where each starts:
+// fine_start[(b << sbits) + sub] (the last CTA also writes the end, n).
+__global__ void __launch_bounds__(kPartThreads, 2)
+bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, const int32_t* __restrict__ in,
+                   uint32_t* __restrict__ fine_start, int32_t* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
+  const int sbits = a.bits - a.cbits;
+  const int nsub = 1 << sbits;
+  const RoundSmem S = carve_round(smem, a.ncols, nsub);
+  const int b = blockIdx.x;
+  const int64_t r0 = p1_start[b], r1 = p1_start[b + 1];
+  for (int i = threadIdx.x; i < nsub; i += blockDim.x) S.lcount[i] = 0u;
+  __syncthreads();
+  {
+    // Eight independent key loads per thread per iteration.
+    const uint32_t mask = (uint32_t)(nsub - 1);
+    int64_t r = r0 + threadIdx.x;
+    for (; r + 7 * (int64_t)blockDim.x < r1; r += 8 * (int64_t)blockDim.x) {
+      int32_t k[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) k[j] = __ldg(in + r + j * (int64_t)blockDim.x);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) atomicAdd(&S.lcount[top_bits(k[j], a.bits) & mask], 1u);
+    }
+    for (; r < r1; r += blockDim.x) atomicAdd(&S.lcount[top_bits(__ldg(in + r), a.bits) & mask], 1u);
+  }
+  __syncthreads();
+  const uint32_t c = (int)threadIdx.x < nsub ? S.lcount[threadIdx.x] : 0u;
+  const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
+  if ((int)threadIdx.x < nsub) {
+    S.cursor[threadIdx.x] = (uint32_t)r0 + ex;
+    fine_start[((int64_t)b << sbits) + threadIdx.x] = (uint32_t)r0 + ex;
+    S.lcount[threadIdx.x] = 0u;
+  }
+  if (b == (int)gridDim.x - 1 && threadIdx.x == 0)
+    fine_start[(int64_t)gridDim.x << sbits] = (uint32_t)r1;
+  __syncthreads();
+  for (int64_t rr = r0; rr < r1; rr += kRound) {
+    const int nt = (int)(r1 - rr < kRound ? r1 - rr : (int64_t)kRound);
+    {
+      const int32_t* src[kGroupCols];
+#pragma unroll
+      for (int q = 0; q < kGroupCols; ++q) src[q] = q < a.ncols ? in + (int64_t)q * a.n + rr : nullptr;
+      load_round(src, a.ncols, nt, S.rows);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nt; i += blockDim.x)
+      S.bin[i] = (uint16_t)(top_bits(S.rows[i], a.bits) & (uint32_t)(nsub - 1));
+    __syncthreads();
+    write_round(S, nt, nsub, a.ncols, out, a.n, s_warp, &s_total);
   }
 }
 
 // ----------------------------------------------------------------------------
 // Persistent evaluation kernel.
+//
+// Work item = (group, partition).  The CTA gathers the partition's binding
+// rows (its positive and negative segments; join column + carried atom
+// columns) into shared memory, then builds a table of the distinct join
+// keys: 16-bit slot owners claimed with atomicCAS, per-slot row counts packed
+// as (positive count, negative count << 16), and, when the group has atom
+// literals, per-key row lists formed by an exclusive scan of the counts.
+// The group's literals' relation entries for the same partition range are
+// then processed as one flat index space (literal-major), so all threads stay
+// busy however few entries each literal has; per-literal counts are combined
+// with a segmented warp scan over lanes of equal literal and added once per
+// segment to per-CTA shared accumulators, flushed to global memory when the
+// CTA retires.  CTAs are small (256 threads) and three share an SM, so that
+// each barrier waits on few warps and one CTA's memory waits overlap the
+// others' shared-memory work.
 
 struct GroupDesc {
-  const int32_t* cols;    // ncols SoA columns of n rows, partitioned
+  const int32_t* cols;      // ncols SoA columns of n rows, partitioned
   int64_t n;
-  const uint32_t* start;  // (2 << bits) + 1 bin offsets
-  int bits, ncols;
+  const uint32_t* fstart;   // (2 << bits) + 1 segment starts
+  int bits, sbits, ncols;
   int lit_begin, lit_end;
   int has_atoms;
   int64_t item_begin;
@@ -188,12 +441,12 @@ struct GroupDesc {
 
 struct LitDesc {
   const int32_t* keys;       // nk SoA columns of `stride` entries
-  int64_t stride;
   const int32_t* mult;
   const uint32_t* offsets;   // (1 << kRelPartitionBits) + 1
+  int64_t stride;
   int nk;
-  int atom_col[QFG_MAX_ARITY];  // key q >= 1 is compared with group column atom_col[q]
   int out;                   // literal index in the caller's array
+  int8_t atom_col[QFG_MAX_ARITY];  // key q >= 1 is compared with group column atom_col[q]
 };
 
 struct EvalArgs {
@@ -201,30 +454,52 @@ struct EvalArgs {
   int num_groups;
   const LitDesc* lits;
   int num_lits;
+  int max_cols;
   int64_t total_items;
   unsigned int* work_counter;
   unsigned long long* counts;
 };
 
-size_t eval_smem_bytes(int num_lits) {
-  return sizeof(long long) * 4 * (size_t)num_lits + sizeof(int32_t) * kGroupCols * kTile +
-         sizeof(int32_t) * kSlots * 4 + sizeof(uint16_t) * 2 * kTile;
+size_t eval_smem_bytes(int num_lits, int max_cols) {
+  return sizeof(unsigned long long) * 4 * (size_t)num_lits +
+         sizeof(int32_t) * (size_t)max_cols * kTile + sizeof(uint32_t) * 2 * kSlots +
+         sizeof(uint32_t) * (2 * kMaxLitsPerLaunch + 2) + sizeof(uint16_t) * (kSlots + 2 * kTile);
 }
 
-__global__ void __launch_bounds__(kEvalThreads, 1) eval_batched_kernel(EvalArgs a) {
+// Inclusive scan restricted to runs of equal `seg` across consecutive lanes.
+__device__ __forceinline__ long long seg_scan(long long v, int seg) {
+  const int lane = lane_id();
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(kFullMask, v, o);
+    const int s = __shfl_up_sync(kFullMask, seg, o);
+    if (lane >= o && s == seg) v += y;
+  }
+  return v;
+}
+
+constexpr unsigned short kNoOwner = 0xffffu;
+
+__global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem);
   int32_t* scol = reinterpret_cast<int32_t*>(acc + 4 * a.num_lits);
-  int32_t* owner = scol + kGroupCols * kTile;
-  uint32_t* cntp = reinterpret_cast<uint32_t*>(owner + kSlots);
-  uint32_t* cntn = cntp + kSlots;
-  uint32_t* lend = cntn + kSlots;
-  uint16_t* rows = reinterpret_cast<uint16_t*>(lend + kSlots);
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(scol + a.max_cols * kTile);
+  uint32_t* lend = cnt + kSlots;
+  uint32_t* lstart = lend + kSlots;                 // kMaxLitsPerLaunch + 1
+  uint32_t* le0 = lstart + kMaxLitsPerLaunch + 1;   // kMaxLitsPerLaunch
+  unsigned short* owner = reinterpret_cast<unsigned short*>(le0 + kMaxLitsPerLaunch + 1);
+  uint16_t* rows = owner + kSlots;
   uint16_t* rslot = rows + kTile;
   __shared__ long long s_item;
   __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
 
   for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) acc[i] = 0ull;
+  for (int i = threadIdx.x; i < kSlots; i += blockDim.x) {
+    owner[i] = kNoOwner;
+    cnt[i] = 0u;
+  }
   __syncthreads();
 
   for (;;) {
@@ -235,34 +510,66 @@ __global__ void __launch_bounds__(kEvalThreads, 1) eval_batched_kernel(EvalArgs 
     int g = 0;
     while (g + 1 < a.num_groups && a.groups[g + 1].item_begin <= item) ++g;
     const GroupDesc G = a.groups[g];
-    const int p = (int)(item - G.item_begin);
-    const uint32_t b0 = G.start[2 * p], bm = G.start[2 * p + 1], b1 = G.start[2 * p + 2];
-    const int shift = kRelPartitionBits - G.bits;
-    const uint32_t q0 = (uint32_t)p << shift, q1 = (uint32_t)(p + 1) << shift;
+    const uint32_t p = (uint32_t)(item - G.item_begin);
+    const int s = G.sbits;
+    const uint32_t hc = p >> s, sub = p & ((1u << s) - 1u);
+    const uint32_t ip = ((2u * hc) << s) + sub, in_ = ((2u * hc + 1u) << s) + sub;
+    const uint32_t ps = G.fstart[ip], Pp = G.fstart[ip + 1] - ps;
+    const uint32_t ns = G.fstart[in_], Np = G.fstart[in_ + 1] - ns;
+    const uint32_t total = Pp + Np;
+    if (total == 0) {
+      __syncthreads();
+      continue;
+    }
+    const int rshift = kRelPartitionBits - G.bits;
+    const uint32_t q0 = p << rshift, q1 = (p + 1) << rshift;
+    const int m = G.lit_end - G.lit_begin;
 
-    for (uint32_t t0 = b0; t0 < b1; t0 += kTile) {
-      const int nt = (int)umin((uint32_t)kTile, b1 - t0);
-      const int npos = (int)umin((uint32_t)nt, bm > t0 ? bm - t0 : 0u);
-      for (int c = 0; c < G.ncols; ++c)
-        for (int i = threadIdx.x; i < nt; i += blockDim.x)
-          scol[c * kTile + i] = G.cols[(int64_t)c * G.n + t0 + i];
-      for (int i = threadIdx.x; i < kSlots; i += blockDim.x) {
-        owner[i] = -1;
-        cntp[i] = 0u;
-        cntn[i] = 0u;
+    // Entry ranges of the group's literals in this partition, flattened.
+    {
+      uint32_t c = 0;
+      if ((int)threadIdx.x < m) {
+        const LitDesc& d = a.lits[G.lit_begin + threadIdx.x];
+        const uint32_t e0 = __ldg(d.offsets + q0), e1 = __ldg(d.offsets + q1);
+        le0[threadIdx.x] = e0;
+        c = e1 - e0;
+      }
+      const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
+      if ((int)threadIdx.x < m) lstart[threadIdx.x] = ex;
+      if (threadIdx.x == 0) lstart[m] = s_total;
+      __syncthreads();
+    }
+    const uint32_t E = lstart[m];
+    if (E == 0) {
+      __syncthreads();
+      continue;
+    }
+
+    for (uint32_t t0 = 0; t0 < total; t0 += kTile) {
+      const int nt = (int)umin((uint32_t)kTile, total - t0);
+      const int npos = (int)umin((uint32_t)nt, Pp > t0 ? Pp - t0 : 0u);
+      for (int q = 0; q < G.ncols; ++q) {
+        const int32_t* __restrict__ src = G.cols + (int64_t)q * G.n;
+        int32_t* dst = scol + q * kTile;
+#pragma unroll 2
+        for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+          const uint32_t v = t0 + i;
+          dst[i] = __ldg(src + (v < Pp ? ps + v : ns + (v - Pp)));
+        }
       }
       __syncthreads();
-      // Distinct join keys of the tile with per-label row counts.
+      // Distinct join keys of the tile with per-label row counts (the table
+      // is all-empty here: zeroed at kernel start, reset after every tile).
       for (int i = threadIdx.x; i < nt; i += blockDim.x) {
         const int32_t key = scol[i];
         uint32_t slot = mix32((uint32_t)key) & (kSlots - 1);
         for (int probe = 0; probe < kSlots; ++probe) {
-          const int32_t o = atomicCAS(&owner[slot], -1, i);
-          if (o == -1 || scol[o] == key) break;
+          const unsigned short o = atomicCAS(&owner[slot], kNoOwner, (unsigned short)i);
+          if (o == kNoOwner || scol[o] == key) break;
           slot = (slot + 1) & (kSlots - 1);
         }
         rslot[i] = (uint16_t)slot;
-        atomicAdd(i < npos ? &cntp[slot] : &cntn[slot], 1u);
+        atomicAdd(&cnt[slot], i < npos ? 1u : 0x10000u);
       }
       __syncthreads();
       if (G.has_atoms) {
@@ -273,30 +580,11 @@ __global__ void __launch_bounds__(kEvalThreads, 1) eval_batched_kernel(EvalArgs 
         uint32_t sum = 0;
 #pragma unroll
         for (int k = 0; k < kPer; ++k) {
-          const int s = threadIdx.x * kPer + k;
-          v[k] = cntp[s] + cntn[s];
+          const uint32_t w = cnt[threadIdx.x * kPer + k];
+          v[k] = (w & 0xffffu) + (w >> 16);
           sum += v[k];
         }
-        uint32_t x = sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(kFullMask, x, o);
-          if (lane_id() >= o) x += y;
-        }
-        if (lane_id() == 31) s_warp[warp_id()] = x;
-        __syncthreads();
-        if (warp_id() == 0) {
-          const uint32_t t = s_warp[lane_id()];
-          uint32_t s = t;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(kFullMask, s, o);
-            if (lane_id() >= o) s += y;
-          }
-          s_warp[lane_id()] = s - t;
-        }
-        __syncthreads();
-        uint32_t run = x - sum + s_warp[warp_id()];
+        uint32_t run = block_scan_excl(sum, s_warp, &s_total);
 #pragma unroll
         for (int k = 0; k < kPer; ++k) {
           lend[threadIdx.x * kPer + k] = run;
@@ -309,64 +597,107 @@ __global__ void __launch_bounds__(kEvalThreads, 1) eval_batched_kernel(EvalArgs 
         }
         __syncthreads();
       }
-      // Stream each literal's relation key tuples of this partition range.
-      for (int L = G.lit_begin; L < G.lit_end; ++L) {
-        const LitDesc d = a.lits[L];
-        const uint32_t e0 = d.offsets[q0], e1 = d.offsets[q1];
+      // Flat pass over (literal, entry) of this partition: each thread takes
+      // a contiguous range of the literal-major entry space, keeps running
+      // sums while the literal stays the same, and adds them to the CTA
+      // accumulators when it changes; the last literal of every thread is
+      // combined across lanes with one segmented warp scan.
+      {
+        const uint32_t per = (E + blockDim.x - 1) / blockDim.x;
+        uint32_t f = threadIdx.x * per;
+        const uint32_t fend = umin(E, f + per);
+        int L = -1;
         long long bp = 0, bn = 0, cp = 0, cn = 0;
-        for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        if (f < fend) {
+          int lo = 0, hi = m - 1;  // largest L with lstart[L] <= f
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (lstart[mid] <= f) lo = mid; else hi = mid - 1;
+          }
+          L = lo;
+        }
+        for (; f < fend; ++f) {
+          if (f >= lstart[L + 1]) {
+            if ((cp | cn | bp | bn) != 0) {
+              unsigned long long* dst = acc + 4 * (G.lit_begin + L);
+              if (cp) atomicAdd(dst + 0, as_ull(cp));
+              if (cn) atomicAdd(dst + 1, as_ull(cn));
+              if (bp) atomicAdd(dst + 2, as_ull(bp));
+              if (bn) atomicAdd(dst + 3, as_ull(bn));
+            }
+            bp = bn = cp = cn = 0;
+            do ++L; while (f >= lstart[L + 1]);
+          }
+          const LitDesc& d = a.lits[G.lit_begin + L];
+          const uint32_t e = le0[L] + (f - lstart[L]);
           const int32_t k0 = __ldg(d.keys + e);
           uint32_t slot = mix32((uint32_t)k0) & (kSlots - 1);
-          int32_t o = -1;
+          unsigned short o = kNoOwner;
           for (int probe = 0; probe < kSlots; ++probe) {
             o = owner[slot];
-            if (o < 0 || scol[o] == k0) break;
+            if (o == kNoOwner || scol[o] == k0) break;
             slot = (slot + 1) & (kSlots - 1);
           }
-          if (o < 0 || scol[o] != k0) continue;
-          const long long m = __ldg(d.mult + e);
-          if (d.nk == 1) {
-            const uint32_t P = cntp[slot], N = cntn[slot];
-            bp += m * P;
-            bn += m * N;
+          if (o == kNoOwner || scol[o] != k0) continue;
+          const long long mlt = __ldg(d.mult + e);
+          const int nk = d.nk;
+          const uint32_t w = cnt[slot];
+          if (nk == 1) {
+            const uint32_t P = w & 0xffffu, N = w >> 16;
+            bp += mlt * P;
+            bn += mlt * N;
             cp += P;
             cn += N;
           } else {
             int32_t kq[QFG_MAX_ARITY];
-            for (int q = 1; q < d.nk; ++q) kq[q] = __ldg(d.keys + q * d.stride + e);
+            int col[QFG_MAX_ARITY];
+#pragma unroll
+            for (int q = 1; q < QFG_MAX_ARITY; ++q) {
+              if (q < nk) {
+                kq[q] = __ldg(d.keys + q * d.stride + e);
+                col[q] = d.atom_col[q] * kTile;
+              }
+            }
             const uint32_t end = lend[slot];
-            const uint32_t beg = end - (cntp[slot] + cntn[slot]);
+            const uint32_t beg = end - ((w & 0xffffu) + (w >> 16));
             for (uint32_t x = beg; x < end; ++x) {
               const int row = rows[x];
               bool pass = true;
-              for (int q = 1; q < d.nk; ++q) {
-                if (scol[d.atom_col[q] * kTile + row] != kq[q]) {
-                  pass = false;
-                  break;
-                }
-              }
+#pragma unroll
+              for (int q = 1; q < QFG_MAX_ARITY; ++q)
+                if (q < nk && scol[col[q] + row] != kq[q]) pass = false;
               if (!pass) continue;
               if (row < npos) {
-                bp += m;
+                bp += mlt;
                 cp += 1;
               } else {
-                bn += m;
+                bn += mlt;
                 cn += 1;
               }
             }
           }
         }
-        bp = warp_sum(bp);
-        bn = warp_sum(bn);
-        cp = warp_sum(cp);
-        cn = warp_sum(cn);
-        if (lane_id() == 0 && (bp | bn | cp | cn) != 0) {
-          unsigned long long* dst = acc + 4 * L;
-          atomicAdd(dst + 0, as_ull(cp));
-          atomicAdd(dst + 1, as_ull(cn));
-          atomicAdd(dst + 2, as_ull(bp));
-          atomicAdd(dst + 3, as_ull(bn));
+        // Lanes' ranges are contiguous and increasing, so equal literals sit
+        // on consecutive lanes; idle lanes (L = -1) trail.
+        cp = seg_scan(cp, L);
+        cn = seg_scan(cn, L);
+        bp = seg_scan(bp, L);
+        bn = seg_scan(bn, L);
+        const int next_L = __shfl_down_sync(kFullMask, L, 1);
+        const bool seg_end = lane_id() == 31 || next_L != L;
+        if (seg_end && L >= 0 && (cp | cn | bp | bn) != 0) {
+          unsigned long long* dst = acc + 4 * (G.lit_begin + L);
+          if (cp) atomicAdd(dst + 0, as_ull(cp));
+          if (cn) atomicAdd(dst + 1, as_ull(cn));
+          if (bp) atomicAdd(dst + 2, as_ull(bp));
+          if (bn) atomicAdd(dst + 3, as_ull(bn));
         }
+      }
+      __syncthreads();
+      // Return the touched slots to empty for the next tile.
+      for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        owner[rslot[i]] = kNoOwner;
+        cnt[rslot[i]] = 0u;
       }
       __syncthreads();
     }
@@ -381,7 +712,7 @@ __global__ void __launch_bounds__(kEvalThreads, 1) eval_batched_kernel(EvalArgs 
 int auto_group_bits(Ctx* ctx, int64_t n) {
   if (ctx->eval_bits > 0) return std::min(ctx->eval_bits, kMaxPartitionBits);
   int bits = 1;
-  while (bits < kMaxPartitionBits && (n >> bits) > kTile / 2) ++bits;
+  while (bits < kMaxPartitionBits && 3 * (n >> bits) > 2 * kTile) ++bits;
   return bits;
 }
 
@@ -500,7 +831,7 @@ static int plan_step(Ctx* ctx, int32_t n, const qfg_literal* lits, StepPlan* pla
     for (int i : kv.second) {
       std::vector<int> add = missing_cols(cur, i);
       if ((int)(cur.cols.size() + add.size()) > kGroupCols ||
-          (int)cur.lits.size() >= kMaxLitsPerLaunch) {
+          (int)cur.lits.size() >= kMaxGroupLits) {
         groups.push_back(cur);
         cur = HostGroup();
         cur.join_col = kv.first;
@@ -531,22 +862,35 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
 
   // Partition the binding set once per group.
   const int bits = auto_group_bits(ctx, nb);
-  const int nbins = 2 << bits;
-  const unsigned pgrid = (unsigned)ctx->num_sms;
+  const bool two_pass = bits > kMaxCoarseBits + 1;
+  const int cbits = two_pass ? kMaxCoarseBits : bits;
+  const int sbits = bits - cbits;
+  const int nfine = 2 << bits, np1 = 2 << cbits;
+  const unsigned pgrid = (unsigned)ctx->num_sms * 2;
   size_t part_words = 0;
-  for (auto& g : groups) part_words += g.cols.size() * (size_t)nb;
-  const size_t bins_words = (size_t)nbins + 1 + (size_t)pgrid * nbins;
-  QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * part_words));
-  QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(ctx, sizeof(uint32_t) * (groups.size() * ((size_t)nbins + 1) + bins_words)));
+  int max_ncols = 1;
+  for (auto& g : groups) {
+    part_words += g.cols.size() * (size_t)nb;
+    max_ncols = std::max(max_ncols, (int)g.cols.size());
+  }
+  const size_t tmp_words = two_pass ? (size_t)max_ncols * (size_t)nb : 0;
+  const size_t fs_words = (size_t)nfine + 1;
+  const size_t bins_words = (size_t)np1 + 1 + (size_t)pgrid * np1 + (size_t)np1 + 1;
+  QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * (part_words + tmp_words)));
+  QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(
+      ctx, sizeof(uint32_t) * (groups.size() * fs_words + bins_words)));
   int32_t* part_base = ctx->scratch[kScrBindPart].as<int32_t>();
-  uint32_t* starts = ctx->scratch[kScrBindOffsets].as<uint32_t>();
-  uint32_t* tot = starts + groups.size() * ((size_t)nbins + 1);
-  uint32_t* cta_base = tot + nbins + 1;
-  const size_t hist_smem = sizeof(uint32_t) * nbins;
-  QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)hist_smem));
-  QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_scatter_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hist_smem));
+  int32_t* tmp_cols = part_base + part_words;
+  uint32_t* fstarts = ctx->scratch[kScrBindOffsets].as<uint32_t>();
+  uint32_t* p1_tot = fstarts + groups.size() * fs_words;
+  uint32_t* p1_base = p1_tot + np1 + 1;
+  uint32_t* p1_start = p1_base + (size_t)pgrid * np1;
+  const size_t p1_smem = round_smem_bytes(max_ncols, np1);
+  const size_t p2_smem = round_smem_bytes(max_ncols, 1 << sbits);
+  QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass1_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p1_smem));
+  QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass2_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p2_smem));
   std::vector<GroupDesc> gdesc(groups.size());
   std::vector<LitDesc> ldesc;
   QFG_TRY(stage_begin(ctx, QFG_STAGE_BIND_PARTITION));
@@ -560,22 +904,39 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
     pa.n = nb;
     pa.npos = b->num_positive;
     pa.bits = bits;
-    pa.tot = tot;
-    pa.base = cta_base;
-    pa.out = part_base + off;
-    uint32_t* start = starts + gi * ((size_t)nbins + 1);
-    QFG_CUDA(ctx, cudaMemsetAsync(tot, 0, sizeof(uint32_t) * nbins, ctx->stream));
-    bpart_hist_kernel<<<pgrid, 1024, hist_smem, ctx->stream>>>(pa);
+    pa.cbits = cbits;
+    pa.p1_tot = p1_tot;
+    pa.p1_base = p1_base;
+    int32_t* final_out = part_base + off;
+    uint32_t* fstart = fstarts + gi * fs_words;
+    bool vec = true;
+    for (int c = 0; c < pa.ncols; ++c)
+      if (reinterpret_cast<uintptr_t>(pa.cols[c]) % 16 != 0) vec = false;
+    QFG_CUDA(ctx, cudaMemsetAsync(p1_tot, 0, sizeof(uint32_t) * (size_t)np1, ctx->stream));
+    if (vec)
+      bpart_hist_kernel<true><<<pgrid, kPartThreads, 0, ctx->stream>>>(pa);
+    else
+      bpart_hist_kernel<false><<<pgrid, kPartThreads, 0, ctx->stream>>>(pa);
     QFG_LAUNCHED(ctx);
-    QFG_TRY(exclusive_scan_u32(ctx, tot, start, nbins, start + nbins));
-    bpart_scatter_kernel<<<pgrid, 1024, hist_smem, ctx->stream>>>(pa, start);
-    QFG_LAUNCHED(ctx);
+    if (two_pass) {
+      QFG_TRY(exclusive_scan_u32(ctx, p1_tot, p1_start, np1, p1_start + np1));
+      bpart_pass1_kernel<<<pgrid, kPartThreads, p1_smem, ctx->stream>>>(pa, p1_start, tmp_cols);
+      QFG_LAUNCHED(ctx);
+      bpart_pass2_kernel<<<np1, kPartThreads, p2_smem, ctx->stream>>>(pa, p1_start, tmp_cols, fstart,
+                                                                     final_out);
+      QFG_LAUNCHED(ctx);
+    } else {
+      QFG_TRY(exclusive_scan_u32(ctx, p1_tot, fstart, np1, fstart + np1));
+      bpart_pass1_kernel<<<pgrid, kPartThreads, p1_smem, ctx->stream>>>(pa, fstart, final_out);
+      QFG_LAUNCHED(ctx);
+    }
 
     GroupDesc& d = gdesc[gi];
-    d.cols = pa.out;
+    d.cols = final_out;
     d.n = nb;
-    d.start = start;
+    d.fstart = fstart;
     d.bits = bits;
+    d.sbits = sbits;
     d.ncols = pa.ncols;
     d.lit_begin = (int)ldesc.size();
     d.has_atoms = g.has_atoms ? 1 : 0;
@@ -591,14 +952,13 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
       ld.offsets = kt->offsets.as<uint32_t>();
       ld.nk = kt->num_keys;
       for (int q = 1; q < ld.nk; ++q)
-        ld.atom_col[q] = (int)(std::find(g.cols.begin(), g.cols.end(), bind_cols[i][q]) - g.cols.begin());
+        ld.atom_col[q] = (int8_t)(std::find(g.cols.begin(), g.cols.end(), bind_cols[i][q]) - g.cols.begin());
       ld.out = i;
       ldesc.push_back(ld);
     }
     d.lit_end = (int)ldesc.size();
     off += g.cols.size() * (size_t)nb;
   }
-
   QFG_TRY(stage_end(ctx, QFG_STAGE_BIND_PARTITION));
 
   // Descriptors, then launches of at most kMaxLitsPerLaunch literals (groups
@@ -621,11 +981,11 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
     const int lit0 = gdesc[gbeg].lit_begin;
     const int64_t item0 = gdesc[gbeg].item_begin;
     for (size_t g = gbeg; g < gend; ++g) {
-      GroupDesc s = gdesc[g];
-      s.lit_begin -= lit0;
-      s.lit_end -= lit0;
-      s.item_begin -= item0;
-      sub_all.push_back(s);
+      GroupDesc sd = gdesc[g];
+      sd.lit_begin -= lit0;
+      sd.lit_end -= lit0;
+      sd.item_begin -= item0;
+      sub_all.push_back(sd);
     }
     launches.push_back({gbeg, gend, lit0, nl});
     gbeg = gend;
@@ -651,10 +1011,16 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
     ea.total_items = (int64_t)(L.gend - L.gbeg) << bits;
     ea.work_counter = counter;
     ea.counts = counts;
-    const size_t smem = eval_smem_bytes(L.nl);
+    ea.max_cols = 1;
+    for (size_t g = L.gbeg; g < L.gend; ++g) ea.max_cols = std::max(ea.max_cols, gdesc[g].ncols);
+    const size_t smem = eval_smem_bytes(L.nl, ea.max_cols);
     QFG_CUDA(ctx, cudaFuncSetAttribute(eval_batched_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    eval_batched_kernel<<<ctx->num_sms, kEvalThreads, smem, ctx->stream>>>(ea);
+    int per_sm = 0;
+    QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_batched_kernel,
+                                                               kEvalThreads, smem));
+    const int grid = ctx->num_sms * std::max(per_sm, 1);
+    eval_batched_kernel<<<grid, kEvalThreads, smem, ctx->stream>>>(ea);
     QFG_LAUNCHED(ctx);
   }
   QFG_TRY(stage_end(ctx, QFG_STAGE_EVALUATE));

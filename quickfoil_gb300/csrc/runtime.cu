@@ -353,8 +353,8 @@ extern "C" int qfg_ctx_set_option(qfg_ctx* c, int option, int64_t value) {
       ctx->num_radix_bits = (int)value;
       return QFG_OK;
     case QFG_OPT_EVAL_BITS:
-      if (value < 0 || value > QFG_MAX_RADIX_BITS)
-        return set_error(ctx, QFG_ERR_INVALID, "eval bits out of range [0, 15]");
+      if (value < 0 || value > 16)
+        return set_error(ctx, QFG_ERR_INVALID, "eval bits out of range [0, 16]");
       ctx->eval_bits = (int)value;
       return QFG_OK;
     case QFG_OPT_WAIT_LIMIT:

@@ -190,3 +190,21 @@ def test_single_literal_full_size(engine, zipf):
     want = np.array([[np.count_nonzero(m[:P]), np.count_nonzero(m[P:]), m[:P].sum(), m[P:].sum()]])
     np.testing.assert_array_equal(engine.evaluate_step(b, lits), want)
     np.testing.assert_array_equal(engine.evaluate_per_literal(b, lits), want)
+
+
+@pytest.mark.parametrize("bits", [1, 3, 8, 9, 12, 14])
+def test_evaluate_partition_bits_do_not_change_counts(engine, bits):
+    """Single-pass (<= 8 bits) and two-pass binding partitions, tiled and
+    untiled work items: identical counts."""
+    from quickfoil_gb300 import _capi as C
+    w = workloads.batched_step(n_bindings=300_000, num_relations=8, min_tuples=50,
+                               max_tuples=200_000, num_literals=48, domain=20_000, seed=21)
+    base = fresh_ids(len(w.relations))
+    lits = _register(engine, w, base)
+    b = engine.bindings(w.binding_columns, w.num_positive)
+    want = brute_counts([None] * base + w.relations, w.binding_columns, w.num_positive, lits)
+    try:
+        engine.set_option(C.QFG_OPT_EVAL_BITS, bits)
+        np.testing.assert_array_equal(engine.evaluate_step(b, lits), want)
+    finally:
+        engine.set_option(C.QFG_OPT_EVAL_BITS, 0)
