@@ -184,6 +184,24 @@ int qfg_step_traffic(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_lit
 int qfg_radix_partition(qfg_ctx* ctx, const int32_t* d_values, int64_t n, int bits,
                         int32_t* d_out_tuples, int64_t* d_offsets);
 
+/* No counterpart in the reference.  The radix partition of
+ * qfg_radix_partition (same inputs, same output) for callers that must not
+ * have device memory allocated on their behalf: a host process that owns all
+ * GPU memory through its own allocator, or a loop that cannot take the
+ * device-wide synchronization cudaMalloc / cudaFree bring.  It needs no
+ * context and allocates nothing: its working memory is a fixed 4 MiB array
+ * in the library's device image (held by every GPU that loads the library
+ * until the process exits).  That bounds the input: about 32 Mi values at 5
+ * radix bits, 8 Mi values at 12 or more bits; larger inputs return
+ * QFG_ERR_INVALID with the reason in `error` (error_len bytes, may be NULL).
+ * The first call on a device looks the array's device address up with that
+ * device current; make that first call before any stream capture.  All calls
+ * on a device share the array, so calls whose work overlaps on the GPU race.
+ * Work is queued on `stream` (a cudaStream_t, NULL = legacy stream). */
+int qfg_radix_partition_static(void* stream, const int32_t* d_values, int64_t n, int bits,
+                               int32_t* d_out_tuples, int64_t* d_offsets, char* error,
+                               int error_len);
+
 /* BuildHashTableOnPartitions (operations/BuildHashTable.cpp:54-93) with the
  * FoilHashTable layout (storage/FoilHashTable.cpp:34-49): for each non-empty
  * partition p, buckets[next_pow2(n_p)] of 1-based chain heads and next[n_p]

@@ -95,6 +95,8 @@ SIGNATURES = [
      [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i64p]),
     ("qfg_radix_partition", ctypes.c_int,
      [c_vp, c_vp, ctypes.c_int64, ctypes.c_int, c_vp, c_vp]),
+    ("qfg_radix_partition_static", ctypes.c_int,
+     [c_vp, c_vp, ctypes.c_int64, ctypes.c_int, c_vp, c_vp, ctypes.c_char_p, ctypes.c_int]),
     ("qfg_build_hash_table_on_partitions", ctypes.c_int,
      [c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_int, c_vp, c_vp, c_vp, c_vp]),
     ("qfg_build_hash_table_on_table", ctypes.c_int,

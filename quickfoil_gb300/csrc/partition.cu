@@ -16,6 +16,9 @@
 // partition positions of one bucket in descending order, so after a stable
 // sort by (partition, bucket) each element's `next` is its predecessor in the
 // sorted order and the bucket head is the last one.
+#include <cstring>
+#include <mutex>
+
 #include "qfg_common.cuh"
 
 namespace qfg {
@@ -411,5 +414,180 @@ extern "C" int qfg_build_hash_table_on_table(qfg_ctx* c, const int32_t* const* d
                                                                      d_buckets, d_next);
   QFG_LAUNCHED(ctx);
   QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return QFG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free radix partition.
+//
+// Some callers cannot let a library allocate device memory: a host process
+// that reserves all GPU memory for its own allocator and forbids cudaMalloc
+// from plug-ins, or a latency-critical loop that cannot afford the device-wide
+// synchronization that cudaMalloc / cudaFree imply.  qfg_radix_partition_static
+// serves them: it computes the same stable partition as qfg_radix_partition,
+// but its only working memory (the per-chunk digit counts and the scan of
+// those counts) is the fixed array below, which every GPU that loads this
+// library keeps for the life of the process.  Nothing is allocated per call.
+//
+// The array is shared by all calls on a device and keeps what the last call
+// left in it; every word a call reads is written earlier in the same call,
+// so nothing has to be cleared first.  Two calls whose work overlaps on the
+// GPU (different streams, or different host threads) race on the array.
+
+namespace qfg {
+namespace {
+
+constexpr int64_t kStaticScratchWords = int64_t(1) << 20;  // 4 MiB of uint32
+constexpr int kStaticScanThreads = 512;
+constexpr int kStaticScanItems = 8;
+constexpr int64_t kStaticScanTile = kStaticScanThreads * kStaticScanItems;
+
+static __device__ __align__(256) uint32_t g_static_scratch[kStaticScratchWords];
+
+// Device address of g_static_scratch per device ordinal, looked up once with
+// that device current (a host-side name of a __device__ array is not a device
+// address).
+std::mutex g_static_mutex;
+std::map<int, uint32_t*> g_static_ptr;
+
+int static_scratch_for_current_device(uint32_t** out, std::string* err) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    *err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+    return QFG_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  auto it = g_static_ptr.find(dev);
+  if (it == g_static_ptr.end()) {
+    uint32_t* ptr = nullptr;
+    e = cudaGetSymbolAddress(reinterpret_cast<void**>(&ptr), g_static_scratch);
+    if (e != cudaSuccess || ptr == nullptr) {
+      *err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      return QFG_ERR_CUDA;
+    }
+    it = g_static_ptr.emplace(dev, ptr).first;
+  }
+  *out = it->second;
+  return QFG_OK;
+}
+
+// In-place exclusive scan of up to kStaticScratchWords - tiles words: tile
+// scans with tile sums, one CTA scanning the sums, then the offsets added.
+__global__ void static_scan_tiles_kernel(uint32_t* __restrict__ data, int64_t n,
+                                         uint32_t* __restrict__ tile_sums) {
+  __shared__ uint32_t warp_tot[32];
+  const int64_t base = (int64_t)blockIdx.x * kStaticScanTile + (int64_t)threadIdx.x * kStaticScanItems;
+  uint32_t v[kStaticScanItems];
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < kStaticScanItems; ++k) {
+    v[k] = base + k < n ? data[base + k] : 0u;
+    sum += v[k];
+  }
+  uint32_t x = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFullMask, x, o);
+    if (lane_id() >= o) x += y;
+  }
+  if (lane_id() == 31) warp_tot[warp_id()] = x;
+  __syncthreads();
+  if (warp_id() == 0) {
+    const int nw = blockDim.x >> 5;
+    const uint32_t t = lane_id() < nw ? warp_tot[lane_id()] : 0u;
+    uint32_t s = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFullMask, s, o);
+      if (lane_id() >= o) s += y;
+    }
+    warp_tot[lane_id()] = s - t;
+    if (lane_id() == 31) tile_sums[blockIdx.x] = s;
+  }
+  __syncthreads();
+  uint32_t run = x - sum + warp_tot[warp_id()];
+#pragma unroll
+  for (int k = 0; k < kStaticScanItems; ++k) {
+    if (base + k < n) data[base + k] = run;
+    run += v[k];
+  }
+}
+
+__global__ void static_scan_sums_kernel(uint32_t* __restrict__ sums, int ntiles) {
+  if (threadIdx.x != 0) return;
+  uint32_t run = 0;
+  for (int i = 0; i < ntiles; ++i) {
+    const uint32_t v = sums[i];
+    sums[i] = run;
+    run += v;
+  }
+}
+
+__global__ void static_scan_add_kernel(uint32_t* __restrict__ data, int64_t n,
+                                       const uint32_t* __restrict__ tile_offsets) {
+  const uint32_t add = tile_offsets[blockIdx.x];
+  const int64_t base = (int64_t)blockIdx.x * kStaticScanTile;
+  for (int k = threadIdx.x; k < kStaticScanTile; k += blockDim.x)
+    if (base + k < n) data[base + k] += add;
+}
+
+}  // namespace
+}  // namespace qfg
+
+extern "C" int qfg_radix_partition_static(void* stream, const int32_t* d_values, int64_t n,
+                                          int bits, int32_t* d_out_tuples, int64_t* d_offsets,
+                                          char* error, int error_len) {
+  std::string err;
+  auto fail = [&](int status, const std::string& msg) {
+    if (error != nullptr && error_len > 0) {
+      strncpy(error, msg.c_str(), (size_t)error_len - 1);
+      error[error_len - 1] = '\0';
+    }
+    return status;
+  };
+  if (bits < 1 || bits > QFG_MAX_RADIX_BITS || n < 0 || n > INT32_MAX || d_offsets == nullptr ||
+      (n > 0 && (d_values == nullptr || d_out_tuples == nullptr)))
+    return fail(QFG_ERR_INVALID, "qfg_radix_partition_static: invalid arguments");
+  const PassShape s = pass_shape(std::max<int64_t>(n, 1), bits);
+  const int64_t entries = s.num_chunks * (int64_t(1) << bits);
+  const int64_t tiles = (entries + kStaticScanTile - 1) / kStaticScanTile;
+  if (entries + tiles > kStaticScratchWords)
+    return fail(QFG_ERR_INVALID,
+                "qfg_radix_partition_static: " + std::to_string(n) + " values at " +
+                    std::to_string(bits) + " radix bits need " + std::to_string(entries + tiles) +
+                    " scratch words, more than the " + std::to_string(kStaticScratchWords) +
+                    " of the static scratch array");
+  uint32_t* scratch = nullptr;
+  int st = static_scratch_for_current_device(&scratch, &err);
+  if (st != QFG_OK) return fail(st, err);
+  cudaStream_t strm = static_cast<cudaStream_t>(stream);
+  const uint32_t P = 1u << bits;
+  cudaError_t e = cudaSuccess;
+  if (n == 0) {
+    e = cudaMemsetAsync(d_offsets, 0, sizeof(int64_t) * (P + 1), strm);
+    return e == cudaSuccess ? QFG_OK : fail(QFG_ERR_CUDA, cudaGetErrorString(e));
+  }
+  uint32_t* hist = scratch;
+  uint32_t* tile_sums = scratch + entries;
+  RefTupleIO io{d_values, reinterpret_cast<int2*>(d_out_tuples)};
+  if (s.smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(stable_hist_kernel<RefTupleIO>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(stable_scatter_kernel<RefTupleIO>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    if (e != cudaSuccess) return fail(QFG_ERR_CUDA, cudaGetErrorString(e));
+  }
+  stable_hist_kernel<RefTupleIO><<<s.grid, 32 * s.warps, s.smem, strm>>>(io, n, 0, bits, s.chunk,
+                                                                          s.num_chunks, hist);
+  static_scan_tiles_kernel<<<(unsigned)tiles, kStaticScanThreads, 0, strm>>>(hist, entries, tile_sums);
+  static_scan_sums_kernel<<<1, 32, 0, strm>>>(tile_sums, (int)tiles);
+  static_scan_add_kernel<<<(unsigned)tiles, kStaticScanThreads, 0, strm>>>(hist, entries, tile_sums);
+  digit_offsets_kernel<<<(P + 256) / 256, 256, 0, strm>>>(hist, s.num_chunks, bits, n, d_offsets);
+  stable_scatter_kernel<RefTupleIO><<<s.grid, 32 * s.warps, s.smem, strm>>>(io, n, 0, bits, s.chunk,
+                                                                             s.num_chunks, hist);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(QFG_ERR_CUDA, cudaGetErrorString(e));
   return QFG_OK;
 }
