@@ -59,7 +59,9 @@ enum {
   QFG_OPT_EVAL_BITS = 2,        /* 0 = autotuned partition bits of the evaluation kernels */
   QFG_OPT_WAIT_LIMIT = 3,       /* iteration limit of bounded device-side waits */
   QFG_OPT_USE_GRAPHS = 4,       /* 1 = replay batched steps from captured CUDA graphs */
-  QFG_OPT_STAGE_TIMING = 5      /* 1 = time each evaluation stage with CUDA events */
+  QFG_OPT_STAGE_TIMING = 5,     /* 1 = time each evaluation stage with CUDA events */
+  QFG_OPT_SHARD_INDEX = 6,      /* this context's shard of the partition space (default 0) */
+  QFG_OPT_SHARD_COUNT = 7       /* number of shards (default 1); see qfg_evaluate_step */
 };
 
 /* Evaluation stages timed under QFG_OPT_STAGE_TIMING (the GPU counterpart of
@@ -157,7 +159,11 @@ int qfg_evaluate_group(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t claus
 
 /* All candidate literals of one refinement step at once, any join variable
  * (the loop of QuickFoil::EvaluateAllCandidateLiterals,
- * learner/QuickFoil.cpp:418-440, in one batched evaluation). */
+ * learner/QuickFoil.cpp:418-440, in one batched evaluation).
+ * With QFG_OPT_SHARD_COUNT = S > 1 the context evaluates only shard
+ * QFG_OPT_SHARD_INDEX of the join-key hash partitions; every binding row
+ * belongs to exactly one shard per literal, so the element-wise sum of the S
+ * shards' counts is the full result (one int64 sum of 4 * n counters). */
 int qfg_evaluate_step(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
                       const qfg_literal* literals, int64_t* counts, int flags);
 

@@ -35,6 +35,8 @@ QFG_OPT_EVAL_BITS = 2
 QFG_OPT_WAIT_LIMIT = 3
 QFG_OPT_USE_GRAPHS = 4
 QFG_OPT_STAGE_TIMING = 5
+QFG_OPT_SHARD_INDEX = 6
+QFG_OPT_SHARD_COUNT = 7
 
 STAGES = ("key_tables", "bind_partition", "evaluate", "per_literal")
 

@@ -436,6 +436,7 @@ struct GroupDesc {
   int bits, sbits, ncols;
   int lit_begin, lit_end;
   int has_atoms;
+  uint32_t p_lo;            // first partition of this context's shard
   int64_t item_begin;
 };
 
@@ -510,7 +511,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     int g = 0;
     while (g + 1 < a.num_groups && a.groups[g + 1].item_begin <= item) ++g;
     const GroupDesc G = a.groups[g];
-    const uint32_t p = (uint32_t)(item - G.item_begin);
+    const uint32_t p = G.p_lo + (uint32_t)(item - G.item_begin);
     const int s = G.sbits;
     const uint32_t hc = p >> s, sub = p & ((1u << s) - 1u);
     const uint32_t ip = ((2u * hc) << s) + sub, in_ = ((2u * hc + 1u) << s) + sub;
@@ -862,6 +863,11 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
 
   // Partition the binding set once per group.
   const int bits = auto_group_bits(ctx, nb);
+  if (ctx->shard_index >= ctx->shard_count)
+    return set_error(ctx, QFG_ERR_INVALID, "shard index must be below the shard count");
+  // Shard s owns partitions [s * 2^bits / S, (s + 1) * 2^bits / S).
+  const uint32_t shard_lo = (uint32_t)(((int64_t)ctx->shard_index << bits) / ctx->shard_count);
+  const uint32_t shard_hi = (uint32_t)(((int64_t)(ctx->shard_index + 1) << bits) / ctx->shard_count);
   const bool two_pass = bits > kMaxCoarseBits + 1;
   const int cbits = two_pass ? kMaxCoarseBits : bits;
   const int sbits = bits - cbits;
@@ -940,8 +946,9 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
     d.ncols = pa.ncols;
     d.lit_begin = (int)ldesc.size();
     d.has_atoms = g.has_atoms ? 1 : 0;
+    d.p_lo = shard_lo;
     d.item_begin = items;
-    items += (int64_t)1 << bits;
+    items += (int64_t)(shard_hi - shard_lo);
     for (int i : g.lits) {
       LitDesc ld;
       memset(&ld, 0, sizeof(ld));
@@ -1008,7 +1015,7 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
     ea.num_groups = (int)(L.gend - L.gbeg);
     ea.lits = ldev + L.lit0;
     ea.num_lits = L.nl;
-    ea.total_items = (int64_t)(L.gend - L.gbeg) << bits;
+    ea.total_items = (int64_t)(L.gend - L.gbeg) * (int64_t)(shard_hi - shard_lo);
     ea.work_counter = counter;
     ea.counts = counts;
     ea.max_cols = 1;

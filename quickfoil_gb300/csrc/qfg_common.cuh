@@ -135,6 +135,8 @@ struct Ctx {
   int eval_bits = 0;
   int64_t wait_limit = 1 << 26;
   int use_graphs = 0;
+  int shard_index = 0;
+  int shard_count = 1;
   int64_t launches = 0;
   std::map<int32_t, std::unique_ptr<Relation>> relations;
   // Grow-only scratch, reused by every call on this context.

@@ -367,6 +367,16 @@ extern "C" int qfg_ctx_set_option(qfg_ctx* c, int option, int64_t value) {
     case QFG_OPT_STAGE_TIMING:
       ctx->stage_timing = value != 0;
       return QFG_OK;
+    case QFG_OPT_SHARD_INDEX:
+      if (value < 0 || value >= 65536)
+        return set_error(ctx, QFG_ERR_INVALID, "shard index out of range");
+      ctx->shard_index = (int)value;
+      return QFG_OK;
+    case QFG_OPT_SHARD_COUNT:
+      if (value < 1 || value > 65536)
+        return set_error(ctx, QFG_ERR_INVALID, "shard count out of range [1, 65536]");
+      ctx->shard_count = (int)value;
+      return QFG_OK;
     default:
       return set_error(ctx, QFG_ERR_INVALID, "unknown option " + std::to_string(option));
   }
