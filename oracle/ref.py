@@ -1,0 +1,97 @@
+"""ctypes access to oracle/_ref/libqfref.so: the reference's own evaluator and
+learner compiled from its sources (see oracle/build_ref.sh).
+
+TEST INFRASTRUCTURE ONLY: used to produce and check golden fixtures in this
+checkout; the library does not exist where the reference sources are absent,
+and the GPU tests read the committed fixtures instead.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import List, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_ref", "libqfref.so")
+_lib = None
+
+
+def available() -> bool:
+    return os.path.exists(LIB_PATH) or os.path.isdir("/root/reference/operations")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            subprocess.check_call(["bash", os.path.join(_HERE, "build_ref.sh")])
+        L = ctypes.CDLL(LIB_PATH)
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        L.qfref_evaluate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), i64p,
+                                     ctypes.POINTER(i32p), ctypes.c_int, ctypes.POINTER(i32p),
+                                     ctypes.c_int64, ctypes.c_int64, ctypes.c_int, i32p,
+                                     ctypes.c_int, i64p]
+        L.qfref_evaluate.restype = ctypes.c_int
+        L.qfref_learn.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), i64p,
+                                  ctypes.POINTER(i32p), ctypes.c_int, ctypes.c_int64,
+                                  ctypes.c_int64, ctypes.POINTER(i32p), ctypes.c_int,
+                                  ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
+        L.qfref_learn.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _cols(arrays):
+    arrs = [np.ascontiguousarray(a, dtype=np.int32) for a in arrays]
+    ptrs = (ctypes.POINTER(ctypes.c_int32) * max(1, len(arrs)))(
+        *[a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)) for a in arrs])
+    return arrs, ptrs
+
+
+def _relations(relations):
+    flat = [c for r in relations for c in r]
+    keep, ptrs = _cols(flat)
+    ncols = (ctypes.c_int * max(1, len(relations)))(*[len(r) for r in relations])
+    ntup = (ctypes.c_int64 * max(1, len(relations)))(*[len(r[0]) for r in relations])
+    return keep, ptrs, ncols, ntup
+
+
+def evaluate(relations, binding_columns, num_positive: int, literals, radix_bits: int = 5):
+    """The reference's CandidateLiteralEvaluator on one binding set, one
+    Evaluate call per clause join variable; counts [n, 4] in the order of
+    `literals` ((relation, vars, join_pos) or Literal)."""
+    keep_r, rptr, rnc, rnt = _relations(relations)
+    keep_b, bptr = _cols(binding_columns)
+    n = len(keep_b[0]) if keep_b else 0
+    desc = np.full((max(1, len(literals)), 10), -1, dtype=np.int32)
+    for k, lit in enumerate(literals):
+        rel, vars_, _ = lit.as_tuple() if hasattr(lit, "as_tuple") else lit
+        desc[k, 0] = rel
+        desc[k, 1] = len(vars_)
+        desc[k, 2:2 + len(vars_)] = vars_
+    counts = np.zeros((max(1, len(literals)), 4), dtype=np.int64)
+    rc = lib().qfref_evaluate(len(relations), rnc, rnt, rptr, len(keep_b), bptr, num_positive,
+                              n - num_positive, len(literals),
+                              desc.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), radix_bits,
+                              counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    if rc != 0:
+        raise ValueError(f"reference driver rejected the input ({rc})")
+    return counts[:len(literals)]
+
+
+def learn(relations, target_columns, num_positive: int, max_clause_length: int,
+          trace_path: str = None) -> List[str]:
+    """Runs the reference learner; returns its learnt clauses (ToString)."""
+    keep_r, rptr, rnc, rnt = _relations(relations)
+    keep_t, tptr = _cols(target_columns)
+    out = ctypes.create_string_buffer(1 << 16)
+    rc = lib().qfref_learn(len(relations), rnc, rnt, rptr, len(keep_t), len(keep_t[0]),
+                           num_positive, tptr, max_clause_length,
+                           trace_path.encode() if trace_path else None, out, len(out))
+    if rc != 0:
+        raise RuntimeError(f"reference learner failed ({rc})")
+    return [l for l in out.value.decode().splitlines() if l]

@@ -1,0 +1,283 @@
+// ref_driver.cpp -- TEST INFRASTRUCTURE: a C entry layer around the
+// reference's own sources (jbalint/quickfoil, compiled unmodified against
+// oracle/shims by oracle/build_ref.sh) so that tests can produce golden
+// outputs from the real reference code.  Nothing in the product links it.
+//
+// qfref_evaluate  builds FoilPredicates and a consecutive binding clause from
+//                 flat int32 columns and runs CandidateLiteralEvaluator::
+//                 Evaluate once per clause join variable, exactly as
+//                 QuickFoil::EvaluateAllCandidateLiterals does
+//                 (learner/QuickFoil.cpp:418-440).
+// qfref_learn     runs QuickFoil::Learn (learner/QuickFoil.cpp:171-359) and,
+//                 through link-time wrappers of Evaluate and
+//                 CreateLabelAwareBindingTables, writes every call's inputs
+//                 and outputs to a trace file.
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "learner/CandidateLiteralEvaluator.hpp"
+#include "learner/CandidateLiteralInfo.hpp"
+#include "learner/QuickFoil.hpp"
+#include "memory/Buffer.hpp"
+#include "operations/MultiColumnHashJoin.hpp"
+#include "schema/FoilClause.hpp"
+#include "schema/FoilLiteral.hpp"
+#include "schema/FoilPredicate.hpp"
+#include "schema/FoilVariable.hpp"
+#include "utility/Vector.hpp"
+
+#include "gflags/gflags.h"
+#include "wrap_names.h"  // generated by oracle/build_ref.sh from the compiled objects
+
+namespace quickfoil {
+DECLARE_int32(num_radix_bits);
+DECLARE_int32(maximum_clause_length);
+}  // namespace quickfoil
+
+using namespace quickfoil;
+
+typedef std::unordered_map<const FoilPredicate*, Vector<const FoilLiteral*>> LiteralGroups;
+
+// The reference's symbols, reached through the linker's --wrap.
+void qfref_real_evaluate(CandidateLiteralEvaluator* self, int clause_join_key_id,
+                         const LiteralGroups& groups, Vector<CandidateLiteralInfo*>* results)
+    asm("__real_" QFREF_EVALUATE);
+void qfref_real_extend(const FoilClauseConstSharedPtr& clause, const FoilLiteral& literal,
+                       const size_type num_pos, const size_type num_neg,
+                       Vector<ConstBufferPtr>* new_table)
+    asm("__real_" QFREF_EXTEND);
+
+namespace {
+
+FILE* g_trace = nullptr;
+
+ConstBufferPtr MakeColumn(const int32_t* src, int64_t n) {
+  BufferPtr b = std::make_shared<Buffer>(sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1), (size_t)n);
+  if (n > 0) memcpy(b->mutable_data(), src, sizeof(int32_t) * (size_t)n);
+  return std::make_shared<const ConstBuffer>(b);
+}
+
+Vector<ConstBufferPtr> MakeColumns(int ncols, const int32_t* const* cols, int64_t n) {
+  Vector<ConstBufferPtr> out;
+  for (int c = 0; c < ncols; ++c) out.emplace_back(MakeColumn(cols[c], n));
+  return out;
+}
+
+void WriteColumn(const char* tag, const int32_t* v, int64_t n) {
+  fprintf(g_trace, "%s", tag);
+  for (int64_t i = 0; i < n; ++i) fprintf(g_trace, " %d", v[i]);
+  fprintf(g_trace, "\n");
+}
+
+// Binding set of a clause as consecutive columns (positives then negatives).
+void WriteBindings(const FoilClause& clause) {
+  const int64_t P = clause.GetNumPositiveBindings(), N = clause.GetNumNegativeBindings();
+  const int ncols = clause.num_variables();
+  fprintf(g_trace, "BINDINGS %d %lld %lld\n", ncols, (long long)P, (long long)N);
+  for (int c = 0; c < ncols; ++c) {
+    std::vector<int32_t> col;
+    if (clause.IsBindingDataConseuctive()) {
+      const int32_t* v = clause.integral_blocks()[c]->as_type<int32_t>();
+      col.assign(v, v + P + N);
+    } else {
+      const int32_t* p = clause.positive_blocks()[c]->as_type<int32_t>();
+      const int32_t* q = clause.negative_blocks()[c]->as_type<int32_t>();
+      col.assign(p, p + P);
+      col.insert(col.end(), q, q + N);
+    }
+    WriteColumn("COL", col.data(), (int64_t)col.size());
+  }
+}
+
+void WriteLiteral(const char* tag, const FoilLiteral& l) {
+  fprintf(g_trace, "%s %d %d %d", tag, l.predicate()->id(), l.num_variables(), l.join_key());
+  for (int i = 0; i < l.num_variables(); ++i) fprintf(g_trace, " %d", l.variable_at(i).variable_id());
+  fprintf(g_trace, "\n");
+}
+
+// The reference crashes when no literal of a call has any join-key match
+// (operations/CountAggregator.cpp:112-116 dereferences the first, null,
+// chunk).  Such a call's counts are all zero, so it is answered directly.
+bool CallHasJoinResult(const FoilClause& clause, int join_var, const LiteralGroups& groups) {
+  std::unordered_set<int32_t> keys;
+  const int64_t total = clause.GetNumTotalBindings();
+  if (clause.IsBindingDataConseuctive()) {
+    const int32_t* v = clause.integral_blocks()[join_var]->as_type<int32_t>();
+    keys.insert(v, v + total);
+  } else {
+    const int32_t* p = clause.positive_blocks()[join_var]->as_type<int32_t>();
+    const int32_t* q = clause.negative_blocks()[join_var]->as_type<int32_t>();
+    keys.insert(p, p + clause.GetNumPositiveBindings());
+    keys.insert(q, q + clause.GetNumNegativeBindings());
+  }
+  for (const auto& g : groups) {
+    for (const FoilLiteral* l : g.second) {
+      const TableView& t = l->predicate()->fact_table();
+      const int32_t* col = t.column_at(l->join_key())->as_type<int32_t>();
+      for (int64_t i = 0; i < t.num_tuples(); ++i)
+        if (keys.count(col[i])) return true;
+    }
+  }
+  return false;
+}
+
+// CandidateLiteralEvaluator holds only `const FoilClauseConstSharedPtr&
+// building_clause_` (learner/CandidateLiteralEvaluator.hpp:42): one pointer.
+const FoilClause& EvaluatorClause(const CandidateLiteralEvaluator* self) {
+  static_assert(sizeof(CandidateLiteralEvaluator) == sizeof(void*), "evaluator layout");
+  const FoilClauseConstSharedPtr* p = *reinterpret_cast<const FoilClauseConstSharedPtr* const*>(self);
+  return **p;
+}
+
+}  // namespace
+
+void qfref_wrap_evaluate(CandidateLiteralEvaluator* self, int clause_join_key_id,
+                         const LiteralGroups& groups, Vector<CandidateLiteralInfo*>* results)
+    asm("__wrap_" QFREF_EVALUATE);
+void qfref_wrap_evaluate(CandidateLiteralEvaluator* self, int clause_join_key_id,
+                         const LiteralGroups& groups, Vector<CandidateLiteralInfo*>* results) {
+  const FoilClause& clause = EvaluatorClause(self);
+  const size_t before = results->size();
+  if (CallHasJoinResult(clause, clause_join_key_id, groups)) {
+    qfref_real_evaluate(self, clause_join_key_id, groups, results);
+  } else {
+    for (const auto& g : groups)
+      for (const FoilLiteral* l : g.second) results->emplace_back(new CandidateLiteralInfo(l));
+  }
+  if (g_trace != nullptr) {
+    fprintf(g_trace, "EVALUATE %d %zu\n", clause_join_key_id, results->size() - before);
+    WriteBindings(clause);
+    for (size_t i = before; i < results->size(); ++i) {
+      const CandidateLiteralInfo* r = (*results)[i];
+      WriteLiteral("LIT", *r->literal);
+      fprintf(g_trace, "COUNTS %d %d %d %d\n", r->num_covered_positive, r->num_covered_negative,
+              r->num_binding_positive, r->num_binding_negative);
+    }
+  }
+}
+
+void qfref_wrap_extend(const FoilClauseConstSharedPtr& clause, const FoilLiteral& literal,
+                       const size_type num_pos, const size_type num_neg,
+                       Vector<ConstBufferPtr>* new_table)
+    asm("__wrap_" QFREF_EXTEND);
+void qfref_wrap_extend(const FoilClauseConstSharedPtr& clause, const FoilLiteral& literal,
+                       const size_type num_pos, const size_type num_neg,
+                       Vector<ConstBufferPtr>* new_table) {
+  const size_t before = new_table->size();
+  qfref_real_extend(clause, literal, num_pos, num_neg, new_table);
+  if (g_trace != nullptr) {
+    fprintf(g_trace, "EXTEND %d %d\n", num_pos, num_neg);
+    WriteBindings(*clause);
+    WriteLiteral("LIT", literal);
+    for (size_t c = before; c < new_table->size(); ++c)
+      WriteColumn("OUT", (*new_table)[c]->as_type<int32_t>(), num_pos + num_neg);
+  }
+}
+
+extern "C" {
+
+// Literal descriptors: lits[k * 10 + 0] = relation index, [1] = number of
+// arguments, [2 .. 9] = clause variable per argument (-1 unbound).  All
+// arguments share one type, so the join key is the first bound argument.
+int qfref_evaluate(int nrel, const int* rel_ncols, const int64_t* rel_ntuples,
+                   const int32_t* const* rel_cols, int bind_ncols, const int32_t* const* bind_cols,
+                   int64_t npos, int64_t nneg, int nlits, const int32_t* lits, int radix_bits,
+                   int64_t* counts) {
+  FLAGS_num_radix_bits = radix_bits;
+  std::vector<std::unique_ptr<FoilPredicate>> preds;
+  int off = 0;
+  for (int r = 0; r < nrel; ++r) {
+    Vector<int> types(rel_ncols[r], 0);
+    preds.emplace_back(new FoilPredicate(r, "r" + std::to_string(r), -1, types,
+                                         MakeColumns(rel_ncols[r], rel_cols + off, rel_ntuples[r])));
+    off += rel_ncols[r];
+  }
+  Vector<int> head_types(bind_ncols, 0);
+  FoilPredicate head_pred(nrel, "head", -1, head_types, MakeColumns(bind_ncols, bind_cols, 0));
+  FoilLiteral head(&head_pred);
+  for (int c = 0; c < bind_ncols; ++c) head.AddVariable(FoilVariable(c, 0));
+  FoilClauseConstSharedPtr clause = FoilClause::Create(
+      head, (size_type)npos, (size_type)nneg, MakeColumns(bind_ncols, bind_cols, npos + nneg));
+
+  std::vector<std::unique_ptr<FoilLiteral>> literals;
+  for (int k = 0; k < nlits; ++k) {
+    const int32_t* d = lits + 10 * k;
+    if (d[0] < 0 || d[0] >= nrel || d[1] != rel_ncols[d[0]]) return 1;
+    Vector<FoilVariable> vars;
+    for (int i = 0; i < d[1]; ++i) vars.emplace_back(d[2 + i] >= 0 ? FoilVariable(d[2 + i], 0) : FoilVariable(0));
+    literals.emplace_back(new FoilLiteral(preds[d[0]].get(), vars));
+    if (literals.back()->join_key() < 0) return 2;
+  }
+  memset(counts, 0, sizeof(int64_t) * 4 * (size_t)nlits);
+  CandidateLiteralEvaluator evaluator(clause);
+  for (int var = 0; var < bind_ncols; ++var) {
+    LiteralGroups groups;
+    for (auto& l : literals)
+      if (l->variable_at(l->join_key()).variable_id() == var) groups[l->predicate()].emplace_back(l.get());
+    if (groups.empty()) continue;
+    Vector<CandidateLiteralInfo*> results;
+    evaluator.Evaluate(var, groups, &results);
+    for (CandidateLiteralInfo* r : results) {
+      for (int k = 0; k < nlits; ++k) {
+        if (literals[k].get() != r->literal) continue;
+        counts[4 * k + 0] = r->num_covered_positive;
+        counts[4 * k + 1] = r->num_covered_negative;
+        counts[4 * k + 2] = r->num_binding_positive;
+        counts[4 * k + 3] = r->num_binding_negative;
+      }
+      delete r;
+    }
+  }
+  return 0;
+}
+
+// Runs the reference learner on one target relation (positives first) and
+// background relations; writes the learnt clauses (one per line) to
+// `clauses` and, when trace_path is given, every Evaluate and
+// CreateLabelAwareBindingTables call to that file.
+int qfref_learn(int nrel, const int* rel_ncols, const int64_t* rel_ntuples,
+                const int32_t* const* rel_cols, int target_ncols, int64_t target_n,
+                int64_t target_npos, const int32_t* const* target_cols, int max_clause_length,
+                const char* trace_path, char* clauses, int clauses_cap) {
+  FLAGS_maximum_clause_length = max_clause_length;
+  std::vector<std::unique_ptr<FoilPredicate>> owned;
+  Vector<const FoilPredicate*> background;
+  int off = 0;
+  for (int r = 0; r < nrel; ++r) {
+    Vector<int> types(rel_ncols[r], 0);
+    owned.emplace_back(new FoilPredicate(r, "r" + std::to_string(r), -1, types,
+                                         MakeColumns(rel_ncols[r], rel_cols + off, rel_ntuples[r])));
+    background.push_back(owned.back().get());
+    off += rel_ncols[r];
+  }
+  Vector<int> ttypes(target_ncols, 0);
+  FoilPredicate target(nrel, "target", -1, ttypes, MakeColumns(target_ncols, target_cols, target_n));
+  if (trace_path != nullptr) {
+    g_trace = fopen(trace_path, "w");
+    if (g_trace == nullptr) return 3;
+  }
+  std::string out;
+  {
+    QuickFoil qf((size_type)target_npos, (size_type)(target_n - target_npos), &target, background);
+    qf.Learn();
+    for (const auto& c : qf.learnt_clauses()) out += c->ToString() + "\n";
+  }
+  if (g_trace != nullptr) {
+    fprintf(g_trace, "CLAUSES\n%sEND\n", out.c_str());
+    fclose(g_trace);
+    g_trace = nullptr;
+  }
+  if (clauses != nullptr && clauses_cap > 0) {
+    strncpy(clauses, out.c_str(), (size_t)clauses_cap - 1);
+    clauses[clauses_cap - 1] = '\0';
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -129,3 +129,67 @@ def small_random(seed: int, n_bindings: int = 3000, ncols: int = 4, num_relation
     lits = random_literals(num_literals, relations, ncols, rng)
     P = int(rng.integers(0, n_bindings + 1))
     return Workload(f"small_random_{seed}", B, P, relations, lits, domain)
+
+
+@dataclass
+class LearnTask:
+    name: str
+    relations: List[List[np.ndarray]]   # background relations, id = index
+    relation_names: List[str]
+    target_columns: List[np.ndarray]    # positives first
+    num_positive: int
+    max_clause_length: int
+
+
+def kinship(seed: int = 1, persons: int = 200, generations: int = 4, max_positive: int = 60,
+            num_negative: int = 600) -> LearnTask:
+    """Kinship knowledge base: `persons` ids split evenly over `generations`
+    generations and over male/female; every person outside the first
+    generation has a father and a mother in the previous generation, so
+    parent(person, person) forms a random forest of that depth.  sibling(X, Y)
+    holds for X != Y sharing a parent.  The target uncle(X, Y) =
+    male(X) & sibling(X, Z) & parent(Z, Y): up to `max_positive` positive
+    pairs sampled from that rule and `num_negative` pairs drawn uniformly from
+    the other ordered pairs."""
+    rng = np.random.default_rng(seed)
+    ids = rng.permutation(persons).astype(np.int32)
+    per_gen = persons // generations
+    gens = [ids[g * per_gen:(g + 1) * per_gen] for g in range(generations)]
+    male, female, parent = [], [], []
+    for g, people in enumerate(gens):
+        half = len(people) // 2
+        male.extend(people[:half].tolist())
+        female.extend(people[half:].tolist())
+        if g == 0:
+            continue
+        fathers = gens[g - 1][:len(gens[g - 1]) // 2]
+        mothers = gens[g - 1][len(gens[g - 1]) // 2:]
+        for child in people:
+            parent.append((int(rng.choice(fathers)), int(child)))
+            parent.append((int(rng.choice(mothers)), int(child)))
+    parents_of = {}
+    for p, c in parent:
+        parents_of.setdefault(c, set()).add(p)
+    children_of = {}
+    for p, c in parent:
+        children_of.setdefault(p, set()).add(c)
+    sibling = sorted({(x, y) for p, cs in children_of.items() for x in cs for y in cs if x != y})
+    male_set = set(male)
+    uncle = sorted({(x, y) for (x, z) in sibling if x in male_set for y in children_of.get(z, ())})
+    pos_idx = rng.permutation(len(uncle))[:max_positive]
+    positives = [uncle[i] for i in sorted(pos_idx)]
+    uncle_set = set(uncle)
+    negatives = set()
+    while len(negatives) < num_negative:
+        x, y = (int(v) for v in rng.integers(0, persons, 2))
+        if x != y and (x, y) not in uncle_set:
+            negatives.add((x, y))
+    negatives = sorted(negatives)
+    cols = lambda pairs, k: np.array([p[k] for p in pairs], dtype=np.int32)
+    relations = [[cols(parent, 0), cols(parent, 1)],
+                 [np.array(sorted(male), dtype=np.int32)],
+                 [np.array(sorted(female), dtype=np.int32)],
+                 [cols(sibling, 0), cols(sibling, 1)]]
+    target = positives + negatives
+    return LearnTask("kinship", relations, ["parent", "male", "female", "sibling"],
+                     [cols(target, 0), cols(target, 1)], len(positives), 3)

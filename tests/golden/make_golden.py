@@ -1,0 +1,177 @@
+"""Generates the golden fixtures in this directory from the reference's own
+code (oracle/_ref, built from the reference sources by oracle/build_ref.sh).
+
+    python tests/golden/make_golden.py
+
+* eval_cases.npz   -- seeded evaluation cases (uniform and Zipf relations,
+                      atoms, repeated variables, P = 0 / P = n, no join
+                      result) with the counts the reference's
+                      CandidateLiteralEvaluator produced.
+* kinship.npz      -- the kinship knowledge base (relations, target) and the
+                      reference learner's trace: every Evaluate call
+                      (binding set, literals in result order, counts) and
+                      every CreateLabelAwareBindingTables call (binding set,
+                      literal, announced counts, output columns), plus the
+                      learnt clauses.
+
+Only this script reads the reference; the tests read the fixtures, so they
+also run where the reference sources are absent.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle.ref as ref  # noqa: E402
+from quickfoil_gb300 import workloads  # noqa: E402
+from quickfoil_gb300.engine import Literal  # noqa: E402
+
+
+def pack_relations(relations, prefix, out):
+    out[f"{prefix}num"] = np.array([len(relations)])
+    for i, r in enumerate(relations):
+        for k, c in enumerate(r):
+            out[f"{prefix}{i}_{k}"] = np.asarray(c, dtype=np.int32)
+
+
+def pack_literals(lits):
+    a = np.full((len(lits), 10), -1, dtype=np.int32)
+    for i, l in enumerate(lits):
+        rel, vars_, jp = l.as_tuple()
+        a[i, 0], a[i, 1] = rel, jp
+        a[i, 2:2 + len(vars_)] = vars_
+        a[i, 2 + len(vars_):] = -2  # arity terminator
+    return a
+
+
+def eval_cases():
+    out = {}
+    cases = []
+    for seed in range(8):
+        w = workloads.small_random(seed, n_bindings=2000, max_tuples=1500, num_literals=30,
+                                   zipf=seed % 2 == 0)
+        P = w.num_positive
+        if seed == 6:
+            P = 0
+        if seed == 7:
+            P = w.num_bindings
+        cases.append((w.relations, w.binding_columns, P, list(dict.fromkeys(w.literals))))
+    # a call with no join result at all: the reference would crash, the
+    # driver answers zeros (operations/CountAggregator.cpp:112-116)
+    rng = np.random.default_rng(99)
+    B = [rng.integers(0, 10, 200).astype(np.int32) for _ in range(2)]
+    R = [[np.arange(100, 120, dtype=np.int32), np.arange(20, dtype=np.int32)]]
+    cases.append((R, B, 50, [Literal(0, (0, -1)), Literal(0, (1, 0))]))
+    for i, (rels, B, P, lits) in enumerate(cases):
+        counts = ref.evaluate(rels, B, P, lits, radix_bits=5)
+        pack_relations(rels, f"c{i}_r", out)
+        for k, c in enumerate(B):
+            out[f"c{i}_b{k}"] = np.asarray(c, dtype=np.int32)
+        out[f"c{i}_meta"] = np.array([len(B), P])
+        out[f"c{i}_lits"] = pack_literals(lits)
+        out[f"c{i}_counts"] = counts
+    out["num_cases"] = np.array([len(cases)])
+    np.savez_compressed(os.path.join(HERE, "eval_cases.npz"), **out)
+    print("eval_cases.npz:", len(cases), "cases")
+
+
+def parse_trace(path):
+    """Trace lines written by oracle/ref_driver.cpp."""
+    lines = open(path).read().splitlines()
+    i = 0
+    calls = []
+
+    def read_bindings():
+        nonlocal i
+        _, ncols, P, N = lines[i].split()
+        i += 1
+        cols = []
+        for _ in range(int(ncols)):
+            vals = lines[i].split()[1:]
+            cols.append(np.array([int(v) for v in vals], dtype=np.int32))
+            i += 1
+        return cols, int(P), int(N)
+
+    def read_literal():
+        nonlocal i
+        parts = [int(v) for v in lines[i].split()[1:]]
+        i += 1
+        pred, nvars, jk = parts[:3]
+        return Literal(pred, tuple(parts[3:3 + nvars]), jk)
+
+    clauses = []
+    while i < len(lines):
+        head = lines[i].split()
+        if head[0] == "EVALUATE":
+            key, n = int(head[1]), int(head[2])
+            i += 1
+            cols, P, N = read_bindings()
+            lits, counts = [], []
+            for _ in range(n):
+                lits.append(read_literal())
+                counts.append([int(v) for v in lines[i].split()[1:]])
+                i += 1
+            calls.append(("evaluate", key, cols, P, lits, np.array(counts, dtype=np.int64)))
+        elif head[0] == "EXTEND":
+            npos, nneg = int(head[1]), int(head[2])
+            i += 1
+            cols, P, N = read_bindings()
+            lit = read_literal()
+            outs = []
+            while i < len(lines) and lines[i].startswith("OUT"):
+                vals = lines[i].split()[1:]
+                outs.append(np.array([int(v) for v in vals], dtype=np.int32))
+                i += 1
+            calls.append(("extend", (npos, nneg), cols, P, [lit], outs))
+        elif head[0] == "CLAUSES":
+            i += 1
+            while lines[i] != "END":
+                clauses.append(lines[i])
+                i += 1
+            i += 1
+        else:
+            raise ValueError(f"unexpected trace line {lines[i][:40]}")
+    return calls, clauses
+
+
+def kinship():
+    task = workloads.kinship(seed=1)
+    trace = os.path.join(HERE, "_kinship_trace.txt")
+    clauses = ref.learn(task.relations, task.target_columns, task.num_positive,
+                        task.max_clause_length, trace)
+    calls, traced_clauses = parse_trace(trace)
+    os.remove(trace)
+    assert traced_clauses == clauses
+    out = {}
+    pack_relations(task.relations, "r", out)
+    for k, c in enumerate(task.target_columns):
+        out[f"target{k}"] = c
+    out["meta"] = np.array([len(task.target_columns), task.num_positive, task.max_clause_length])
+    out["num_calls"] = np.array([len(calls)])
+    for j, (kind, key, cols, P, lits, result) in enumerate(calls):
+        out[f"k{j}_kind"] = np.array([0 if kind == "evaluate" else 1])
+        out[f"k{j}_key"] = np.array(key if kind == "extend" else [key, 0])
+        out[f"k{j}_meta"] = np.array([len(cols), P])
+        for k, c in enumerate(cols):
+            out[f"k{j}_b{k}"] = c
+        out[f"k{j}_lits"] = pack_literals(lits)
+        if kind == "evaluate":
+            out[f"k{j}_counts"] = result
+        else:
+            out[f"k{j}_nout"] = np.array([len(result)])
+            for k, c in enumerate(result):
+                out[f"k{j}_out{k}"] = c
+    out["clauses"] = np.array(clauses)
+    np.savez_compressed(os.path.join(HERE, "kinship.npz"), **out)
+    print("kinship.npz:", len(calls), "calls;", clauses)
+
+
+if __name__ == "__main__":
+    eval_cases()
+    kinship()
