@@ -181,6 +181,54 @@ int qfg_evaluate_per_literal(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t
 int qfg_step_traffic(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
                      const qfg_literal* literals, int64_t* bytes);
 
+/* Device scratch (bytes) a batched step of these literals over this binding
+ * set needs beyond the relations' cached key tables -- the figure the
+ * serving loop admits requests by.  No reference counterpart. */
+int qfg_step_scratch_bytes(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
+                           const qfg_literal* literals, int64_t* bytes);
+
+/* ---- batched steps replayed from CUDA graphs ---------------------------- */
+/* No reference counterpart.  Captures the batched evaluation of `literals`
+ * over `bindings` (as qfg_evaluate_step) into a CUDA graph with its own
+ * scratch: planning, relation key tables, scratch sizing and the descriptor
+ * upload happen here once; qfg_step_graph_launch replays the device work
+ * with one launch on the context's stream and writes 4 int64 per literal to
+ * counts_dev (device memory).  The graph reads the binding set's columns at
+ * replay time, so binding data refilled in place (same binding set, same
+ * sizes) is evaluated by a replay.  The binding set, the relations and
+ * counts_dev must outlive the graph. */
+typedef struct qfg_step_graph qfg_step_graph;
+int qfg_step_graph_create(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
+                          const qfg_literal* literals, int64_t* counts_dev,
+                          qfg_step_graph** out);
+int qfg_step_graph_launch(qfg_ctx* ctx, qfg_step_graph* graph);
+int qfg_step_graph_destroy(qfg_ctx* ctx, qfg_step_graph* graph);
+
+/* ---- serving loop -------------------------------------------------------- */
+/* No reference counterpart (the reference runs one search at a time).  A
+ * server scores candidate-literal batches of many concurrent rule searches:
+ * each request is a device-resident binding set plus literals; requests are
+ * admitted in arrival order when one of `slots` workspaces (own stream and
+ * scratch) is free and the scratch they need fits hbm_budget_bytes (0 = half
+ * the context budget) next to the requests in flight, run concurrently, and
+ * are admitted as others finish.  qfg_server_submit returns at once;
+ * qfg_server_poll retires finished requests (their counts land in the host
+ * arrays given at submission), returns up to max_ids ids retired and not yet
+ * returned, and admits queued ones; qfg_server_wait blocks
+ * for one request; qfg_server_drain for all.  qfg_server_stats reports
+ * latency percentiles (submission to completion).  While a server is alive
+ * the context is used through it only. */
+typedef struct qfg_server qfg_server;
+int qfg_server_create(qfg_ctx* ctx, int32_t slots, int64_t hbm_budget_bytes, qfg_server** out);
+int qfg_server_submit(qfg_server* server, const qfg_bindings* bindings, int32_t num_literals,
+                      const qfg_literal* literals, int64_t* host_counts, int64_t* request_id);
+int qfg_server_poll(qfg_server* server, int64_t* done_ids, int32_t max_ids, int32_t* num_done);
+int qfg_server_wait(qfg_server* server, int64_t request_id);
+int qfg_server_drain(qfg_server* server);
+int qfg_server_stats(qfg_server* server, double* p50_ms, double* p99_ms, int64_t* completed,
+                     int64_t* peak_in_flight);
+int qfg_server_destroy(qfg_server* server);
+
 /* ---- API-kept operators (device pointers, context stream) -------------- */
 /* RadixPartition (operations/RadixPartition.hpp:13-14, .cpp:56-186):
  * stable partition of n int32 values by ((uint32)v) & (2^bits - 1) into

@@ -95,6 +95,21 @@ SIGNATURES = [
      [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i64p, ctypes.c_int]),
     ("qfg_step_traffic", ctypes.c_int,
      [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i64p]),
+    ("qfg_step_scratch_bytes", ctypes.c_int,
+     [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i64p]),
+    ("qfg_step_graph_create", ctypes.c_int,
+     [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_vp, ctypes.POINTER(c_vp)]),
+    ("qfg_step_graph_launch", ctypes.c_int, [c_vp, c_vp]),
+    ("qfg_step_graph_destroy", ctypes.c_int, [c_vp, c_vp]),
+    ("qfg_server_create", ctypes.c_int, [c_vp, ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(c_vp)]),
+    ("qfg_server_submit", ctypes.c_int,
+     [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i64p, c_i64p]),
+    ("qfg_server_poll", ctypes.c_int, [c_vp, c_i64p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+    ("qfg_server_wait", ctypes.c_int, [c_vp, ctypes.c_int64]),
+    ("qfg_server_drain", ctypes.c_int, [c_vp]),
+    ("qfg_server_stats", ctypes.c_int,
+     [c_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), c_i64p, c_i64p]),
+    ("qfg_server_destroy", ctypes.c_int, [c_vp]),
     ("qfg_radix_partition", ctypes.c_int,
      [c_vp, c_vp, ctypes.c_int64, ctypes.c_int, c_vp, c_vp]),
     ("qfg_radix_partition_static", ctypes.c_int,

@@ -777,6 +777,8 @@ int relation_key_table(Ctx* ctx, Relation* rel, const std::vector<int>& position
                                                            std::max<int64_t>(distinct, 1),
                                                            kt->mult.as<int32_t>());
     QFG_LAUNCHED(ctx);
+    // A cached table is read later from any stream (serving slots, graphs).
+    QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   } else {
     QFG_TRY(kt->keys.reserve(ctx, sizeof(int32_t) * (size_t)kt->num_keys));
     QFG_TRY(kt->mult.reserve(ctx, sizeof(int32_t)));
@@ -848,9 +850,45 @@ static int plan_step(Ctx* ctx, int32_t n, const qfg_literal* lits, StepPlan* pla
   return QFG_OK;
 }
 
-int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
-                     unsigned long long* counts) {
+// A batched step decided on the host: scratch reserved, descriptors built,
+// partition passes and evaluation launches listed.  enqueue_step() then
+// issues only stream work (memsets and kernel launches, no host
+// synchronization), so a prepared step can be enqueued directly or captured
+// into a CUDA graph and replayed on new binding data of the same shape.
+struct PartJob {
+  BPartArgs pa;
+  bool vec;
+  int32_t* final_out;
+  uint32_t* fstart;
+};
+
+struct LaunchJob {
+  EvalArgs ea;
+  size_t smem;
+  int grid;
+};
+
+struct PreparedStep {
+  int bits = 0, cbits = 0, sbits = 0, np1 = 0;
+  bool two_pass = false;
+  unsigned pgrid = 0;
+  size_t p1_smem = 0, p2_smem = 0;
+  uint32_t* p1_tot = nullptr;
+  uint32_t* p1_start = nullptr;
+  int32_t* tmp_cols = nullptr;
+  std::vector<PartJob> parts;
+  std::vector<LaunchJob> launches;
+  std::vector<unsigned char> blob;  // descriptors, to be copied to blob_dev
+  void* blob_dev = nullptr;
+  unsigned int* counter = nullptr;
+};
+
+int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
+                 unsigned long long* counts, PreparedStep* ps) {
   const int64_t nb = b->num_positive + b->num_negative;
+  ps->parts.clear();
+  ps->launches.clear();
+  ps->blob.clear();
   if (n == 0 || nb == 0) return QFG_OK;
 
   QFG_TRY(stage_begin(ctx, QFG_STAGE_KEY_TABLES));
@@ -861,88 +899,74 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
   const auto& bind_cols = plan.bind_cols;
   const auto& groups = plan.groups;
 
-  // Partition the binding set once per group.
+  // Partition shape and shard.
   const int bits = auto_group_bits(ctx, nb);
   if (ctx->shard_index >= ctx->shard_count)
     return set_error(ctx, QFG_ERR_INVALID, "shard index must be below the shard count");
   // Shard s owns partitions [s * 2^bits / S, (s + 1) * 2^bits / S).
   const uint32_t shard_lo = (uint32_t)(((int64_t)ctx->shard_index << bits) / ctx->shard_count);
   const uint32_t shard_hi = (uint32_t)(((int64_t)(ctx->shard_index + 1) << bits) / ctx->shard_count);
-  const bool two_pass = bits > kMaxCoarseBits + 1;
-  const int cbits = two_pass ? kMaxCoarseBits : bits;
-  const int sbits = bits - cbits;
-  const int nfine = 2 << bits, np1 = 2 << cbits;
-  const unsigned pgrid = (unsigned)ctx->num_sms * 2;
+  ps->bits = bits;
+  ps->two_pass = bits > kMaxCoarseBits + 1;
+  ps->cbits = ps->two_pass ? kMaxCoarseBits : bits;
+  ps->sbits = bits - ps->cbits;
+  const int nfine = 2 << bits;
+  ps->np1 = 2 << ps->cbits;
+  ps->pgrid = (unsigned)ctx->num_sms * 2;
   size_t part_words = 0;
   int max_ncols = 1;
   for (auto& g : groups) {
     part_words += g.cols.size() * (size_t)nb;
     max_ncols = std::max(max_ncols, (int)g.cols.size());
   }
-  const size_t tmp_words = two_pass ? (size_t)max_ncols * (size_t)nb : 0;
+  const size_t tmp_words = ps->two_pass ? (size_t)max_ncols * (size_t)nb : 0;
   const size_t fs_words = (size_t)nfine + 1;
-  const size_t bins_words = (size_t)np1 + 1 + (size_t)pgrid * np1 + (size_t)np1 + 1;
+  const size_t bins_words = (size_t)ps->np1 + 1 + (size_t)ps->pgrid * ps->np1 + (size_t)ps->np1 + 1;
   QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * (part_words + tmp_words)));
   QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(
       ctx, sizeof(uint32_t) * (groups.size() * fs_words + bins_words)));
   int32_t* part_base = ctx->scratch[kScrBindPart].as<int32_t>();
-  int32_t* tmp_cols = part_base + part_words;
+  ps->tmp_cols = part_base + part_words;
   uint32_t* fstarts = ctx->scratch[kScrBindOffsets].as<uint32_t>();
-  uint32_t* p1_tot = fstarts + groups.size() * fs_words;
-  uint32_t* p1_base = p1_tot + np1 + 1;
-  uint32_t* p1_start = p1_base + (size_t)pgrid * np1;
-  const size_t p1_smem = round_smem_bytes(max_ncols, np1);
-  const size_t p2_smem = round_smem_bytes(max_ncols, 1 << sbits);
+  ps->p1_tot = fstarts + groups.size() * fs_words;
+  uint32_t* p1_base = ps->p1_tot + ps->np1 + 1;
+  ps->p1_start = p1_base + (size_t)ps->pgrid * ps->np1;
+  ps->p1_smem = round_smem_bytes(max_ncols, ps->np1);
+  ps->p2_smem = round_smem_bytes(max_ncols, 1 << ps->sbits);
   QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass1_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p1_smem));
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps->p1_smem));
   QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass2_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p2_smem));
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps->p2_smem));
+
   std::vector<GroupDesc> gdesc(groups.size());
   std::vector<LitDesc> ldesc;
-  QFG_TRY(stage_begin(ctx, QFG_STAGE_BIND_PARTITION));
   size_t off = 0;
   int64_t items = 0;
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     const HostGroup& g = groups[gi];
-    BPartArgs pa;
+    PartJob job;
+    BPartArgs& pa = job.pa;
     pa.ncols = (int)g.cols.size();
     for (int c = 0; c < pa.ncols; ++c) pa.cols[c] = b->columns[g.cols[c]];
     pa.n = nb;
     pa.npos = b->num_positive;
     pa.bits = bits;
-    pa.cbits = cbits;
-    pa.p1_tot = p1_tot;
+    pa.cbits = ps->cbits;
+    pa.p1_tot = ps->p1_tot;
     pa.p1_base = p1_base;
-    int32_t* final_out = part_base + off;
-    uint32_t* fstart = fstarts + gi * fs_words;
-    bool vec = true;
+    job.final_out = part_base + off;
+    job.fstart = fstarts + gi * fs_words;
+    job.vec = true;
     for (int c = 0; c < pa.ncols; ++c)
-      if (reinterpret_cast<uintptr_t>(pa.cols[c]) % 16 != 0) vec = false;
-    QFG_CUDA(ctx, cudaMemsetAsync(p1_tot, 0, sizeof(uint32_t) * (size_t)np1, ctx->stream));
-    if (vec)
-      bpart_hist_kernel<true><<<pgrid, kPartThreads, 0, ctx->stream>>>(pa);
-    else
-      bpart_hist_kernel<false><<<pgrid, kPartThreads, 0, ctx->stream>>>(pa);
-    QFG_LAUNCHED(ctx);
-    if (two_pass) {
-      QFG_TRY(exclusive_scan_u32(ctx, p1_tot, p1_start, np1, p1_start + np1));
-      bpart_pass1_kernel<<<pgrid, kPartThreads, p1_smem, ctx->stream>>>(pa, p1_start, tmp_cols);
-      QFG_LAUNCHED(ctx);
-      bpart_pass2_kernel<<<np1, kPartThreads, p2_smem, ctx->stream>>>(pa, p1_start, tmp_cols, fstart,
-                                                                     final_out);
-      QFG_LAUNCHED(ctx);
-    } else {
-      QFG_TRY(exclusive_scan_u32(ctx, p1_tot, fstart, np1, fstart + np1));
-      bpart_pass1_kernel<<<pgrid, kPartThreads, p1_smem, ctx->stream>>>(pa, fstart, final_out);
-      QFG_LAUNCHED(ctx);
-    }
+      if (reinterpret_cast<uintptr_t>(pa.cols[c]) % 16 != 0) job.vec = false;
+    ps->parts.push_back(job);
 
     GroupDesc& d = gdesc[gi];
-    d.cols = final_out;
+    d.cols = job.final_out;
     d.n = nb;
-    d.fstart = fstart;
+    d.fstart = job.fstart;
     d.bits = bits;
-    d.sbits = sbits;
+    d.sbits = ps->sbits;
     d.ncols = pa.ncols;
     d.lit_begin = (int)ldesc.size();
     d.has_atoms = g.has_atoms ? 1 : 0;
@@ -966,16 +990,15 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
     d.lit_end = (int)ldesc.size();
     off += g.cols.size() * (size_t)nb;
   }
-  QFG_TRY(stage_end(ctx, QFG_STAGE_BIND_PARTITION));
 
-  // Descriptors, then launches of at most kMaxLitsPerLaunch literals (groups
-  // never straddle a launch: they are capped at that size).  Each launch
-  // gets its own rebased copy of its groups; everything goes up in one copy.
-  struct Launch {
+  // Launches of at most kMaxLitsPerLaunch literals (groups never straddle a
+  // launch: they are capped below that size); each launch gets a rebased copy
+  // of its groups, and all descriptors go up in one copy.
+  struct Span {
     size_t gbeg, gend;
     int lit0, nl;
   };
-  std::vector<Launch> launches;
+  std::vector<Span> spans;
   std::vector<GroupDesc> sub_all;
   for (size_t gbeg = 0; gbeg < gdesc.size();) {
     size_t gend = gbeg;
@@ -994,44 +1017,120 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
       sd.item_begin -= item0;
       sub_all.push_back(sd);
     }
-    launches.push_back({gbeg, gend, lit0, nl});
+    spans.push_back({gbeg, gend, lit0, nl});
     gbeg = gend;
   }
   const size_t gbytes = sizeof(GroupDesc) * sub_all.size();
   const size_t lbytes = sizeof(LitDesc) * ldesc.size();
-  std::vector<unsigned char> blob(gbytes + lbytes);
-  memcpy(blob.data(), sub_all.data(), gbytes);
-  memcpy(blob.data() + gbytes, ldesc.data(), lbytes);
-  QFG_TRY(ctx->scratch[kScrLits].reserve(ctx, blob.size() + 64));
+  ps->blob.resize(gbytes + lbytes);
+  memcpy(ps->blob.data(), sub_all.data(), gbytes);
+  memcpy(ps->blob.data() + gbytes, ldesc.data(), lbytes);
+  QFG_TRY(ctx->scratch[kScrLits].reserve(ctx, ps->blob.size() + 64));
   GroupDesc* gdev = ctx->scratch[kScrLits].as<GroupDesc>();
   LitDesc* ldev = reinterpret_cast<LitDesc*>(gdev + sub_all.size());
-  unsigned int* counter = reinterpret_cast<unsigned int*>(ldev + ldesc.size());
-  QFG_TRY(upload_small(ctx, gdev, blob.data(), blob.size()));
-  QFG_TRY(stage_begin(ctx, QFG_STAGE_EVALUATE));
-  for (const Launch& L : launches) {
-    QFG_CUDA(ctx, cudaMemsetAsync(counter, 0, sizeof(unsigned int), ctx->stream));
-    EvalArgs ea;
-    ea.groups = gdev + L.gbeg;
-    ea.num_groups = (int)(L.gend - L.gbeg);
-    ea.lits = ldev + L.lit0;
-    ea.num_lits = L.nl;
-    ea.total_items = (int64_t)(L.gend - L.gbeg) * (int64_t)(shard_hi - shard_lo);
-    ea.work_counter = counter;
+  ps->blob_dev = gdev;
+  ps->counter = reinterpret_cast<unsigned int*>(ldev + ldesc.size());
+  for (const Span& S : spans) {
+    LaunchJob L;
+    EvalArgs& ea = L.ea;
+    ea.groups = gdev + S.gbeg;
+    ea.num_groups = (int)(S.gend - S.gbeg);
+    ea.lits = ldev + S.lit0;
+    ea.num_lits = S.nl;
+    ea.total_items = (int64_t)(S.gend - S.gbeg) * (int64_t)(shard_hi - shard_lo);
+    ea.work_counter = ps->counter;
     ea.counts = counts;
     ea.max_cols = 1;
-    for (size_t g = L.gbeg; g < L.gend; ++g) ea.max_cols = std::max(ea.max_cols, gdesc[g].ncols);
-    const size_t smem = eval_smem_bytes(L.nl, ea.max_cols);
+    for (size_t g = S.gbeg; g < S.gend; ++g) ea.max_cols = std::max(ea.max_cols, gdesc[g].ncols);
+    L.smem = eval_smem_bytes(S.nl, ea.max_cols);
     QFG_CUDA(ctx, cudaFuncSetAttribute(eval_batched_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
     int per_sm = 0;
     QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_batched_kernel,
-                                                               kEvalThreads, smem));
-    const int grid = ctx->num_sms * std::max(per_sm, 1);
-    eval_batched_kernel<<<grid, kEvalThreads, smem, ctx->stream>>>(ea);
+                                                               kEvalThreads, L.smem));
+    L.grid = ctx->num_sms * std::max(per_sm, 1);
+    ps->launches.push_back(L);
+  }
+  return QFG_OK;
+}
+
+int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
+  const PreparedStep& ps = *pps;
+  if (ps.parts.empty()) return QFG_OK;
+  QFG_TRY(stage_begin(ctx, QFG_STAGE_BIND_PARTITION));
+  for (const PartJob& job : ps.parts) {
+    QFG_CUDA(ctx, cudaMemsetAsync(ps.p1_tot, 0, sizeof(uint32_t) * (size_t)ps.np1, ctx->stream));
+    if (job.vec)
+      bpart_hist_kernel<true><<<ps.pgrid, kPartThreads, 0, ctx->stream>>>(job.pa);
+    else
+      bpart_hist_kernel<false><<<ps.pgrid, kPartThreads, 0, ctx->stream>>>(job.pa);
+    QFG_LAUNCHED(ctx);
+    if (ps.two_pass) {
+      QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, ps.p1_start, ps.np1, ps.p1_start + ps.np1));
+      bpart_pass1_kernel<<<ps.pgrid, kPartThreads, ps.p1_smem, ctx->stream>>>(job.pa, ps.p1_start,
+                                                                               ps.tmp_cols);
+      QFG_LAUNCHED(ctx);
+      bpart_pass2_kernel<<<ps.np1, kPartThreads, ps.p2_smem, ctx->stream>>>(
+          job.pa, ps.p1_start, ps.tmp_cols, job.fstart, job.final_out);
+      QFG_LAUNCHED(ctx);
+    } else {
+      QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, job.fstart, ps.np1, job.fstart + ps.np1));
+      bpart_pass1_kernel<<<ps.pgrid, kPartThreads, ps.p1_smem, ctx->stream>>>(job.pa, job.fstart,
+                                                                               job.final_out);
+      QFG_LAUNCHED(ctx);
+    }
+  }
+  QFG_TRY(stage_end(ctx, QFG_STAGE_BIND_PARTITION));
+  QFG_TRY(stage_begin(ctx, QFG_STAGE_EVALUATE));
+  for (const LaunchJob& L : ps.launches) {
+    QFG_CUDA(ctx, cudaMemsetAsync(ps.counter, 0, sizeof(unsigned int), ctx->stream));
+    eval_batched_kernel<<<L.grid, kEvalThreads, L.smem, ctx->stream>>>(L.ea);
     QFG_LAUNCHED(ctx);
   }
   QFG_TRY(stage_end(ctx, QFG_STAGE_EVALUATE));
   return QFG_OK;
+}
+
+PreparedStep* prepared_step_new() { return new PreparedStep(); }
+void prepared_step_free(PreparedStep* ps) { delete ps; }
+bool prepared_is_empty(const PreparedStep* ps) { return ps->parts.empty(); }
+
+int upload_prepared(Ctx* ctx, const PreparedStep* ps, bool sync) {
+  if (ps->blob.empty()) return QFG_OK;
+  if (!sync) return upload_small(ctx, ps->blob_dev, ps->blob.data(), ps->blob.size());
+  QFG_CUDA(ctx, cudaMemcpy(ps->blob_dev, ps->blob.data(), ps->blob.size(), cudaMemcpyHostToDevice));
+  return QFG_OK;
+}
+
+int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
+                       int64_t* bytes) {
+  *bytes = 0;
+  const int64_t nb = b->num_positive + b->num_negative;
+  if (n == 0 || nb == 0) return QFG_OK;
+  StepPlan plan;
+  QFG_TRY(plan_step(ctx, n, lits, &plan));
+  const int bits = auto_group_bits(ctx, nb);
+  const bool two_pass = bits > kMaxCoarseBits + 1;
+  const int np1 = 2 << (two_pass ? kMaxCoarseBits : bits);
+  int64_t words = 0;
+  int max_ncols = 1;
+  for (auto& g : plan.groups) {
+    words += (int64_t)g.cols.size() * nb + (2 << bits) + 1;
+    max_ncols = std::max(max_ncols, (int)g.cols.size());
+  }
+  if (two_pass) words += (int64_t)max_ncols * nb;
+  words += (int64_t)np1 * (ctx->num_sms * 2 + 3);
+  *bytes = 4 * words + (int64_t)(sizeof(GroupDesc) + sizeof(LitDesc)) * n + 32 * (int64_t)n;
+  return QFG_OK;
+}
+
+int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
+                     unsigned long long* counts) {
+  PreparedStep ps;
+  QFG_TRY(prepare_step(ctx, b, n, lits, counts, &ps));
+  if (ps.parts.empty()) return QFG_OK;
+  QFG_TRY(upload_prepared(ctx, &ps, false));
+  return enqueue_step(ctx, &ps);
 }
 
 }  // namespace qfg

@@ -23,4 +23,20 @@ int evaluate_plain_one(Ctx* ctx, const qfg_bindings* b, const qfg_literal& l,
 int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
                      unsigned long long* counts);
 
+// A batched step split into its host part (planning, key tables, scratch,
+// descriptors) and its device part (stream work only).
+struct PreparedStep;
+PreparedStep* prepared_step_new();
+void prepared_step_free(PreparedStep* ps);
+int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
+                 unsigned long long* counts, PreparedStep* ps);
+// Copies the descriptors to the device: through pinned staging on the stream
+// (sync = false) or with a blocking copy (sync = true, before a capture).
+int upload_prepared(Ctx* ctx, const PreparedStep* ps, bool sync);
+int enqueue_step(Ctx* ctx, const PreparedStep* ps);
+bool prepared_is_empty(const PreparedStep* ps);
+// Device scratch bytes a batched step over these literals needs.
+int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
+                       int64_t* bytes);
+
 }  // namespace qfg

@@ -183,6 +183,35 @@ enum ScratchSlot {
   kScrLits = 15,
 };
 
+// An independent set of scratch buffers and a stream.  Evaluation code uses
+// ctx->scratch and ctx->stream; a WorkspaceScope swaps a workspace's buffers
+// and stream in for its lifetime, so that a captured graph or a serving slot
+// owns scratch that no other call touches.
+struct Workspace {
+  DevBuf scratch[16];
+  cudaStream_t stream = nullptr;
+  int64_t bytes() const {
+    int64_t t = 0;
+    for (const DevBuf& d : scratch) t += (int64_t)d.bytes();
+    return t;
+  }
+  void release() {
+    for (DevBuf& d : scratch) d.release();
+  }
+};
+
+class WorkspaceScope {
+ public:
+  WorkspaceScope(Ctx* ctx, Workspace* ws);
+  ~WorkspaceScope();
+  WorkspaceScope(const WorkspaceScope&) = delete;
+  WorkspaceScope& operator=(const WorkspaceScope&) = delete;
+
+ private:
+  Ctx* ctx_;
+  Workspace* ws_;
+};
+
 int set_error(Ctx* ctx, int status, const std::string& msg);
 
 // Copies `bytes` of host data to device `dst` on the context stream through

@@ -80,6 +80,16 @@ int DevBuf::reserve(Ctx* ctx, size_t bytes) {
   return QFG_OK;
 }
 
+WorkspaceScope::WorkspaceScope(Ctx* ctx, Workspace* ws) : ctx_(ctx), ws_(ws) {
+  for (int i = 0; i < 16; ++i) std::swap(ctx_->scratch[i], ws_->scratch[i]);
+  std::swap(ctx_->stream, ws_->stream);
+}
+
+WorkspaceScope::~WorkspaceScope() {
+  for (int i = 0; i < 16; ++i) std::swap(ctx_->scratch[i], ws_->scratch[i]);
+  std::swap(ctx_->stream, ws_->stream);
+}
+
 int upload_small(Ctx* ctx, void* dst, const void* src, size_t bytes) {
   if (bytes == 0) return QFG_OK;
   const int slot = ctx->staging_next;

@@ -1,0 +1,412 @@
+// step_runtime.cu -- replaying batched steps from CUDA graphs, and a serving
+// loop that runs literal-scoring requests of many rule searches concurrently.
+//
+// Graphs.  A refinement step's host work (planning, relation key tables,
+// scratch sizing, descriptor building) is done once; its device work -- ~50
+// memsets, scans, partition passes and evaluation launches -- is captured
+// into a CUDA graph with its own workspace and replayed with one
+// cudaGraphLaunch.  The graph reads the binding set at replay time, so new
+// binding data of the same shape (the same binding set refilled in place) is
+// evaluated by a replay.
+//
+// Serving.  A server owns `slots` workspaces, each with its own stream and
+// pinned count buffer.  Requests (a device-resident binding set plus a batch
+// of candidate literals) are admitted in arrival order when a slot is free
+// and the scratch they need fits the server's HBM budget next to the
+// requests in flight; admitted requests run concurrently on their slots'
+// streams, and requests that arrive meanwhile are admitted as slots and
+// memory free up (continuous batching).  Completion is stamped on the host by
+// a stream callback; latency = completion - submission.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <vector>
+
+#include "eval_common.cuh"
+
+using namespace qfg;
+
+extern "C" int qfg_step_scratch_bytes(qfg_ctx* c, const qfg_bindings* b, int32_t n,
+                                      const qfg_literal* lits, int64_t* bytes) {
+  if (c == nullptr || b == nullptr || bytes == nullptr) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  QFG_TRY(validate_literals(ctx, b, n, lits));
+  return step_scratch_bytes(ctx, b, n, lits, bytes);
+}
+
+struct qfg_step_graph {
+  Workspace ws;
+  cudaStream_t capture_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t launches_per_replay = 0;
+};
+
+extern "C" int qfg_step_graph_destroy(qfg_ctx* c, qfg_step_graph* g) {
+  if (c == nullptr || g == nullptr) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  cudaStreamSynchronize(ctx->stream);
+  if (g->exec != nullptr) cudaGraphExecDestroy(g->exec);
+  if (g->graph != nullptr) cudaGraphDestroy(g->graph);
+  if (g->capture_stream != nullptr) cudaStreamSynchronize(g->capture_stream);
+  g->ws.release();
+  if (g->capture_stream != nullptr) cudaStreamDestroy(g->capture_stream);
+  delete g;
+  return QFG_OK;
+}
+
+extern "C" int qfg_step_graph_create(qfg_ctx* c, const qfg_bindings* b, int32_t n,
+                                     const qfg_literal* lits, int64_t* counts_dev,
+                                     qfg_step_graph** out) {
+  if (c == nullptr || b == nullptr || out == nullptr) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  *out = nullptr;
+  QFG_TRY(validate_literals(ctx, b, n, lits));
+  if (n > 0 && counts_dev == nullptr) return set_error(ctx, QFG_ERR_INVALID, "null counts");
+  auto g = new qfg_step_graph();
+  auto fail = [&](int st) {
+    qfg_step_graph_destroy(c, g);
+    return st;
+  };
+  if (cudaStreamCreateWithFlags(&g->capture_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(cuda_error(ctx, cudaGetLastError(), "cudaStreamCreate"));
+  g->ws.stream = g->capture_stream;
+  unsigned long long* counts = reinterpret_cast<unsigned long long*>(counts_dev);
+  const bool timing = ctx->stage_timing;
+  int st = QFG_OK;
+  {
+    WorkspaceScope scope(ctx, &g->ws);
+    PreparedStep* ps = prepared_step_new();
+    st = prepare_step(ctx, b, n, lits, counts, ps);
+    if (st == QFG_OK) st = upload_prepared(ctx, ps, true);
+    // One uncaptured run sizes every scratch buffer the step touches, so the
+    // captured run allocates nothing.
+    if (st == QFG_OK) {
+      ctx->stage_timing = false;
+      st = enqueue_step(ctx, ps);
+    }
+    if (st == QFG_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      st = cuda_error(ctx, cudaGetLastError(), "warm-up run");
+    if (st == QFG_OK) {
+      const int64_t before = ctx->launches;
+      cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) {
+        st = cuda_error(ctx, e, "cudaStreamBeginCapture");
+      } else {
+        if (n > 0) e = cudaMemsetAsync(counts, 0, sizeof(int64_t) * 4 * (size_t)n, ctx->stream);
+        int st2 = e == cudaSuccess ? enqueue_step(ctx, ps) : cuda_error(ctx, e, "memset");
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(ctx->stream, &graph);
+        g->graph = graph;
+        if (st2 != QFG_OK) st = st2;
+        else if (e != cudaSuccess) st = cuda_error(ctx, e, "cudaStreamEndCapture");
+        g->launches_per_replay = ctx->launches - before;
+      }
+    }
+    ctx->stage_timing = timing;
+    prepared_step_free(ps);
+  }
+  if (st != QFG_OK) return fail(st);
+  cudaError_t e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e != cudaSuccess) return fail(cuda_error(ctx, e, "cudaGraphInstantiate"));
+  *out = g;
+  return QFG_OK;
+}
+
+extern "C" int qfg_step_graph_launch(qfg_ctx* c, qfg_step_graph* g) {
+  if (c == nullptr || g == nullptr) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  if (g->exec == nullptr) return QFG_OK;
+  QFG_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+  ctx->launches += g->launches_per_replay;
+  return QFG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Serving loop.
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  int64_t id = 0;
+  const qfg_bindings* bindings = nullptr;
+  std::vector<qfg_literal> literals;
+  int64_t* host_counts = nullptr;
+  int64_t scratch_bytes = 0;
+  Clock::time_point submitted;
+  Clock::time_point finished;
+  std::atomic<int> done{0};  // set by the stream callback after `finished`
+  int slot = -1;
+  int status = QFG_OK;
+};
+
+struct Slot {
+  Workspace ws;
+  cudaStream_t stream = nullptr;
+  int64_t* pinned_counts = nullptr;
+  size_t pinned_cap = 0;
+  Request* running = nullptr;
+};
+
+void CUDART_CB mark_done(void* user) {
+  Request* r = static_cast<Request*>(user);
+  r->finished = Clock::now();
+  r->done.store(1, std::memory_order_release);
+}
+
+}  // namespace
+
+struct qfg_server {
+  Ctx* ctx = nullptr;
+  int64_t budget = 0;
+  std::vector<Slot> slots;
+  std::deque<Request*> queue;
+  std::vector<Request*> all;
+  int64_t next_id = 1;
+  int64_t in_flight_bytes = 0;
+  int64_t peak_in_flight = 0;
+  std::vector<double> latencies_ms;
+  std::deque<int64_t> finished;  // retired ids not yet returned by poll
+};
+
+namespace {
+
+int server_admit(qfg_server* s) {
+  Ctx* ctx = s->ctx;
+  while (!s->queue.empty()) {
+    Request* r = s->queue.front();
+    int free_slot = -1;
+    int running = 0;
+    for (size_t i = 0; i < s->slots.size(); ++i) {
+      if (s->slots[i].running == nullptr) {
+        if (free_slot < 0) free_slot = (int)i;
+      } else {
+        ++running;
+      }
+    }
+    if (free_slot < 0) return QFG_OK;
+    if (running > 0 && s->in_flight_bytes + r->scratch_bytes > s->budget) return QFG_OK;
+    s->queue.pop_front();
+    if (running == 0 && r->scratch_bytes > s->budget) {
+      // Can never run: it fails alone instead of blocking the queue.
+      r->status = set_error(ctx, QFG_ERR_BUDGET,
+                            "request needs more scratch than the server's HBM budget");
+      r->finished = Clock::now();
+      r->done.store(1, std::memory_order_release);
+      s->finished.push_back(r->id);
+      continue;
+    }
+    Slot& slot = s->slots[free_slot];
+    r->slot = free_slot;
+    slot.running = r;
+    s->in_flight_bytes += r->scratch_bytes;
+    s->peak_in_flight = std::max<int64_t>(s->peak_in_flight, running + 1);
+    // Idle slots give their cached scratch back when it would not fit.
+    int64_t held = 0;
+    for (const Slot& o : s->slots) held += o.ws.bytes();
+    if (held - slot.ws.bytes() + r->scratch_bytes > s->budget) {
+      for (Slot& o : s->slots)
+        if (o.running == nullptr && &o != &slot) o.ws.release();
+    }
+    const int n = (int)r->literals.size();
+    int st = QFG_OK;
+    if ((size_t)std::max(n, 1) * 4 > slot.pinned_cap) {
+      if (slot.pinned_counts != nullptr) cudaFreeHost(slot.pinned_counts);
+      slot.pinned_counts = nullptr;
+      slot.pinned_cap = 0;
+      cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&slot.pinned_counts),
+                                    sizeof(int64_t) * 4 * (size_t)std::max(n, 1), cudaHostAllocDefault);
+      if (e != cudaSuccess) st = cuda_error(ctx, e, "cudaHostAlloc");
+      else slot.pinned_cap = (size_t)std::max(n, 1) * 4;
+    }
+    if (st == QFG_OK) {
+      WorkspaceScope scope(ctx, &slot.ws);
+      unsigned long long* dev = nullptr;
+      st = ctx->scratch[kScrCounts].reserve(ctx, sizeof(int64_t) * 4 * (size_t)std::max(n, 1));
+      if (st == QFG_OK) {
+        dev = ctx->scratch[kScrCounts].as<unsigned long long>();
+        cudaError_t e = cudaMemsetAsync(dev, 0, sizeof(int64_t) * 4 * (size_t)std::max(n, 1),
+                                        ctx->stream);
+        if (e != cudaSuccess) st = cuda_error(ctx, e, "memset");
+      }
+      if (st == QFG_OK && n > 0) {
+        PreparedStep* ps = prepared_step_new();
+        st = prepare_step(ctx, r->bindings, n, r->literals.data(), dev, ps);
+        if (st == QFG_OK) st = upload_prepared(ctx, ps, false);
+        if (st == QFG_OK) st = enqueue_step(ctx, ps);
+        prepared_step_free(ps);
+        if (st == QFG_OK) {
+          cudaError_t e = cudaMemcpyAsync(slot.pinned_counts, dev, sizeof(int64_t) * 4 * (size_t)n,
+                                          cudaMemcpyDeviceToHost, ctx->stream);
+          if (e != cudaSuccess) st = cuda_error(ctx, e, "count download");
+        }
+      }
+      if (st == QFG_OK) {
+        cudaError_t e = cudaLaunchHostFunc(ctx->stream, mark_done, r);
+        if (e != cudaSuccess) st = cuda_error(ctx, e, "cudaLaunchHostFunc");
+      }
+    }
+    if (st != QFG_OK) {
+      r->status = st;
+      r->finished = Clock::now();
+      r->done.store(1, std::memory_order_release);
+    }
+  }
+  return QFG_OK;
+}
+
+// Retires finished requests: copies their counts out and frees their slots.
+int server_reap(qfg_server* s) {
+  for (Slot& slot : s->slots) {
+    Request* r = slot.running;
+    if (r == nullptr || !r->done.load(std::memory_order_acquire)) continue;
+    if (r->status == QFG_OK && !r->literals.empty())
+      memcpy(r->host_counts, slot.pinned_counts, sizeof(int64_t) * 4 * r->literals.size());
+    s->in_flight_bytes -= r->scratch_bytes;
+    slot.running = nullptr;
+    s->latencies_ms.push_back(
+        std::chrono::duration<double, std::milli>(r->finished - r->submitted).count());
+    s->finished.push_back(r->id);
+  }
+  return QFG_OK;
+}
+
+}  // namespace
+
+extern "C" int qfg_server_create(qfg_ctx* c, int32_t slots, int64_t hbm_budget_bytes,
+                                 qfg_server** out) {
+  if (c == nullptr || out == nullptr || slots < 1 || slots > 1024) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  auto s = new qfg_server();
+  s->ctx = ctx;
+  s->budget = hbm_budget_bytes > 0 ? hbm_budget_bytes : ctx->budget / 2;
+  s->slots.resize(slots);
+  for (Slot& slot : s->slots) {
+    if (cudaStreamCreateWithFlags(&slot.stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      for (Slot& o : s->slots)
+        if (o.stream != nullptr) cudaStreamDestroy(o.stream);
+      delete s;
+      return set_error(ctx, QFG_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    slot.ws.stream = slot.stream;
+  }
+  *out = s;
+  return QFG_OK;
+}
+
+extern "C" int qfg_server_submit(qfg_server* s, const qfg_bindings* b, int32_t n,
+                                 const qfg_literal* lits, int64_t* host_counts,
+                                 int64_t* request_id) {
+  if (s == nullptr || b == nullptr || (n > 0 && host_counts == nullptr)) return QFG_ERR_INVALID;
+  Ctx* ctx = s->ctx;
+  QFG_TRY(validate_literals(ctx, b, n, lits));
+  auto r = new Request();
+  r->id = s->next_id++;
+  r->bindings = b;
+  r->literals.assign(lits, lits + n);
+  r->host_counts = host_counts;
+  r->submitted = Clock::now();
+  int st = step_scratch_bytes(ctx, b, n, lits, &r->scratch_bytes);
+  if (st != QFG_OK) {
+    delete r;
+    return st;
+  }
+  s->all.push_back(r);
+  s->queue.push_back(r);
+  if (request_id != nullptr) *request_id = r->id;
+  QFG_TRY(server_reap(s));
+  return server_admit(s);
+}
+
+extern "C" int qfg_server_poll(qfg_server* s, int64_t* done_ids, int32_t max, int32_t* num_done) {
+  if (s == nullptr) return QFG_ERR_INVALID;
+  QFG_TRY(server_reap(s));
+  int32_t k = 0;
+  while (k < max && done_ids != nullptr && !s->finished.empty()) {
+    done_ids[k++] = s->finished.front();
+    s->finished.pop_front();
+  }
+  if (num_done != nullptr) *num_done = k;
+  return server_admit(s);
+}
+
+extern "C" int qfg_server_wait(qfg_server* s, int64_t request_id) {
+  if (s == nullptr) return QFG_ERR_INVALID;
+  Request* target = nullptr;
+  for (Request* r : s->all)
+    if (r->id == request_id) target = r;
+  if (target == nullptr) return set_error(s->ctx, QFG_ERR_NOT_FOUND, "unknown request id");
+  for (;;) {
+    QFG_TRY(server_reap(s));
+    QFG_TRY(server_admit(s));
+    if (target->done.load() && target->slot >= 0 && s->slots[target->slot].running != target) break;
+    if (target->done.load() && target->slot < 0) break;
+    if (target->slot < 0 && !target->done.load()) {
+      bool any = false;
+      for (Slot& slot : s->slots) any = any || slot.running != nullptr;
+      if (!any) return set_error(s->ctx, QFG_ERR_INVALID, "request cannot be admitted");
+    }
+    // Block on the stream of the slot the request runs on, or on any busy one.
+    cudaStream_t wait_on = nullptr;
+    if (target->slot >= 0 && s->slots[target->slot].running == target)
+      wait_on = s->slots[target->slot].stream;
+    else
+      for (Slot& slot : s->slots)
+        if (slot.running != nullptr) wait_on = slot.stream;
+    if (wait_on == nullptr) break;
+    QFG_CUDA(s->ctx, cudaStreamSynchronize(wait_on));
+  }
+  return target->status;
+}
+
+extern "C" int qfg_server_drain(qfg_server* s) {
+  if (s == nullptr) return QFG_ERR_INVALID;
+  for (;;) {
+    QFG_TRY(server_reap(s));
+    QFG_TRY(server_admit(s));
+    bool busy = false;
+    for (Slot& slot : s->slots)
+      if (slot.running != nullptr) {
+        busy = true;
+        QFG_CUDA(s->ctx, cudaStreamSynchronize(slot.stream));
+      }
+    if (!busy && s->queue.empty()) break;
+  }
+  return QFG_OK;
+}
+
+extern "C" int qfg_server_stats(qfg_server* s, double* p50_ms, double* p99_ms, int64_t* completed,
+                                int64_t* peak_in_flight) {
+  if (s == nullptr) return QFG_ERR_INVALID;
+  std::vector<double> v = s->latencies_ms;
+  std::sort(v.begin(), v.end());
+  auto pct = [&](double q) {
+    if (v.empty()) return 0.0;
+    const size_t i = (size_t)std::min<double>(v.size() - 1, std::ceil(q * v.size()) - 1);
+    return v[i];
+  };
+  if (p50_ms) *p50_ms = pct(0.50);
+  if (p99_ms) *p99_ms = pct(0.99);
+  if (completed) *completed = (int64_t)v.size();
+  if (peak_in_flight) *peak_in_flight = s->peak_in_flight;
+  return QFG_OK;
+}
+
+extern "C" int qfg_server_destroy(qfg_server* s) {
+  if (s == nullptr) return QFG_ERR_INVALID;
+  qfg_server_drain(s);
+  for (Slot& slot : s->slots) {
+    slot.ws.release();
+    if (slot.pinned_counts != nullptr) cudaFreeHost(slot.pinned_counts);
+    if (slot.stream != nullptr) cudaStreamDestroy(slot.stream);
+  }
+  for (Request* r : s->all) delete r;
+  delete s;
+  return QFG_OK;
+}

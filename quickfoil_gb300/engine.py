@@ -280,6 +280,26 @@ class Engine:
                                            C.QFG_COUNTS_DEVICE),
                 self.ctx, "qfg_evaluate_step")
 
+    def step_scratch_bytes(self, bindings: BindingSet, literals: Sequence[Literal]) -> int:
+        """Device scratch a batched step of these literals needs."""
+        lits = (C.QfgLiteral * max(1, len(literals)))(*[l.to_c() for l in literals])
+        out = ctypes.c_int64()
+        C.check(self.lib.qfg_step_scratch_bytes(self.ctx, bindings.handle, len(literals), lits,
+                                                ctypes.byref(out)),
+                self.ctx, "qfg_step_scratch_bytes")
+        return out.value
+
+    def step_graph(self, bindings: BindingSet, literals: Sequence[Literal],
+                   counts_dev_ptr: int) -> "StepGraph":
+        """A batched step captured into a CUDA graph; each ``launch()`` writes
+        the counts of the binding set's current contents to ``counts_dev_ptr``
+        (device, 4*n int64)."""
+        return StepGraph(self, bindings, literals, counts_dev_ptr)
+
+    def server(self, slots: int = 4, hbm_budget: int = 0) -> "StepServer":
+        """A serving loop over concurrent requests of many rule searches."""
+        return StepServer(self, slots, hbm_budget)
+
     # -- API-kept operators (torch CUDA tensors) ------------------------------
     def radix_partition(self, values, bits: int):
         """RadixPartition: returns (tuples [n, 2] int32, offsets [2^bits+1] int64)."""
@@ -353,6 +373,103 @@ class Engine:
                 self.ctx, "qfg_extend_bindings")
         ncols = bindings.num_columns + sum(1 for v in literal.vars if v < 0)
         return BindingSet(self, h, ncols, num_out_positive, num_out_negative)
+
+
+class StepGraph:
+    """qfg_step_graph_*: one refinement step replayed with a single launch."""
+
+    def __init__(self, engine: Engine, bindings: BindingSet, literals: Sequence[Literal],
+                 counts_dev_ptr: int):
+        self.engine = engine
+        self._keep = bindings
+        self.num_literals = len(literals)
+        self._lits = (C.QfgLiteral * max(1, len(literals)))(*[l.to_c() for l in literals])
+        h = C.c_vp()
+        C.check(engine.lib.qfg_step_graph_create(engine.ctx, bindings.handle, len(literals),
+                                                 self._lits, counts_dev_ptr, ctypes.byref(h)),
+                engine.ctx, "qfg_step_graph_create")
+        self.handle = h
+
+    def launch(self):
+        C.check(self.engine.lib.qfg_step_graph_launch(self.engine.ctx, self.handle),
+                self.engine.ctx, "qfg_step_graph_launch")
+
+    def close(self):
+        if self.handle:
+            self.engine.lib.qfg_step_graph_destroy(self.engine.ctx, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class StepServer:
+    """qfg_server_*: requests (binding set + candidate literals) of many
+    concurrent rule searches, admitted under an HBM budget and run on
+    separate streams; counts land in host arrays."""
+
+    def __init__(self, engine: Engine, slots: int, hbm_budget: int):
+        self.engine = engine
+        h = C.c_vp()
+        C.check(engine.lib.qfg_server_create(engine.ctx, slots, hbm_budget, ctypes.byref(h)),
+                engine.ctx, "qfg_server_create")
+        self.handle = h
+        self._pending: Dict[int, Tuple[BindingSet, object, np.ndarray]] = {}
+
+    def submit(self, bindings: BindingSet, literals: Sequence[Literal]) -> int:
+        lits = (C.QfgLiteral * max(1, len(literals)))(*[l.to_c() for l in literals])
+        counts = np.zeros((max(1, len(literals)), 4), dtype=np.int64)
+        rid = ctypes.c_int64()
+        C.check(self.engine.lib.qfg_server_submit(self.handle, bindings.handle, len(literals), lits,
+                                                  counts.ctypes.data_as(C.c_i64p),
+                                                  ctypes.byref(rid)),
+                self.engine.ctx, "qfg_server_submit")
+        self._pending[rid.value] = (bindings, lits, counts[:len(literals)])
+        return rid.value
+
+    def poll(self) -> List[int]:
+        ids = (ctypes.c_int64 * 256)()
+        n = ctypes.c_int32()
+        out: List[int] = []
+        while True:
+            C.check(self.engine.lib.qfg_server_poll(self.handle, ids, 256, ctypes.byref(n)),
+                    self.engine.ctx, "qfg_server_poll")
+            out.extend(ids[i] for i in range(n.value))
+            if n.value < 256:
+                return out
+
+    def result(self, request_id: int) -> np.ndarray:
+        """Waits for the request; its counts [n, 4]."""
+        C.check(self.engine.lib.qfg_server_wait(self.handle, request_id), self.engine.ctx,
+                "qfg_server_wait")
+        return self._pending[request_id][2]
+
+    def drain(self):
+        C.check(self.engine.lib.qfg_server_drain(self.handle), self.engine.ctx, "qfg_server_drain")
+
+    def stats(self):
+        p50, p99 = ctypes.c_double(), ctypes.c_double()
+        done, peak = ctypes.c_int64(), ctypes.c_int64()
+        C.check(self.engine.lib.qfg_server_stats(self.handle, ctypes.byref(p50), ctypes.byref(p99),
+                                                 ctypes.byref(done), ctypes.byref(peak)),
+                self.engine.ctx, "qfg_server_stats")
+        return {"p50_ms": p50.value, "p99_ms": p99.value, "completed": done.value,
+                "peak_in_flight": peak.value}
+
+    def close(self):
+        if self.handle:
+            self.engine.lib.qfg_server_destroy(self.handle)
+            self.handle = None
+            self._pending.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class CandidateLiteralEvaluator:

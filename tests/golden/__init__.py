@@ -64,3 +64,19 @@ def kinship():
             calls.append(("extend", tuple(int(v) for v in z[f"k{j}_key"]), cols, P, lits,
                           [z[f"k{j}_out{k}"] for k in range(nout)]))
     return rels, calls, [str(c) for c in z["clauses"]]
+
+
+def input_checksum(w):
+    """Order-sensitive checksums of a workload's binding columns and relations
+    (one per column, below 2^61)."""
+    def col_sum(c):
+        c = np.asarray(c, dtype=np.int64)
+        return int((c * (np.arange(len(c), dtype=np.int64) % 1000003 + 1)).sum() % (1 << 61))
+    return [col_sum(c) for c in w.binding_columns] + [col_sum(c) for r in w.relations for c in r]
+
+
+def batched_step_reference():
+    """(distinct literals, reference counts, input checksums) of the full-size
+    batched step (32M x 6 bindings, 32 relations, 256 literals)."""
+    z = np.load(os.path.join(HERE, "batched_step_reference.npz"))
+    return unpack_literals(z["lits"]), z["counts"], [int(v) for v in z["checksum"]]

@@ -7,6 +7,9 @@ code (oracle/_ref, built from the reference sources by oracle/build_ref.sh).
                       atoms, repeated variables, P = 0 / P = n, no join
                       result) with the counts the reference's
                       CandidateLiteralEvaluator produced.
+* batched_step_reference.npz (--batched-step, about 6 minutes) -- the
+                      reference's counts for every distinct literal of the
+                      full-size batched step with checksums of its inputs.
 * kinship.npz      -- the kinship knowledge base (relations, target) and the
                       reference learner's trace: every Evaluate call
                       (binding set, literals in result order, counts) and
@@ -31,6 +34,7 @@ sys.path.insert(0, ROOT)
 import oracle.ref as ref  # noqa: E402
 from quickfoil_gb300 import workloads  # noqa: E402
 from quickfoil_gb300.engine import Literal  # noqa: E402
+from tests.golden import input_checksum  # noqa: E402
 
 
 def pack_relations(relations, prefix, out):
@@ -172,6 +176,24 @@ def kinship():
     print("kinship.npz:", len(calls), "calls;", clauses)
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--batched-step" not in sys.argv:
     eval_cases()
     kinship()
+
+
+def batched_step_reference():
+    """Reference counts for every distinct literal of the full-size batched
+    step (32M x 6 bindings, 32 relations, 256 literals) plus checksums of the
+    generated inputs, so a test can regenerate the step and compare the GPU
+    engine with the reference's own counts at full size."""
+    w = workloads.batched_step()
+    lits = list(dict.fromkeys(w.literals))
+    counts = ref.evaluate(w.relations, w.binding_columns, w.num_positive, lits, radix_bits=5)
+    out = {"lits": pack_literals(lits), "counts": counts,
+           "checksum": np.array(input_checksum(w), dtype=np.uint64)}
+    np.savez_compressed(os.path.join(HERE, "batched_step_reference.npz"), **out)
+    print("batched_step_reference.npz:", len(lits), "literals")
+
+
+if __name__ == "__main__" and "--batched-step" in sys.argv:
+    batched_step_reference()

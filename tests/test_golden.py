@@ -27,6 +27,22 @@ def test_fixture_covers_the_edge_cases():
                for _, _, _, lits, _ in cases for l in lits)
 
 
+def test_batched_step_fixture_matches_the_workload_generator():
+    """The full-size batched step regenerates bit for bit (checksums of every
+    column), and the oracle reproduces the reference's counts on a sample of
+    its literals."""
+    from quickfoil_gb300 import workloads
+    lits, want, checksum = golden.batched_step_reference()
+    w = workloads.batched_step()
+    assert golden.input_checksum(w) == checksum
+    assert list(dict.fromkeys(w.literals)) == lits
+    pick = [i for i in range(len(lits)) if want[i].any()][:4] + \
+           [i for i in range(len(lits)) if not want[i].any()][:1]
+    got = oracle.evaluate(w.relations, w.binding_columns, w.num_positive,
+                          [lits[i].as_tuple() for i in pick], bits=5)
+    np.testing.assert_array_equal(got, want[pick])
+
+
 def test_kinship_learns_the_planted_rule():
     _, _, clauses = golden.kinship()
     # uncle(X, Y) :- male(X), sibling(Z, X), parent(Z, Y)

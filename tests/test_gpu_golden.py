@@ -64,3 +64,22 @@ def test_kinship_trace_replays_on_the_gpu(engine):
         best = max(s for s, _, _ in scored)
         chosen = [s for s, l, c in scored if l == lit and c[2:] == (npos, nneg)]
         assert chosen and chosen[0] == pytest.approx(best, abs=1e-5)
+
+
+def test_full_size_batched_step_matches_the_reference(engine):
+    """32M x 6 bindings, 32 relations, 256 literals (199 distinct): every
+    count equals the reference's own CandidateLiteralEvaluator output."""
+    from quickfoil_gb300 import workloads
+    lits, want, checksum = golden.batched_step_reference()
+    w = workloads.batched_step()
+    assert golden.input_checksum(w) == checksum
+    base = _register(engine, w.relations)
+    glits = [Literal(base + l.relation, l.vars, l.join_pos) for l in lits]
+    b = engine.bindings(w.binding_columns, w.num_positive)
+    np.testing.assert_array_equal(engine.evaluate_step(b, glits), want)
+    pick = list(range(0, len(glits), 25))
+    np.testing.assert_array_equal(engine.evaluate_per_literal(b, [glits[i] for i in pick]),
+                                  want[pick])
+    b.close()
+    for i in range(len(w.relations)):
+        engine.release_relation(base + i)
