@@ -38,11 +38,13 @@ namespace qfg {
 
 namespace {
 
-constexpr int kTile = 1536;            // binding rows per shared-memory tile
+constexpr int kTile = 1280;            // binding rows per shared-memory tile
+constexpr int kTargetRows = 1024;      // partition bits keep the mean partition below this
 constexpr int kSlots = 2048;           // key-table slots (power of two > kTile)
 constexpr int kEvalThreads = 256;
 constexpr int kGroupCols = QFG_MAX_ARITY;  // join column + up to 7 atom columns
 constexpr int kMaxLitsPerLaunch = 512;
+constexpr int kChunk = 2 * kEvalThreads;     // relation entries per work unit: two per thread
 constexpr int kMaxGroupLits = kEvalThreads;  // one thread per literal in the per-item prefix
 constexpr int kRound = 2048;           // rows staged per partition round
 constexpr int kPartThreads = 512;
@@ -414,20 +416,30 @@ bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, const int
 // ----------------------------------------------------------------------------
 // Persistent evaluation kernel.
 //
-// Work item = (group, partition).  The CTA gathers the partition's binding
-// rows (its positive and negative segments; join column + carried atom
-// columns) into shared memory, then builds a table of the distinct join
-// keys: 16-bit slot owners claimed with atomicCAS, per-slot row counts packed
-// as (positive count, negative count << 16), and, when the group has atom
-// literals, per-key row lists formed by an exclusive scan of the counts.
-// The group's literals' relation entries for the same partition range are
-// then processed as one flat index space (literal-major), so all threads stay
-// busy however few entries each literal has; per-literal counts are combined
-// with a segmented warp scan over lanes of equal literal and added once per
-// segment to per-CTA shared accumulators, flushed to global memory when the
-// CTA retires.  CTAs are small (256 threads) and three share an SM, so that
-// each barrier waits on few warps and one CTA's memory waits overlap the
-// others' shared-memory work.
+// Work unit = a range of at most kChunk relation entries of one (group,
+// partition) item.  A planning kernel lists the units of a launch: it reads
+// each item's segment bounds and the number of relation entries its literals
+// hold in the partition's key range, drops items without rows or entries,
+// and splits items with more than kChunk entries (hot join keys of skewed
+// relations) into several units so that no single CTA is left with a long
+// tail.  The evaluation CTA then repeatedly
+//   1. takes a unit (its record was prefetched while the previous unit ran),
+//   2. starts asynchronous copies (cp.async) of the partition's binding rows
+//      -- join column and the carried atom columns -- into shared memory,
+//   3. meanwhile forms the literal-major entry space of the item (one
+//      offsets pair per literal, block scan) and loads the key tuples and
+//      multiplicities of its own two entries into registers,
+//   4. builds the tile's distinct-key table: one 64-bit word per slot,
+//      (key << 32 | positive count | negative count << 16), claimed by a
+//      single atomicCAS, so a slot with a zero count is empty,
+//   5. for groups with atom literals, groups the tile's rows by key --
+//      positives first -- with a scan of the slot counts and permutes the atom
+//      columns into that order, so that the rows of a key are one contiguous
+//      range per label,
+//   6. probes the table with its entries and, for atom literals, compares the
+//      key's rows with the entry's further keys,
+//   7. combines per-literal sums with a segmented warp scan into per-CTA
+//      accumulators, flushed to global memory when the CTA retires.
 
 struct GroupDesc {
   const int32_t* cols;      // ncols SoA columns of n rows, partitioned
@@ -450,6 +462,12 @@ struct LitDesc {
   int8_t atom_col[QFG_MAX_ARITY];  // key q >= 1 is compared with group column atom_col[q]
 };
 
+struct WorkUnit {
+  uint32_t group, p;
+  uint32_t ps, Pp, ns, Np;   // positive / negative segment of the partition
+  uint32_t f0, f1;           // entry range in the item's literal-major space
+};
+
 struct EvalArgs {
   const GroupDesc* groups;
   int num_groups;
@@ -457,14 +475,78 @@ struct EvalArgs {
   int num_lits;
   int max_cols;
   int64_t total_items;
+  WorkUnit* units;
+  uint32_t* unit_count;
+  uint32_t unit_cap;
   unsigned int* work_counter;
   unsigned long long* counts;
 };
 
 size_t eval_smem_bytes(int num_lits, int max_cols) {
-  return sizeof(unsigned long long) * 4 * (size_t)num_lits +
-         sizeof(int32_t) * (size_t)max_cols * kTile + sizeof(uint32_t) * 2 * kSlots +
-         sizeof(uint32_t) * (2 * kMaxLitsPerLaunch + 2) + sizeof(uint16_t) * (kSlots + 2 * kTile);
+  return sizeof(unsigned long long) * (4 * (size_t)num_lits + kSlots) +
+         sizeof(int32_t) * (size_t)max_cols * kTile + sizeof(uint32_t) * kSlots +
+         sizeof(uint32_t) * 2 * (kMaxGroupLits + 1) + sizeof(uint16_t) * 2 * kTile;
+}
+
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+__global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
+  const int lane = lane_id();
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < a.total_items;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t item = base + threadIdx.x;
+    uint32_t nch = 0, E = 0;
+    WorkUnit u{};
+    if (item < a.total_items) {
+      int lo = 0, hi = a.num_groups - 1;  // largest g with item_begin <= item
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.groups[mid].item_begin <= item) lo = mid; else hi = mid - 1;
+      }
+      const GroupDesc& G = a.groups[lo];
+      const uint32_t p = G.p_lo + (uint32_t)(item - G.item_begin);
+      const int s = G.sbits;
+      const uint32_t hc = p >> s, sub = p & ((1u << s) - 1u);
+      const uint32_t ip = ((2u * hc) << s) + sub, in_ = ((2u * hc + 1u) << s) + sub;
+      u.group = (uint32_t)lo;
+      u.p = p;
+      u.ps = G.fstart[ip];
+      u.Pp = G.fstart[ip + 1] - u.ps;
+      u.ns = G.fstart[in_];
+      u.Np = G.fstart[in_ + 1] - u.ns;
+      if (u.Pp + u.Np > 0) {
+        const int rshift = kRelPartitionBits - G.bits;
+        const uint32_t q0 = p << rshift, q1 = (p + 1) << rshift;
+        for (int L = G.lit_begin; L < G.lit_end; ++L) {
+          const uint32_t* off = a.lits[L].offsets;
+          E += __ldg(off + q1) - __ldg(off + q0);
+        }
+        nch = (E + kChunk - 1) / kChunk;
+      }
+    }
+    uint32_t x = nch;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFullMask, x, o);
+      if (lane >= o) x += y;
+    }
+    const uint32_t warp_total = __shfl_sync(kFullMask, x, 31);
+    uint32_t wbase = 0;
+    if (lane == 31 && warp_total > 0) wbase = atomicAdd(a.unit_count, warp_total);
+    wbase = __shfl_sync(kFullMask, wbase, 31);
+    const uint32_t pos = wbase + x - nch;
+    for (uint32_t k = 0; k < nch; ++k) {
+      if (pos + k >= a.unit_cap) break;
+      u.f0 = k * kChunk;
+      u.f1 = umin(E, (k + 1) * kChunk);
+      a.units[pos + k] = u;
+    }
+  }
 }
 
 // Inclusive scan restricted to runs of equal `seg` across consecutive lanes.
@@ -479,229 +561,284 @@ __device__ __forceinline__ long long seg_scan(long long v, int seg) {
   return v;
 }
 
-constexpr unsigned short kNoOwner = 0xffffu;
+__device__ __forceinline__ void flush_acc(unsigned long long* dst, long long cp, long long cn,
+                                          long long bp, long long bn) {
+  if (cp) atomicAdd(dst + 0, as_ull(cp));
+  if (cn) atomicAdd(dst + 1, as_ull(cn));
+  if (bp) atomicAdd(dst + 2, as_ull(bp));
+  if (bn) atomicAdd(dst + 3, as_ull(bn));
+}
+
+// One relation entry held in registers.
+struct Entry {
+  int L;                 // literal within the group, -1 = none
+  int nk;
+  int32_t k0, kA, kB;    // join key, keys of the first two checked columns
+  int cA, cB, nchk;      // checked columns (smem column offsets), their count
+  bool ok0;              // keys compared with the join column itself match k0
+  uint32_t e;
+  long long mult;
+};
 
 __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem);
-  int32_t* scol = reinterpret_cast<int32_t*>(acc + 4 * a.num_lits);
-  uint32_t* cnt = reinterpret_cast<uint32_t*>(scol + a.max_cols * kTile);
-  uint32_t* lend = cnt + kSlots;
-  uint32_t* lstart = lend + kSlots;                 // kMaxLitsPerLaunch + 1
-  uint32_t* le0 = lstart + kMaxLitsPerLaunch + 1;   // kMaxLitsPerLaunch
-  unsigned short* owner = reinterpret_cast<unsigned short*>(le0 + kMaxLitsPerLaunch + 1);
-  uint16_t* rows = owner + kSlots;
-  uint16_t* rslot = rows + kTile;
-  __shared__ long long s_item;
+  unsigned long long* tbl = acc + 4 * a.num_lits;                     // kSlots
+  int32_t* raw = reinterpret_cast<int32_t*>(tbl + kSlots);            // max_cols * kTile
+  uint32_t* cur = reinterpret_cast<uint32_t*>(raw + a.max_cols * kTile);  // kSlots
+  uint32_t* lstart = cur + kSlots;                                    // kMaxGroupLits + 1
+  uint32_t* le0 = lstart + kMaxGroupLits + 1;                         // kMaxGroupLits + 1
+  uint16_t* rslot = reinterpret_cast<uint16_t*>(le0 + kMaxGroupLits + 1);  // kTile
+  uint16_t* rpos = rslot + kTile;                                     // kTile
+  __shared__ WorkUnit s_unit;
+  __shared__ uint32_t s_idx, s_count;
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
 
   for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) acc[i] = 0ull;
-  for (int i = threadIdx.x; i < kSlots; i += blockDim.x) {
-    owner[i] = kNoOwner;
-    cnt[i] = 0u;
+  for (int i = threadIdx.x; i < kSlots; i += blockDim.x) tbl[i] = 0ull;
+  if (threadIdx.x == 0) {
+    s_count = umin(*a.unit_count, a.unit_cap);
+    s_idx = atomicAdd(a.work_counter, 1u);
+    if (s_idx < s_count) s_unit = a.units[s_idx];
   }
   __syncthreads();
 
   for (;;) {
-    if (threadIdx.x == 0) s_item = (long long)atomicAdd(a.work_counter, 1u);
-    __syncthreads();
-    const long long item = s_item;
-    if (item >= a.total_items) break;
-    int g = 0;
-    while (g + 1 < a.num_groups && a.groups[g + 1].item_begin <= item) ++g;
-    const GroupDesc G = a.groups[g];
-    const uint32_t p = G.p_lo + (uint32_t)(item - G.item_begin);
-    const int s = G.sbits;
-    const uint32_t hc = p >> s, sub = p & ((1u << s) - 1u);
-    const uint32_t ip = ((2u * hc) << s) + sub, in_ = ((2u * hc + 1u) << s) + sub;
-    const uint32_t ps = G.fstart[ip], Pp = G.fstart[ip + 1] - ps;
-    const uint32_t ns = G.fstart[in_], Np = G.fstart[in_ + 1] - ns;
-    const uint32_t total = Pp + Np;
-    if (total == 0) {
-      __syncthreads();
-      continue;
+    const uint32_t idx = s_idx;
+    if (idx >= s_count) break;
+    const WorkUnit U = s_unit;
+    // The next unit's record loads while this one runs.
+    uint32_t nidx = 0;
+    WorkUnit nu{};
+    if (threadIdx.x == 0) {
+      nidx = atomicAdd(a.work_counter, 1u);
+      if (nidx < s_count) nu = a.units[nidx];
     }
-    const int rshift = kRelPartitionBits - G.bits;
-    const uint32_t q0 = p << rshift, q1 = (p + 1) << rshift;
-    const int m = G.lit_end - G.lit_begin;
+    const GroupDesc& G = a.groups[U.group];
+    const int32_t* __restrict__ gcols = G.cols;
+    const int64_t gn = G.n;
+    const int ncols = G.ncols;
+    const int lit_begin = G.lit_begin;
+    const int m = G.lit_end - lit_begin;
+    const bool has_atoms = G.has_atoms != 0;
+    const uint32_t total = U.Pp + U.Np;
 
-    // Entry ranges of the group's literals in this partition, flattened.
-    {
-      uint32_t c = 0;
-      if ((int)threadIdx.x < m) {
-        const LitDesc& d = a.lits[G.lit_begin + threadIdx.x];
-        const uint32_t e0 = __ldg(d.offsets + q0), e1 = __ldg(d.offsets + q1);
-        le0[threadIdx.x] = e0;
-        c = e1 - e0;
-      }
-      const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
-      if ((int)threadIdx.x < m) lstart[threadIdx.x] = ex;
-      if (threadIdx.x == 0) lstart[m] = s_total;
-      __syncthreads();
-    }
-    const uint32_t E = lstart[m];
-    if (E == 0) {
-      __syncthreads();
-      continue;
-    }
-
+    Entry ent[2];
+    long long bp = 0, bn = 0, cp = 0, cn = 0;
+    int Lrun = -1;
     for (uint32_t t0 = 0; t0 < total; t0 += kTile) {
       const int nt = (int)umin((uint32_t)kTile, total - t0);
-      const int npos = (int)umin((uint32_t)nt, Pp > t0 ? Pp - t0 : 0u);
-      for (int q = 0; q < G.ncols; ++q) {
-        const int32_t* __restrict__ src = G.cols + (int64_t)q * G.n;
-        int32_t* dst = scol + q * kTile;
-#pragma unroll 2
+      const int npos = (int)umin((uint32_t)nt, U.Pp > t0 ? U.Pp - t0 : 0u);
+      for (int q = 0; q < ncols; ++q) {
+        const int32_t* src = gcols + (int64_t)q * gn;
+        int32_t* dst = raw + q * kTile;
         for (int i = threadIdx.x; i < nt; i += blockDim.x) {
           const uint32_t v = t0 + i;
-          dst[i] = __ldg(src + (v < Pp ? ps + v : ns + (v - Pp)));
+          cp_async4(dst + i, src + (v < U.Pp ? U.ps + v : U.ns + (v - U.Pp)));
         }
       }
+      cp_async_commit();
+      if (t0 == 0) {
+        // Literal-major entry space of the item, then this thread's entries.
+        const int rshift = kRelPartitionBits - G.bits;
+        const uint32_t q0 = U.p << rshift, q1 = (U.p + 1) << rshift;
+        uint32_t c = 0;
+        if ((int)threadIdx.x < m) {
+          const uint32_t* off = a.lits[lit_begin + threadIdx.x].offsets;
+          const uint32_t e0 = __ldg(off + q0), e1 = __ldg(off + q1);
+          le0[threadIdx.x] = e0;
+          c = e1 - e0;
+        }
+        const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
+        if ((int)threadIdx.x < m) lstart[threadIdx.x] = ex;
+        if (threadIdx.x == 0) lstart[m] = s_total;
+        __syncthreads();
+        const uint32_t fbase = U.f0 + 2u * threadIdx.x;
+        int L = -1;
+        if (fbase < U.f1) {
+          int lo = 0, hi = m - 1;  // largest L with lstart[L] <= fbase
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (lstart[mid] <= fbase) lo = mid; else hi = mid - 1;
+          }
+          L = lo;
+        }
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const uint32_t f = fbase + j;
+          Entry& x = ent[j];
+          x.L = -1;
+          if (L < 0 || f >= U.f1) continue;
+          while (f >= lstart[L + 1]) ++L;
+          const LitDesc& d = a.lits[lit_begin + L];
+          const int32_t* __restrict__ kp = d.keys;
+          x.L = L;
+          x.nk = d.nk;
+          x.e = le0[L] + (f - lstart[L]);
+          x.k0 = __ldg(kp + x.e);
+          x.mult = __ldg(d.mult + x.e);
+          x.ok0 = true;
+          x.nchk = 0;
+          x.kA = x.kB = 0;
+          x.cA = x.cB = 0;
+          for (int q = 1; q < x.nk; ++q) {
+            const int ac = d.atom_col[q];
+            const int32_t kq = __ldg(kp + q * d.stride + x.e);
+            if (ac == 0) {
+              x.ok0 = x.ok0 && kq == x.k0;
+            } else {
+              if (x.nchk == 0) { x.kA = kq; x.cA = ac * kTile; }
+              else if (x.nchk == 1) { x.kB = kq; x.cB = ac * kTile; }
+              ++x.nchk;
+            }
+          }
+        }
+      }
+      cp_async_wait_all();
       __syncthreads();
-      // Distinct join keys of the tile with per-label row counts (the table
-      // is all-empty here: zeroed at kernel start, reset after every tile).
+      // Distinct join keys of the tile.
       for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-        const int32_t key = scol[i];
+        const int32_t key = raw[i];
+        const uint32_t inc = i < npos ? 1u : 0x10000u;
+        const unsigned long long mine = ((unsigned long long)(uint32_t)key << 32) | inc;
         uint32_t slot = mix32((uint32_t)key) & (kSlots - 1);
         for (int probe = 0; probe < kSlots; ++probe) {
-          const unsigned short o = atomicCAS(&owner[slot], kNoOwner, (unsigned short)i);
-          if (o == kNoOwner || scol[o] == key) break;
+          unsigned long long w = *reinterpret_cast<volatile unsigned long long*>(&tbl[slot]);
+          if (w == 0ull) {
+            w = atomicCAS(&tbl[slot], 0ull, mine);
+            if (w == 0ull) break;
+          }
+          if ((uint32_t)(w >> 32) == (uint32_t)key) {
+            atomicAdd(&tbl[slot], (unsigned long long)inc);
+            break;
+          }
           slot = (slot + 1) & (kSlots - 1);
         }
         rslot[i] = (uint16_t)slot;
-        atomicAdd(&cnt[slot], i < npos ? 1u : 0x10000u);
       }
       __syncthreads();
-      if (G.has_atoms) {
-        // Row lists per key: exclusive scan of row counts, then fill; after
-        // the fill lend[s] is the end of slot s's list.
+      if (has_atoms) {
+        // Rows grouped by key, positives first: cur[s] packs the positive
+        // cursor (low half) and the negative cursor (high half); after the
+        // fill its high half is the end of slot s's rows.
         constexpr int kPer = kSlots / kEvalThreads;
-        uint32_t v[kPer];
+        uint32_t v[kPer], pc[kPer];
         uint32_t sum = 0;
 #pragma unroll
         for (int k = 0; k < kPer; ++k) {
-          const uint32_t w = cnt[threadIdx.x * kPer + k];
-          v[k] = (w & 0xffffu) + (w >> 16);
+          const uint32_t w = (uint32_t)tbl[threadIdx.x * kPer + k];
+          pc[k] = w & 0xffffu;
+          v[k] = pc[k] + (w >> 16);
           sum += v[k];
         }
         uint32_t run = block_scan_excl(sum, s_warp, &s_total);
 #pragma unroll
         for (int k = 0; k < kPer; ++k) {
-          lend[threadIdx.x * kPer + k] = run;
+          cur[threadIdx.x * kPer + k] = run | ((run + pc[k]) << 16);
           run += v[k];
         }
         __syncthreads();
         for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-          const uint32_t pos = atomicAdd(&lend[rslot[i]], 1u);
-          rows[pos] = (uint16_t)i;
+          const uint32_t old = atomicAdd(&cur[rslot[i]], i < npos ? 1u : 0x10000u);
+          rpos[i] = (uint16_t)(i < npos ? (old & 0xffffu) : (old >> 16));
+        }
+        // Permute the atom columns into key order, in place: every thread
+        // holds its rows' values of one column across a barrier.
+        constexpr int kRowsPer = (kTile + kEvalThreads - 1) / kEvalThreads;
+        for (int q = 1; q < ncols; ++q) {
+          int32_t* col = raw + q * kTile;
+          int32_t val[kRowsPer];
+#pragma unroll
+          for (int k = 0; k < kRowsPer; ++k) {
+            const int i = threadIdx.x + k * kEvalThreads;
+            if (i < nt) val[k] = col[i];
+          }
+          __syncthreads();
+#pragma unroll
+          for (int k = 0; k < kRowsPer; ++k) {
+            const int i = threadIdx.x + k * kEvalThreads;
+            if (i < nt) col[rpos[i]] = val[k];
+          }
         }
         __syncthreads();
       }
-      // Flat pass over (literal, entry) of this partition: each thread takes
-      // a contiguous range of the literal-major entry space, keeps running
-      // sums while the literal stays the same, and adds them to the CTA
-      // accumulators when it changes; the last literal of every thread is
-      // combined across lanes with one segmented warp scan.
-      {
-        const uint32_t per = (E + blockDim.x - 1) / blockDim.x;
-        uint32_t f = threadIdx.x * per;
-        const uint32_t fend = umin(E, f + per);
-        int L = -1;
-        long long bp = 0, bn = 0, cp = 0, cn = 0;
-        if (f < fend) {
-          int lo = 0, hi = m - 1;  // largest L with lstart[L] <= f
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (lstart[mid] <= f) lo = mid; else hi = mid - 1;
-          }
-          L = lo;
+      // This thread's entries against the tile.
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const Entry& x = ent[j];
+        if (x.L < 0) continue;
+        if (x.L != Lrun) {
+          if (Lrun >= 0 && (cp | cn | bp | bn) != 0)
+            flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
+          bp = bn = cp = cn = 0;
+          Lrun = x.L;
         }
-        for (; f < fend; ++f) {
-          if (f >= lstart[L + 1]) {
-            if ((cp | cn | bp | bn) != 0) {
-              unsigned long long* dst = acc + 4 * (G.lit_begin + L);
-              if (cp) atomicAdd(dst + 0, as_ull(cp));
-              if (cn) atomicAdd(dst + 1, as_ull(cn));
-              if (bp) atomicAdd(dst + 2, as_ull(bp));
-              if (bn) atomicAdd(dst + 3, as_ull(bn));
-            }
-            bp = bn = cp = cn = 0;
-            do ++L; while (f >= lstart[L + 1]);
-          }
-          const LitDesc& d = a.lits[G.lit_begin + L];
-          const uint32_t e = le0[L] + (f - lstart[L]);
-          const int32_t k0 = __ldg(d.keys + e);
-          uint32_t slot = mix32((uint32_t)k0) & (kSlots - 1);
-          unsigned short o = kNoOwner;
-          for (int probe = 0; probe < kSlots; ++probe) {
-            o = owner[slot];
-            if (o == kNoOwner || scol[o] == k0) break;
-            slot = (slot + 1) & (kSlots - 1);
-          }
-          if (o == kNoOwner || scol[o] != k0) continue;
-          const long long mlt = __ldg(d.mult + e);
-          const int nk = d.nk;
-          const uint32_t w = cnt[slot];
-          if (nk == 1) {
-            const uint32_t P = w & 0xffffu, N = w >> 16;
-            bp += mlt * P;
-            bn += mlt * N;
-            cp += P;
-            cn += N;
+        if (!x.ok0) continue;
+        uint32_t slot = mix32((uint32_t)x.k0) & (kSlots - 1);
+        unsigned long long w = 0;
+        for (int probe = 0; probe < kSlots; ++probe) {
+          w = tbl[slot];
+          if ((uint32_t)w == 0u || (int32_t)(w >> 32) == x.k0) break;
+          slot = (slot + 1) & (kSlots - 1);
+        }
+        const uint32_t P = (uint32_t)w & 0xffffu, N = ((uint32_t)w >> 16) & 0xffffu;
+        if (P + N == 0u) continue;
+        uint32_t hp = 0, hn = 0;
+        if (x.nchk == 0) {
+          hp = P;
+          hn = N;
+        } else {
+          const uint32_t end = cur[slot] >> 16;
+          const uint32_t mid = end - N;
+          const uint32_t beg = mid - P;
+          if (x.nchk == 1) {
+            const int32_t* ca = raw + x.cA;
+            for (uint32_t r = beg; r < mid; ++r) hp += ca[r] == x.kA;
+            for (uint32_t r = mid; r < end; ++r) hn += ca[r] == x.kA;
+          } else if (x.nchk == 2) {
+            const int32_t* ca = raw + x.cA;
+            const int32_t* cb = raw + x.cB;
+            for (uint32_t r = beg; r < mid; ++r) hp += (ca[r] == x.kA) & (cb[r] == x.kB);
+            for (uint32_t r = mid; r < end; ++r) hn += (ca[r] == x.kA) & (cb[r] == x.kB);
           } else {
-            int32_t kq[QFG_MAX_ARITY];
-            int col[QFG_MAX_ARITY];
-#pragma unroll
-            for (int q = 1; q < QFG_MAX_ARITY; ++q) {
-              if (q < nk) {
-                kq[q] = __ldg(d.keys + q * d.stride + e);
-                col[q] = d.atom_col[q] * kTile;
-              }
-            }
-            const uint32_t end = lend[slot];
-            const uint32_t beg = end - ((w & 0xffffu) + (w >> 16));
-            for (uint32_t x = beg; x < end; ++x) {
-              const int row = rows[x];
+            const LitDesc& d = a.lits[lit_begin + x.L];
+            for (uint32_t r = beg; r < end; ++r) {
               bool pass = true;
-#pragma unroll
-              for (int q = 1; q < QFG_MAX_ARITY; ++q)
-                if (q < nk && scol[col[q] + row] != kq[q]) pass = false;
-              if (!pass) continue;
-              if (row < npos) {
-                bp += mlt;
-                cp += 1;
-              } else {
-                bn += mlt;
-                cn += 1;
+              for (int q = 1; q < x.nk && pass; ++q) {
+                const int ac = d.atom_col[q];
+                if (ac != 0) pass = raw[ac * kTile + r] == __ldg(d.keys + q * d.stride + x.e);
+              }
+              if (pass) {
+                if (r < mid) ++hp; else ++hn;
               }
             }
           }
         }
-        // Lanes' ranges are contiguous and increasing, so equal literals sit
-        // on consecutive lanes; idle lanes (L = -1) trail.
-        cp = seg_scan(cp, L);
-        cn = seg_scan(cn, L);
-        bp = seg_scan(bp, L);
-        bn = seg_scan(bn, L);
-        const int next_L = __shfl_down_sync(kFullMask, L, 1);
-        const bool seg_end = lane_id() == 31 || next_L != L;
-        if (seg_end && L >= 0 && (cp | cn | bp | bn) != 0) {
-          unsigned long long* dst = acc + 4 * (G.lit_begin + L);
-          if (cp) atomicAdd(dst + 0, as_ull(cp));
-          if (cn) atomicAdd(dst + 1, as_ull(cn));
-          if (bp) atomicAdd(dst + 2, as_ull(bp));
-          if (bn) atomicAdd(dst + 3, as_ull(bn));
-        }
+        bp += x.mult * hp;
+        bn += x.mult * hn;
+        cp += hp;
+        cn += hn;
       }
       __syncthreads();
-      // Return the touched slots to empty for the next tile.
-      for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-        owner[rslot[i]] = kNoOwner;
-        cnt[rslot[i]] = 0u;
-      }
+      for (int i = threadIdx.x; i < nt; i += blockDim.x) tbl[rslot[i]] = 0ull;
       __syncthreads();
     }
+    // Threads' entries are contiguous and increasing, so equal literals sit
+    // on consecutive lanes; idle lanes (Lrun = -1) trail.
+    cp = seg_scan(cp, Lrun);
+    cn = seg_scan(cn, Lrun);
+    bp = seg_scan(bp, Lrun);
+    bn = seg_scan(bn, Lrun);
+    const int next_L = __shfl_down_sync(kFullMask, Lrun, 1);
+    const bool seg_end = lane_id() == 31 || next_L != Lrun;
+    if (seg_end && Lrun >= 0 && (cp | cn | bp | bn) != 0)
+      flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
+    if (threadIdx.x == 0) {
+      s_idx = nidx;
+      if (nidx < s_count) s_unit = nu;
+    }
+    __syncthreads();
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) {
@@ -713,7 +850,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
 int auto_group_bits(Ctx* ctx, int64_t n) {
   if (ctx->eval_bits > 0) return std::min(ctx->eval_bits, kMaxPartitionBits);
   int bits = 1;
-  while (bits < kMaxPartitionBits && 3 * (n >> bits) > 2 * kTile) ++bits;
+  while (bits < kMaxPartitionBits && (n >> bits) > kTargetRows) ++bits;
   return bits;
 }
 
@@ -866,6 +1003,7 @@ struct LaunchJob {
   EvalArgs ea;
   size_t smem;
   int grid;
+  int plan_grid;
 };
 
 struct PreparedStep {
@@ -880,7 +1018,7 @@ struct PreparedStep {
   std::vector<LaunchJob> launches;
   std::vector<unsigned char> blob;  // descriptors, to be copied to blob_dev
   void* blob_dev = nullptr;
-  unsigned int* counter = nullptr;
+  unsigned int* counter = nullptr;  // [work counter, unit count]
 };
 
 int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
@@ -1026,11 +1164,24 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   memcpy(ps->blob.data(), sub_all.data(), gbytes);
   memcpy(ps->blob.data() + gbytes, ldesc.data(), lbytes);
   QFG_TRY(ctx->scratch[kScrLits].reserve(ctx, ps->blob.size() + 64));
+  // Work units: at most one per item plus one per kChunk entries.
+  std::vector<int64_t> caps;
+  int64_t max_cap = 1;
+  for (const Span& S : spans) {
+    int64_t cap = 1;
+    for (size_t g = S.gbeg; g < S.gend; ++g) cap += (int64_t)(shard_hi - shard_lo);
+    for (int l = S.lit0; l < S.lit0 + S.nl; ++l) cap += ldesc[l].stride / kChunk + 1;
+    if (cap > (int64_t)UINT32_MAX) return set_error(ctx, QFG_ERR_INVALID, "too many work units");
+    caps.push_back(cap);
+    max_cap = std::max(max_cap, cap);
+  }
+  QFG_TRY(ctx->scratch[kScrWork].reserve(ctx, sizeof(WorkUnit) * (size_t)max_cap));
   GroupDesc* gdev = ctx->scratch[kScrLits].as<GroupDesc>();
   LitDesc* ldev = reinterpret_cast<LitDesc*>(gdev + sub_all.size());
   ps->blob_dev = gdev;
   ps->counter = reinterpret_cast<unsigned int*>(ldev + ldesc.size());
-  for (const Span& S : spans) {
+  for (size_t si = 0; si < spans.size(); ++si) {
+    const Span& S = spans[si];
     LaunchJob L;
     EvalArgs& ea = L.ea;
     ea.groups = gdev + S.gbeg;
@@ -1039,6 +1190,9 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     ea.num_lits = S.nl;
     ea.total_items = (int64_t)(S.gend - S.gbeg) * (int64_t)(shard_hi - shard_lo);
     ea.work_counter = ps->counter;
+    ea.units = ctx->scratch[kScrWork].as<WorkUnit>();
+    ea.unit_count = ps->counter + 1;
+    ea.unit_cap = (uint32_t)caps[si];
     ea.counts = counts;
     ea.max_cols = 1;
     for (size_t g = S.gbeg; g < S.gend; ++g) ea.max_cols = std::max(ea.max_cols, gdesc[g].ncols);
@@ -1049,6 +1203,8 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_batched_kernel,
                                                                kEvalThreads, L.smem));
     L.grid = ctx->num_sms * std::max(per_sm, 1);
+    L.plan_grid = (int)std::max<int64_t>(
+        1, std::min<int64_t>((ea.total_items + 255) / 256, (int64_t)ctx->num_sms * 8));
     ps->launches.push_back(L);
   }
   return QFG_OK;
@@ -1083,7 +1239,9 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
   QFG_TRY(stage_end(ctx, QFG_STAGE_BIND_PARTITION));
   QFG_TRY(stage_begin(ctx, QFG_STAGE_EVALUATE));
   for (const LaunchJob& L : ps.launches) {
-    QFG_CUDA(ctx, cudaMemsetAsync(ps.counter, 0, sizeof(unsigned int), ctx->stream));
+    QFG_CUDA(ctx, cudaMemsetAsync(ps.counter, 0, 2 * sizeof(unsigned int), ctx->stream));
+    plan_units_kernel<<<L.plan_grid, 256, 0, ctx->stream>>>(L.ea);
+    QFG_LAUNCHED(ctx);
     eval_batched_kernel<<<L.grid, kEvalThreads, L.smem, ctx->stream>>>(L.ea);
     QFG_LAUNCHED(ctx);
   }
@@ -1120,6 +1278,9 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
   }
   if (two_pass) words += (int64_t)max_ncols * nb;
   words += (int64_t)np1 * (ctx->num_sms * 2 + 3);
+  int64_t units = (int64_t)plan.groups.size() << bits;
+  for (KeyTable* kt : plan.tables) units += kt->num_entries / kChunk + 1;
+  words += units * (int64_t)(sizeof(WorkUnit) / 4);
   *bytes = 4 * words + (int64_t)(sizeof(GroupDesc) + sizeof(LitDesc)) * n + 32 * (int64_t)n;
   return QFG_OK;
 }
