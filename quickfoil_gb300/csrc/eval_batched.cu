@@ -46,8 +46,8 @@ constexpr int kGroupCols = QFG_MAX_ARITY;  // join column + up to 7 atom columns
 constexpr int kMaxLitsPerLaunch = 512;
 constexpr int kChunk = 2 * kEvalThreads;     // relation entries per work unit: two per thread
 constexpr int kMaxGroupLits = kEvalThreads;  // one thread per literal in the per-item prefix
-constexpr int kRound = 2048;           // rows staged per partition round
-constexpr int kPartThreads = 512;
+constexpr int kRound = 4096;           // rows staged per partition round
+constexpr int kPartThreads = 1024;
 constexpr int kMaxCoarseBits = 7;      // pass 1 fan-out: 2 << 7 = 256 bins
 constexpr int kMaxSubBits = 9;         // pass 2 fan-out: up to 512 sub-bins
 constexpr int kMaxPartitionBits = kMaxCoarseBits + kMaxSubBits;
@@ -199,7 +199,7 @@ __device__ __forceinline__ int lane_of(const int4& v, int k) {
 }
 
 template <bool kVec>
-__global__ void __launch_bounds__(kPartThreads, 2) bpart_hist_kernel(BPartArgs a) {
+__global__ void __launch_bounds__(kPartThreads, 1) bpart_hist_kernel(BPartArgs a) {
   __shared__ uint32_t p1[2 << (kMaxCoarseBits + 1)];
   const int np1 = 2 << a.cbits;
   for (int i = threadIdx.x; i < np1; i += blockDim.x) p1[i] = 0;
@@ -238,102 +238,135 @@ __global__ void __launch_bounds__(kPartThreads, 2) bpart_hist_kernel(BPartArgs a
   }
 }
 
-// Shared-memory staging for one round of up to kRound rows of ncols columns.
+// Round processing, templated on the number of carried columns NC so that
+// every per-column loop unrolls without predicated-off lanes.  A round of
+// kRound rows lives in shared memory (NC columns) while the next round's rows
+// are already loading into registers; the round is counting-sorted by bin in
+// shared memory and written so that the threads writing one bin's run write
+// consecutive addresses.
 struct RoundSmem {
-  int32_t* rows;      // ncols * kRound
-  uint16_t* bin;      // kRound
-  uint16_t* rank;     // kRound
-  uint16_t* perm;     // kRound
+  int32_t* rows;      // NC * kRound
+  uint32_t* br;       // kRound: bin << 16 | rank within the bin
+  uint16_t* perm;     // kRound: sorted position -> row
   uint32_t* lcount;   // nbins
   uint32_t* lstart;   // nbins
-  uint32_t* cursor;   // nbins (global output cursor of each bin)
+  uint32_t* gpos;     // nbins: output position of sorted position 0 of bin b
+  uint32_t* cursor;   // nbins: output cursor of each bin
 };
 
 __device__ __forceinline__ RoundSmem carve_round(unsigned char* smem, int ncols, int nbins) {
   RoundSmem S;
   S.rows = reinterpret_cast<int32_t*>(smem);
-  S.bin = reinterpret_cast<uint16_t*>(S.rows + ncols * kRound);
-  S.rank = S.bin + kRound;
-  S.perm = S.rank + kRound;
+  S.br = reinterpret_cast<uint32_t*>(S.rows + ncols * kRound);
+  S.perm = reinterpret_cast<uint16_t*>(S.br + kRound);
   S.lcount = reinterpret_cast<uint32_t*>(S.perm + kRound);
   S.lstart = S.lcount + nbins;
-  S.cursor = S.lstart + nbins;
+  S.gpos = S.lstart + nbins;
+  S.cursor = S.gpos + nbins;
   return S;
 }
 
 size_t round_smem_bytes(int ncols, int nbins) {
-  return sizeof(int32_t) * (size_t)ncols * kRound + 3 * sizeof(uint16_t) * kRound +
-         3 * sizeof(uint32_t) * (size_t)nbins;
+  return sizeof(int32_t) * (size_t)ncols * kRound + (sizeof(uint32_t) + sizeof(uint16_t)) * kRound +
+         4 * sizeof(uint32_t) * (size_t)nbins;
 }
 
-// Counting-sorts the staged round by bin (nbins <= blockDim.x; lcount zero on
-// entry) and writes it out: sorted position k goes to cursor[bin] +
-// (k - lstart[bin]), so the threads writing one bin's run write consecutive
-// addresses.
-__device__ __forceinline__ void write_round(const RoundSmem& S, int nt, int nbins, int ncols,
-                                            int32_t* __restrict__ out, int64_t out_stride,
-                                            uint32_t* s_warp, uint32_t* s_total) {
-  for (int i = threadIdx.x; i < nt; i += blockDim.x)
-    S.rank[i] = (uint16_t)atomicAdd(&S.lcount[S.bin[i]], 1u);
-  __syncthreads();
-  const uint32_t c = (int)threadIdx.x < nbins ? S.lcount[threadIdx.x] : 0u;
-  const uint32_t ex = block_scan_excl(c, s_warp, s_total);
-  if ((int)threadIdx.x < nbins) S.lstart[threadIdx.x] = ex;
-  __syncthreads();
-  for (int i = threadIdx.x; i < nt; i += blockDim.x) S.perm[S.lstart[S.bin[i]] + S.rank[i]] = (uint16_t)i;
-  __syncthreads();
-  for (int k = threadIdx.x; k < nt; k += blockDim.x) {
-    const int i = S.perm[k];
-    const int b = S.bin[i];
-    const int64_t g = (int64_t)S.cursor[b] + (k - (int)S.lstart[b]);
-    for (int q = 0; q < ncols; ++q) out[(int64_t)q * out_stride + g] = S.rows[q * kRound + i];
-  }
-  __syncthreads();
-  if ((int)threadIdx.x < nbins) {
-    S.cursor[threadIdx.x] += S.lcount[threadIdx.x];
-    S.lcount[threadIdx.x] = 0u;
-  }
-  __syncthreads();
-}
-
-// Stages rows [0, nt) of up to kGroupCols columns (column q starts at
-// src[q]) into S.rows.  All loads of a thread are issued before any store so
-// that they are in flight together.
 constexpr int kRowsPerThread = kRound / kPartThreads;
 
-__device__ __forceinline__ void load_round(const int32_t* const* src, int ncols, int nt,
-                                           int32_t* rows) {
-  int32_t v[kGroupCols][kRowsPerThread];
+template <int NC>
+__device__ __forceinline__ void load_rows(int32_t (&v)[NC][kRowsPerThread], const int32_t* const (&src)[NC],
+                                          uint32_t rr, int nt) {
 #pragma unroll
-  for (int q = 0; q < kGroupCols; ++q) {
-    if (q < ncols) {
+  for (int k = 0; k < kRowsPerThread; ++k) {
+    const int i = threadIdx.x + k * kPartThreads;
 #pragma unroll
-      for (int k = 0; k < kRowsPerThread; ++k) {
-        const int i = threadIdx.x + k * kPartThreads;
-        v[q][k] = i < nt ? __ldg(src[q] + i) : 0;
-      }
-    }
+    for (int q = 0; q < NC; ++q) v[q][k] = i < nt ? __ldg(src[q] + rr + i) : 0;
   }
+}
+
+// Rows [r0, r1): staging and ranking, a block scan of the bin counts (which
+// also advances the output cursors), the permutation and the writes, each
+// separated by a barrier.
+// Rounds never straddle `split` (the first negative row in pass 1), so a
+// round's rows share one label and fan out to half the bins.
+__device__ __forceinline__ uint32_t round_end(uint32_t rr, uint32_t r1, uint32_t split) {
+  const uint32_t e = umin(r1, rr + kRound);
+  return (rr < split && split < e) ? split : e;
+}
+
+template <int NC, typename BinFn>
+__device__ __forceinline__ void stream_rounds(const RoundSmem& S, const int32_t* const (&src)[NC],
+                                              uint32_t r0, uint32_t r1, uint32_t split, int nbins,
+                                              int32_t* const (&out)[NC], uint32_t* s_warp,
+                                              uint32_t* s_total, BinFn bin_of) {
+  if (r0 >= r1) return;
+  int32_t v[NC][kRowsPerThread];
+  uint32_t re = round_end(r0, r1, split);
+  load_rows<NC>(v, src, r0, (int)(re - r0));
+  for (uint32_t rr = r0; rr < r1;) {
+    const uint32_t rend = re;
+    const int nt = (int)(rend - rr);
 #pragma unroll
-  for (int q = 0; q < kGroupCols; ++q) {
-    if (q < ncols) {
+    for (int k = 0; k < kRowsPerThread; ++k) {
+      const int i = threadIdx.x + k * kPartThreads;
+      if (i < nt) {
 #pragma unroll
-      for (int k = 0; k < kRowsPerThread; ++k) {
-        const int i = threadIdx.x + k * kPartThreads;
-        if (i < nt) rows[q * kRound + i] = v[q][k];
+        for (int q = 0; q < NC; ++q) S.rows[q * kRound + i] = v[q][k];
+        const uint32_t bin = bin_of(v[0][k], rr + i);
+        S.br[i] = (bin << 16) | atomicAdd(&S.lcount[bin], 1u);
       }
     }
+    __syncthreads();
+    if (rend < r1) {
+      re = round_end(rend, r1, split);
+      load_rows<NC>(v, src, rend, (int)(re - rend));
+    }
+    {
+      // Exclusive scan of the bin counts, one bin per thread (nbins <=
+      // blockDim.x); each bin's output cursor advances by its count.
+      const uint32_t c = (int)threadIdx.x < nbins ? S.lcount[threadIdx.x] : 0u;
+      const uint32_t ex = block_scan_excl(c, s_warp, s_total);
+      if ((int)threadIdx.x < nbins) {
+        S.lstart[threadIdx.x] = ex;
+        S.gpos[threadIdx.x] = S.cursor[threadIdx.x] - ex;
+        S.cursor[threadIdx.x] += c;
+        S.lcount[threadIdx.x] = 0u;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kRowsPerThread; ++k) {
+      const int i = threadIdx.x + k * kPartThreads;
+      if (i < nt) {
+        const uint32_t w = S.br[i];
+        S.perm[S.lstart[w >> 16] + (w & 0xffffu)] = (uint16_t)i;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kRowsPerThread; ++k) {
+      const int kk = threadIdx.x + k * kPartThreads;
+      if (kk < nt) {
+        const int i = S.perm[kk];
+        const uint32_t g = S.gpos[S.br[i] >> 16] + (uint32_t)kk;
+#pragma unroll
+        for (int q = 0; q < NC; ++q) out[q][g] = S.rows[q * kRound + i];
+      }
+    }
+    __syncthreads();
+    rr = rend;
   }
 }
 
 // Pass 1: the CTA's chunk of the original columns into pass-1 bins.
-__global__ void __launch_bounds__(kPartThreads, 2)
+template <int NC>
+__global__ void __launch_bounds__(kPartThreads, 1)
 bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   const int np1 = 2 << a.cbits;
-  const RoundSmem S = carve_round(smem, a.ncols, np1);
+  const RoundSmem S = carve_round(smem, NC, np1);
   for (int i = threadIdx.x; i < np1; i += blockDim.x) {
     S.cursor[i] = p1_start[i] + a.p1_base[(int64_t)blockIdx.x * np1 + i];
     S.lcount[i] = 0u;
@@ -341,26 +374,26 @@ bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* 
   __syncthreads();
   int64_t r0, r1;
   cta_range4(a.n, &r0, &r1);
-  for (int64_t rr = r0; rr < r1; rr += kRound) {
-    const int nt = (int)(r1 - rr < kRound ? r1 - rr : (int64_t)kRound);
-    {
-      const int32_t* src[kGroupCols];
+  const int32_t* src[NC];
+  int32_t* dst[NC];
 #pragma unroll
-      for (int q = 0; q < kGroupCols; ++q) src[q] = q < a.ncols ? a.cols[q] + rr : nullptr;
-      load_round(src, a.ncols, nt, S.rows);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nt; i += blockDim.x)
-      S.bin[i] = (uint16_t)((top_bits(S.rows[i], a.cbits) << 1) | (rr + i >= a.npos ? 1u : 0u));
-    __syncthreads();
-    write_round(S, nt, np1, a.ncols, out, a.n, s_warp, &s_total);
+  for (int q = 0; q < NC; ++q) {
+    src[q] = a.cols[q];
+    dst[q] = out + (int64_t)q * a.n;
   }
+  const int cbits = a.cbits;
+  const uint32_t npos = (uint32_t)a.npos;
+  stream_rounds<NC>(S, src, (uint32_t)r0, (uint32_t)r1, npos, np1, dst, s_warp, &s_total,
+                    [=](int32_t key, uint32_t r) {
+                      return (top_bits(key, cbits) << 1) | (r >= npos ? 1u : 0u);
+                    });
 }
 
 // Pass 2: CTA b splits pass-1 bin b = (hash prefix c, label) inside its own
 // range into sub-bins 0 .. 2^sbits - 1 and records where each starts:
 // fine_start[(b << sbits) + sub] (the last CTA also writes the end, n).
-__global__ void __launch_bounds__(kPartThreads, 2)
+template <int NC>
+__global__ void __launch_bounds__(kPartThreads, 1)
 bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, const int32_t* __restrict__ in,
                    uint32_t* __restrict__ fine_start, int32_t* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -368,50 +401,79 @@ bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, const int
   __shared__ uint32_t s_total;
   const int sbits = a.bits - a.cbits;
   const int nsub = 1 << sbits;
-  const RoundSmem S = carve_round(smem, a.ncols, nsub);
+  const RoundSmem S = carve_round(smem, NC, nsub);
   const int b = blockIdx.x;
-  const int64_t r0 = p1_start[b], r1 = p1_start[b + 1];
+  const uint32_t r0 = p1_start[b], r1 = p1_start[b + 1];
   for (int i = threadIdx.x; i < nsub; i += blockDim.x) S.lcount[i] = 0u;
   __syncthreads();
+  const uint32_t mask = (uint32_t)(nsub - 1);
+  const int bits = a.bits;
   {
     // Eight independent key loads per thread per iteration.
-    const uint32_t mask = (uint32_t)(nsub - 1);
-    int64_t r = r0 + threadIdx.x;
-    for (; r + 7 * (int64_t)blockDim.x < r1; r += 8 * (int64_t)blockDim.x) {
+    uint32_t r = r0 + threadIdx.x;
+    for (; r + 7 * blockDim.x < r1; r += 8 * blockDim.x) {
       int32_t k[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) k[j] = __ldg(in + r + j * (int64_t)blockDim.x);
+      for (int j = 0; j < 8; ++j) k[j] = __ldg(in + r + j * blockDim.x);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) atomicAdd(&S.lcount[top_bits(k[j], a.bits) & mask], 1u);
+      for (int j = 0; j < 8; ++j) atomicAdd(&S.lcount[top_bits(k[j], bits) & mask], 1u);
     }
-    for (; r < r1; r += blockDim.x) atomicAdd(&S.lcount[top_bits(__ldg(in + r), a.bits) & mask], 1u);
+    for (; r < r1; r += blockDim.x) atomicAdd(&S.lcount[top_bits(__ldg(in + r), bits) & mask], 1u);
   }
   __syncthreads();
   const uint32_t c = (int)threadIdx.x < nsub ? S.lcount[threadIdx.x] : 0u;
   const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
   if ((int)threadIdx.x < nsub) {
-    S.cursor[threadIdx.x] = (uint32_t)r0 + ex;
-    fine_start[((int64_t)b << sbits) + threadIdx.x] = (uint32_t)r0 + ex;
+    S.cursor[threadIdx.x] = r0 + ex;
+    fine_start[((int64_t)b << sbits) + threadIdx.x] = r0 + ex;
     S.lcount[threadIdx.x] = 0u;
   }
   if (b == (int)gridDim.x - 1 && threadIdx.x == 0)
-    fine_start[(int64_t)gridDim.x << sbits] = (uint32_t)r1;
+    fine_start[(int64_t)gridDim.x << sbits] = r1;
   __syncthreads();
-  for (int64_t rr = r0; rr < r1; rr += kRound) {
-    const int nt = (int)(r1 - rr < kRound ? r1 - rr : (int64_t)kRound);
-    {
-      const int32_t* src[kGroupCols];
+  const int32_t* src[NC];
+  int32_t* dst[NC];
 #pragma unroll
-      for (int q = 0; q < kGroupCols; ++q) src[q] = q < a.ncols ? in + (int64_t)q * a.n + rr : nullptr;
-      load_round(src, a.ncols, nt, S.rows);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nt; i += blockDim.x)
-      S.bin[i] = (uint16_t)(top_bits(S.rows[i], a.bits) & (uint32_t)(nsub - 1));
-    __syncthreads();
-    write_round(S, nt, nsub, a.ncols, out, a.n, s_warp, &s_total);
+  for (int q = 0; q < NC; ++q) {
+    src[q] = in + (int64_t)q * a.n;
+    dst[q] = out + (int64_t)q * a.n;
   }
+  stream_rounds<NC>(S, src, r0, r1, r1, nsub, dst, s_warp, &s_total,
+                    [=](int32_t key, uint32_t) { return top_bits(key, bits) & mask; });
 }
+
+// Launches of the templated passes for a group's column count.
+template <int NC>
+void launch_pass1(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t st,
+                  const uint32_t* p1_start, int32_t* out) {
+  bpart_pass1_kernel<NC><<<grid, kPartThreads, smem, st>>>(pa, p1_start, out);
+}
+template <int NC>
+void launch_pass2(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t st,
+                  const uint32_t* p1_start, const int32_t* in, uint32_t* fstart, int32_t* out) {
+  bpart_pass2_kernel<NC><<<grid, kPartThreads, smem, st>>>(pa, p1_start, in, fstart, out);
+}
+template <int NC>
+cudaError_t set_pass_smem(size_t smem1, size_t smem2) {
+  cudaError_t e = cudaFuncSetAttribute(bpart_pass1_kernel<NC>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(bpart_pass2_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem2);
+}
+
+#define QFG_NC_SWITCH(nc, CALL) \
+  switch (nc) {                 \
+    case 1: CALL(1); break;     \
+    case 2: CALL(2); break;     \
+    case 3: CALL(3); break;     \
+    case 4: CALL(4); break;     \
+    case 5: CALL(5); break;     \
+    case 6: CALL(6); break;     \
+    case 7: CALL(7); break;     \
+    default: CALL(8); break;    \
+  }
+static_assert(kGroupCols == 8, "column-count dispatch covers 1..8");
 
 // ----------------------------------------------------------------------------
 // Persistent evaluation kernel.
@@ -1050,7 +1112,7 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   ps->sbits = bits - ps->cbits;
   const int nfine = 2 << bits;
   ps->np1 = 2 << ps->cbits;
-  ps->pgrid = (unsigned)ctx->num_sms * 2;
+  ps->pgrid = (unsigned)ctx->num_sms;
   size_t part_words = 0;
   int max_ncols = 1;
   for (auto& g : groups) {
@@ -1069,12 +1131,13 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   ps->p1_tot = fstarts + groups.size() * fs_words;
   uint32_t* p1_base = ps->p1_tot + ps->np1 + 1;
   ps->p1_start = p1_base + (size_t)ps->pgrid * ps->np1;
-  ps->p1_smem = round_smem_bytes(max_ncols, ps->np1);
-  ps->p2_smem = round_smem_bytes(max_ncols, 1 << ps->sbits);
-  QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass1_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps->p1_smem));
-  QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass2_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps->p2_smem));
+  for (auto& g : groups) {
+    const int nc = (int)g.cols.size();
+    const size_t s1 = round_smem_bytes(nc, ps->np1), s2 = round_smem_bytes(nc, 1 << ps->sbits);
+#define QFG_SET_SMEM(N) QFG_CUDA(ctx, set_pass_smem<N>(s1, s2))
+    QFG_NC_SWITCH(nc, QFG_SET_SMEM)
+#undef QFG_SET_SMEM
+  }
 
   std::vector<GroupDesc> gdesc(groups.size());
   std::vector<LitDesc> ldesc;
@@ -1221,18 +1284,24 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
     else
       bpart_hist_kernel<false><<<ps.pgrid, kPartThreads, 0, ctx->stream>>>(job.pa);
     QFG_LAUNCHED(ctx);
+    const int nc = job.pa.ncols;
+    const size_t s1 = round_smem_bytes(nc, ps.np1), s2 = round_smem_bytes(nc, 1 << ps.sbits);
     if (ps.two_pass) {
       QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, ps.p1_start, ps.np1, ps.p1_start + ps.np1));
-      bpart_pass1_kernel<<<ps.pgrid, kPartThreads, ps.p1_smem, ctx->stream>>>(job.pa, ps.p1_start,
-                                                                               ps.tmp_cols);
+#define QFG_P1(N) launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, ps.p1_start, ps.tmp_cols)
+      QFG_NC_SWITCH(nc, QFG_P1)
+#undef QFG_P1
       QFG_LAUNCHED(ctx);
-      bpart_pass2_kernel<<<ps.np1, kPartThreads, ps.p2_smem, ctx->stream>>>(
-          job.pa, ps.p1_start, ps.tmp_cols, job.fstart, job.final_out);
+#define QFG_P2(N) \
+  launch_pass2<N>(job.pa, (unsigned)ps.np1, s2, ctx->stream, ps.p1_start, ps.tmp_cols, job.fstart, job.final_out)
+      QFG_NC_SWITCH(nc, QFG_P2)
+#undef QFG_P2
       QFG_LAUNCHED(ctx);
     } else {
       QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, job.fstart, ps.np1, job.fstart + ps.np1));
-      bpart_pass1_kernel<<<ps.pgrid, kPartThreads, ps.p1_smem, ctx->stream>>>(job.pa, job.fstart,
-                                                                               job.final_out);
+#define QFG_P1(N) launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, job.fstart, job.final_out)
+      QFG_NC_SWITCH(nc, QFG_P1)
+#undef QFG_P1
       QFG_LAUNCHED(ctx);
     }
   }
