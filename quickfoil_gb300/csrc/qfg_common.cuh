@@ -77,6 +77,11 @@ class DevBuf {
 
   // Ensures at least `bytes` (grow-only); contents are not preserved.
   int reserve(Ctx* ctx, size_t bytes);
+  // Like reserve, but takes a block from the context's pool of released
+  // binding-set storage when one is large enough, and returns its block to
+  // that pool on release (binding sets uploaded step after step then
+  // allocate nothing).
+  int reserve_pooled(Ctx* ctx, size_t bytes);
   void release();
   template <typename T>
   T* as() const { return static_cast<T*>(ptr_); }
@@ -87,6 +92,7 @@ class DevBuf {
   Ctx* ctx_ = nullptr;
   void* ptr_ = nullptr;
   size_t bytes_ = 0;
+  bool pooled_ = false;
 };
 
 // Relation tuples projected onto an ordered list of argument positions,
@@ -139,6 +145,8 @@ struct Ctx {
   int shard_count = 1;
   int64_t launches = 0;
   std::map<int32_t, std::unique_ptr<Relation>> relations;
+  // Released binding-set storage kept for reuse (still charged to `used`).
+  std::vector<std::pair<void*, size_t>> binding_pool;
   // Grow-only scratch, reused by every call on this context.
   DevBuf scratch[16];
   // Double-buffered pinned staging for small host->device uploads

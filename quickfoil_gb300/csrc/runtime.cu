@@ -33,22 +33,60 @@ DevBuf& DevBuf::operator=(DevBuf&& o) noexcept {
     ctx_ = o.ctx_;
     ptr_ = o.ptr_;
     bytes_ = o.bytes_;
+    pooled_ = o.pooled_;
     o.ctx_ = nullptr;
     o.ptr_ = nullptr;
     o.bytes_ = 0;
+    o.pooled_ = false;
   }
   return *this;
+}
+
+constexpr size_t kBindingPoolBlocks = 2;
+
+static void free_binding_pool(Ctx* ctx) {
+  for (auto& blk : ctx->binding_pool) {
+    cudaFree(blk.first);
+    ctx->used -= (int64_t)blk.second;
+  }
+  ctx->binding_pool.clear();
 }
 
 void DevBuf::release() {
   if (ptr_ != nullptr) {
     // Work queued on the context stream may still read this buffer.
     if (ctx_ != nullptr) cudaStreamSynchronize(ctx_->stream);
-    cudaFree(ptr_);
-    if (ctx_ != nullptr) ctx_->used -= (int64_t)bytes_;
+    if (pooled_ && ctx_ != nullptr && ctx_->binding_pool.size() < kBindingPoolBlocks) {
+      ctx_->binding_pool.emplace_back(ptr_, bytes_);
+    } else {
+      cudaFree(ptr_);
+      if (ctx_ != nullptr) ctx_->used -= (int64_t)bytes_;
+    }
   }
   ptr_ = nullptr;
   bytes_ = 0;
+  pooled_ = false;
+}
+
+int DevBuf::reserve_pooled(Ctx* ctx, size_t bytes) {
+  if (bytes <= bytes_ && ptr_ != nullptr) return QFG_OK;
+  int best = -1;
+  for (size_t i = 0; i < ctx->binding_pool.size(); ++i) {
+    const size_t sz = ctx->binding_pool[i].second;
+    if (sz >= bytes && (best < 0 || sz < ctx->binding_pool[best].second)) best = (int)i;
+  }
+  if (best >= 0) {
+    release();
+    ctx_ = ctx;
+    ptr_ = ctx->binding_pool[best].first;
+    bytes_ = ctx->binding_pool[best].second;
+    ctx->binding_pool.erase(ctx->binding_pool.begin() + best);
+    pooled_ = true;
+    return QFG_OK;
+  }
+  QFG_TRY(reserve(ctx, bytes));
+  pooled_ = true;
+  return QFG_OK;
 }
 
 int DevBuf::reserve(Ctx* ctx, size_t bytes) {
@@ -57,6 +95,7 @@ int DevBuf::reserve(Ctx* ctx, size_t bytes) {
   // Round up so repeated growth does not reallocate for small increases.
   size_t want = (bytes + 255) & ~size_t(255);
   if (ptr_ != nullptr) want = std::max(want, bytes_ + bytes_ / 4);
+  if (ctx->used - (int64_t)bytes_ + (int64_t)want > ctx->budget) free_binding_pool(ctx);
   const int64_t after = ctx->used - (int64_t)bytes_ + (int64_t)want;
   if (after > ctx->budget) {
     want = (bytes + 255) & ~size_t(255);
@@ -325,6 +364,7 @@ extern "C" int qfg_ctx_destroy(qfg_ctx* c) {
   cudaStreamSynchronize(ctx->stream);
   ctx->relations.clear();
   for (auto& s : ctx->scratch) s.release();
+  free_binding_pool(ctx);
   for (int i = 0; i < 2; ++i) {
     if (ctx->staging_host[i] != nullptr) cudaFreeHost(ctx->staging_host[i]);
     if (ctx->staging_done[i] != nullptr) cudaEventDestroy(ctx->staging_done[i]);
@@ -514,8 +554,8 @@ extern "C" int qfg_bindings_create(qfg_ctx* c, int32_t num_columns, const int32_
   b->num_negative = num_negative;
   b->borrowed = flags == QFG_DEVICE_BORROW;
   if (!b->borrowed)
-    QFG_TRY(b->storage.reserve(ctx, sizeof(int32_t) * (size_t)num_columns *
-                                        (size_t)std::max<int64_t>(n, 1)));
+    QFG_TRY(b->storage.reserve_pooled(ctx, sizeof(int32_t) * (size_t)num_columns *
+                                               (size_t)std::max<int64_t>(n, 1)));
   QFG_TRY(load_columns(ctx, num_columns, columns, n, 0, n, flags, &b->storage, &b->columns));
   *out = b.release();
   return QFG_OK;
@@ -539,8 +579,8 @@ extern "C" int qfg_bindings_create_split(qfg_ctx* c, int32_t num_columns,
   b->num_columns = num_columns;
   b->num_positive = num_positive;
   b->num_negative = num_negative;
-  QFG_TRY(b->storage.reserve(ctx, sizeof(int32_t) * (size_t)num_columns *
-                                      (size_t)std::max<int64_t>(n, 1)));
+  QFG_TRY(b->storage.reserve_pooled(ctx, sizeof(int32_t) * (size_t)num_columns *
+                                             (size_t)std::max<int64_t>(n, 1)));
   QFG_TRY(load_columns(ctx, num_columns, positive_columns, num_positive, 0, n, flags,
                        &b->storage, &b->columns));
   QFG_TRY(load_columns(ctx, num_columns, negative_columns, num_negative, num_positive, n, flags,
