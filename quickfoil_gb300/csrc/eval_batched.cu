@@ -46,7 +46,6 @@ constexpr int kGroupCols = QFG_MAX_ARITY;  // join column + up to 7 atom columns
 constexpr int kMaxLitsPerLaunch = 512;
 constexpr int kChunk = 2 * kEvalThreads;     // relation entries per work unit: two per thread
 constexpr int kMaxGroupLits = kEvalThreads;  // one thread per literal in the per-item prefix
-constexpr int kRound = 4096;           // rows staged per partition round
 constexpr int kPartThreads = 1024;
 constexpr int kMaxCoarseBits = 7;      // pass 1 fan-out: 2 << 7 = 256 bins
 constexpr int kMaxSubBits = 9;         // pass 2 fan-out: up to 512 sub-bins
@@ -164,7 +163,7 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* s_warp
 // stores, so the scatter runs in two passes of modest fan-out: pass 1 sends
 // rows to (top cbits bits, label) coarse bins, pass 2 splits every coarse
 // bin, inside its own range, into its 2^(bits - cbits) partitions.  Both
-// passes stage rounds of kRound rows in shared memory, counting-sort them by
+// passes stage rounds of rows in shared memory, counting-sort them by
 // destination bin there and write each bin's run with consecutive threads on
 // consecutive addresses.  A histogram pass counts the coarse bins per CTA
 // (one atomicAdd per bin and CTA gives the CTA its cursor); pass 2 counts its
@@ -239,27 +238,37 @@ __global__ void __launch_bounds__(kPartThreads, 1) bpart_hist_kernel(BPartArgs a
 }
 
 // Round processing, templated on the number of carried columns NC so that
-// every per-column loop unrolls without predicated-off lanes.  A round of
-// kRound rows lives in shared memory (NC columns) while the next round's rows
-// are already loading into registers; the round is counting-sorted by bin in
-// shared memory and written so that the threads writing one bin's run write
-// consecutive addresses.
+// every per-column loop unrolls without predicated-off lanes.  Each thread
+// owns four consecutive rows of a round; rounds arrive by cp.async (16-byte
+// copies where the source is aligned) into one of two shared-memory buffers
+// while the previous round is sorted and written.  A round is
+// counting-sorted by bin in shared memory: ranks come from shared atomics on
+// the bin counters and stay in registers, one block scan gives the bins'
+// starts (and advances their output cursors), the permutation records (row,
+// bin) at each sorted position, and the threads then write sorted positions
+// in order, so the threads writing one bin's run write consecutive
+// addresses.
+template <int NC>
+struct PassShape {
+  static constexpr int kThreads = NC <= 6 ? 1024 : 512;
+  static constexpr int kRows = 4 * kThreads;  // rows per round
+};
+
 struct RoundSmem {
-  int32_t* rows;      // NC * kRound
-  uint32_t* br;       // kRound: bin << 16 | rank within the bin
-  uint16_t* perm;     // kRound: sorted position -> row
+  int32_t* rows[2];   // NC * kRows each
+  uint32_t* perm;     // kRows: row | bin << 16 at each sorted position
   uint32_t* lcount;   // nbins
   uint32_t* lstart;   // nbins
   uint32_t* gpos;     // nbins: output position of sorted position 0 of bin b
   uint32_t* cursor;   // nbins: output cursor of each bin
 };
 
-__device__ __forceinline__ RoundSmem carve_round(unsigned char* smem, int ncols, int nbins) {
+__device__ __forceinline__ RoundSmem carve_round(unsigned char* smem, int ncols, int nbins, int rows) {
   RoundSmem S;
-  S.rows = reinterpret_cast<int32_t*>(smem);
-  S.br = reinterpret_cast<uint32_t*>(S.rows + ncols * kRound);
-  S.perm = reinterpret_cast<uint16_t*>(S.br + kRound);
-  S.lcount = reinterpret_cast<uint32_t*>(S.perm + kRound);
+  S.rows[0] = reinterpret_cast<int32_t*>(smem);
+  S.rows[1] = S.rows[0] + ncols * rows;
+  S.perm = reinterpret_cast<uint32_t*>(S.rows[1] + ncols * rows);
+  S.lcount = S.perm + rows;
   S.lstart = S.lcount + nbins;
   S.gpos = S.lstart + nbins;
   S.cursor = S.gpos + nbins;
@@ -267,63 +276,101 @@ __device__ __forceinline__ RoundSmem carve_round(unsigned char* smem, int ncols,
 }
 
 size_t round_smem_bytes(int ncols, int nbins) {
-  return sizeof(int32_t) * (size_t)ncols * kRound + (sizeof(uint32_t) + sizeof(uint16_t)) * kRound +
-         4 * sizeof(uint32_t) * (size_t)nbins;
+  const size_t rows = ncols <= 6 ? 4096 : 2048;
+  return sizeof(int32_t) * (2 * (size_t)ncols * rows + rows + 4 * (size_t)nbins);
 }
 
-constexpr int kRowsPerThread = kRound / kPartThreads;
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Starts the copies of rows [rr, rr + nt) of NC columns into `dst` (column
+// stride R): thread c copies rows 4c .. 4c + 3, with one 16-byte copy per
+// column when the source is 16-byte aligned and the chunk is whole.
 template <int NC>
-__device__ __forceinline__ void load_rows(int32_t (&v)[NC][kRowsPerThread], const int32_t* const (&src)[NC],
-                                          uint32_t rr, int nt) {
+struct ColPtrs {
+  const int32_t* p[NC];
+};
+template <int NC>
+struct OutPtrs {
+  int32_t* p[NC];
+};
+
+template <int NC, int R>
+__device__ __forceinline__ void issue_round(const ColPtrs<NC> src, uint32_t rr, int nt, int32_t* dst,
+                                            bool vec) {
+  const int i0 = 4 * threadIdx.x;
 #pragma unroll
-  for (int k = 0; k < kRowsPerThread; ++k) {
-    const int i = threadIdx.x + k * kPartThreads;
+  for (int q = 0; q < NC; ++q) {
+    int32_t* d = dst + q * R + i0;
+    const int32_t* s = src.p[q] + rr + i0;
+    if (vec && i0 + 4 <= nt) {
+      cp_async16(d, s);
+    } else {
 #pragma unroll
-    for (int q = 0; q < NC; ++q) v[q][k] = i < nt ? __ldg(src[q] + rr + i) : 0;
+      for (int j = 0; j < 4; ++j)
+        if (i0 + j < nt) cp_async4(d + j, s + j);
+    }
   }
+  cp_async_commit();
 }
 
-// Rows [r0, r1): staging and ranking, a block scan of the bin counts (which
-// also advances the output cursors), the permutation and the writes, each
-// separated by a barrier.
-// Rounds never straddle `split` (the first negative row in pass 1), so a
-// round's rows share one label and fan out to half the bins.
-__device__ __forceinline__ uint32_t round_end(uint32_t rr, uint32_t r1, uint32_t split) {
-  const uint32_t e = umin(r1, rr + kRound);
+// End of the round starting at rr: rounds are anchored at r0 and never
+// straddle `split`.
+__device__ __forceinline__ uint32_t round_end(uint32_t r0, uint32_t rr, uint32_t r1, uint32_t split,
+                                              uint32_t R) {
+  const uint32_t e = umin(r0 + ((rr - r0) / R + 1) * R, r1);
   return (rr < split && split < e) ? split : e;
 }
 
+// Rows [r0, r1) in rounds anchored at r0 (which is a multiple of 4); rounds
+// never straddle `split` (the first negative row in pass 1), so a round's
+// rows share one label and fan out to half the bins.  `aligned` says the
+// source columns are 16-byte aligned.
 template <int NC, typename BinFn>
-__device__ __forceinline__ void stream_rounds(const RoundSmem& S, const int32_t* const (&src)[NC],
-                                              uint32_t r0, uint32_t r1, uint32_t split, int nbins,
-                                              int32_t* const (&out)[NC], uint32_t* s_warp,
-                                              uint32_t* s_total, BinFn bin_of) {
+__device__ __forceinline__ void stream_rounds(const RoundSmem& S, const ColPtrs<NC> src, uint32_t r0,
+                                              uint32_t r1, uint32_t split, int nbins,
+                                              const OutPtrs<NC> out, bool aligned,
+                                              uint32_t* s_warp, uint32_t* s_total, BinFn bin_of) {
+  constexpr int T = PassShape<NC>::kThreads;
+  constexpr int R = PassShape<NC>::kRows;
   if (r0 >= r1) return;
-  int32_t v[NC][kRowsPerThread];
-  uint32_t re = round_end(r0, r1, split);
-  load_rows<NC>(v, src, r0, (int)(re - r0));
-  for (uint32_t rr = r0; rr < r1;) {
-    const uint32_t rend = re;
-    const int nt = (int)(rend - rr);
-#pragma unroll
-    for (int k = 0; k < kRowsPerThread; ++k) {
-      const int i = threadIdx.x + k * kPartThreads;
-      if (i < nt) {
-#pragma unroll
-        for (int q = 0; q < NC; ++q) S.rows[q * kRound + i] = v[q][k];
-        const uint32_t bin = bin_of(v[0][k], rr + i);
-        S.br[i] = (bin << 16) | atomicAdd(&S.lcount[bin], 1u);
-      }
+  uint32_t rr = r0, re = round_end(r0, r0, r1, split, R);
+  issue_round<NC, R>(src, rr, (int)(re - rr), S.rows[0], aligned && (rr & 3u) == 0u);
+  int buf = 0;
+  while (rr < r1) {
+    const int nt = (int)(re - rr);
+    cp_async_wait_all();
+    __syncthreads();
+    const uint32_t nrr = re;
+    uint32_t nre = nrr;
+    if (nrr < r1) {
+      nre = round_end(r0, nrr, r1, split, R);
+      issue_round<NC, R>(src, nrr, (int)(nre - nrr), S.rows[buf ^ 1], aligned && (nrr & 3u) == 0u);
+    }
+    const int32_t* rows = S.rows[buf];
+    const int i0 = 4 * threadIdx.x;
+    uint32_t b0, b1, b2, b3, k0 = 0, k1 = 0, k2 = 0, k3 = 0;
+    {
+      const int4 kv = *reinterpret_cast<const int4*>(rows + i0);
+      b0 = bin_of(kv.x, rr + i0);
+      b1 = bin_of(kv.y, rr + i0 + 1);
+      b2 = bin_of(kv.z, rr + i0 + 2);
+      b3 = bin_of(kv.w, rr + i0 + 3);
+      if (i0 < nt) k0 = atomicAdd(&S.lcount[b0], 1u);
+      if (i0 + 1 < nt) k1 = atomicAdd(&S.lcount[b1], 1u);
+      if (i0 + 2 < nt) k2 = atomicAdd(&S.lcount[b2], 1u);
+      if (i0 + 3 < nt) k3 = atomicAdd(&S.lcount[b3], 1u);
     }
     __syncthreads();
-    if (rend < r1) {
-      re = round_end(rend, r1, split);
-      load_rows<NC>(v, src, rend, (int)(re - rend));
-    }
     {
-      // Exclusive scan of the bin counts, one bin per thread (nbins <=
-      // blockDim.x); each bin's output cursor advances by its count.
       const uint32_t c = (int)threadIdx.x < nbins ? S.lcount[threadIdx.x] : 0u;
       const uint32_t ex = block_scan_excl(c, s_warp, s_total);
       if ((int)threadIdx.x < nbins) {
@@ -334,39 +381,39 @@ __device__ __forceinline__ void stream_rounds(const RoundSmem& S, const int32_t*
       }
     }
     __syncthreads();
-#pragma unroll
-    for (int k = 0; k < kRowsPerThread; ++k) {
-      const int i = threadIdx.x + k * kPartThreads;
-      if (i < nt) {
-        const uint32_t w = S.br[i];
-        S.perm[S.lstart[w >> 16] + (w & 0xffffu)] = (uint16_t)i;
-      }
-    }
+    if (i0 < nt) S.perm[S.lstart[b0] + k0] = (uint32_t)i0 | (b0 << 16);
+    if (i0 + 1 < nt) S.perm[S.lstart[b1] + k1] = (uint32_t)(i0 + 1) | (b1 << 16);
+    if (i0 + 2 < nt) S.perm[S.lstart[b2] + k2] = (uint32_t)(i0 + 2) | (b2 << 16);
+    if (i0 + 3 < nt) S.perm[S.lstart[b3] + k3] = (uint32_t)(i0 + 3) | (b3 << 16);
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < kRowsPerThread; ++k) {
-      const int kk = threadIdx.x + k * kPartThreads;
+    for (int k = 0; k < 4; ++k) {
+      const int kk = threadIdx.x + k * T;
       if (kk < nt) {
-        const int i = S.perm[kk];
-        const uint32_t g = S.gpos[S.br[i] >> 16] + (uint32_t)kk;
+        const uint32_t w = S.perm[kk];
+        const int i = (int)(w & 0xffffu);
+        const uint32_t g = S.gpos[w >> 16] + (uint32_t)kk;
 #pragma unroll
-        for (int q = 0; q < NC; ++q) out[q][g] = S.rows[q * kRound + i];
+        for (int q = 0; q < NC; ++q) out.p[q][g] = rows[q * R + i];
       }
     }
-    __syncthreads();
-    rr = rend;
+    rr = nrr;
+    re = nre;
+    buf ^= 1;
   }
 }
 
-// Pass 1: the CTA's chunk of the original columns into pass-1 bins.
+// Pass 1: the CTA's chunk of the original columns into pass-1 bins at
+// p1_start[bin] + this CTA's base (out: column stride out_stride).
 template <int NC>
-__global__ void __launch_bounds__(kPartThreads, 1)
-bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* __restrict__ out) {
+__global__ void __launch_bounds__(PassShape<NC>::kThreads, 1)
+bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* __restrict__ out,
+                   int64_t out_stride, int aligned) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   const int np1 = 2 << a.cbits;
-  const RoundSmem S = carve_round(smem, NC, np1);
+  const RoundSmem S = carve_round(smem, NC, np1, PassShape<NC>::kRows);
   for (int i = threadIdx.x; i < np1; i += blockDim.x) {
     S.cursor[i] = p1_start[i] + a.p1_base[(int64_t)blockIdx.x * np1 + i];
     S.lcount[i] = 0u;
@@ -374,36 +421,60 @@ bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* 
   __syncthreads();
   int64_t r0, r1;
   cta_range4(a.n, &r0, &r1);
-  const int32_t* src[NC];
-  int32_t* dst[NC];
+  ColPtrs<NC> src;
+  OutPtrs<NC> dst;
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
-    src[q] = a.cols[q];
-    dst[q] = out + (int64_t)q * a.n;
+    src.p[q] = a.cols[q];
+    dst.p[q] = out + (int64_t)q * out_stride;
   }
   const int cbits = a.cbits;
   const uint32_t npos = (uint32_t)a.npos;
-  stream_rounds<NC>(S, src, (uint32_t)r0, (uint32_t)r1, npos, np1, dst, s_warp, &s_total,
-                    [=](int32_t key, uint32_t r) {
+  stream_rounds<NC>(S, src, (uint32_t)r0, (uint32_t)r1, npos, np1, dst, aligned != 0, s_warp,
+                    &s_total, [=](int32_t key, uint32_t r) {
                       return (top_bits(key, cbits) << 1) | (r >= npos ? 1u : 0u);
                     });
 }
 
-// Pass 2: CTA b splits pass-1 bin b = (hash prefix c, label) inside its own
-// range into sub-bins 0 .. 2^sbits - 1 and records where each starts:
-// fine_start[(b << sbits) + sub] (the last CTA also writes the end, n).
+// Bin starts of pass 1, twice: padded to multiples of 4 rows (where pass 1
+// writes and pass 2 reads, so that pass 2's copies are 16-byte aligned) and
+// unpadded (where pass 2 writes).  One block, nbins <= blockDim.x.
+__global__ void pad_scan_kernel(const uint32_t* __restrict__ tot, int nbins, uint32_t* __restrict__ pad,
+                                uint32_t* __restrict__ unp) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
+  const uint32_t c = (int)threadIdx.x < nbins ? tot[threadIdx.x] : 0u;
+  const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
+  const uint32_t total = s_total;
+  const uint32_t exp = block_scan_excl((c + 3u) & ~3u, s_warp, &s_total);
+  if ((int)threadIdx.x < nbins) {
+    unp[threadIdx.x] = ex;
+    pad[threadIdx.x] = exp;
+  }
+  if (threadIdx.x == 0) {
+    unp[nbins] = total;
+    pad[nbins] = s_total;
+  }
+}
+
+// Pass 2: CTA b splits pass-1 bin b = (hash prefix c, label), read from its
+// padded range, into sub-bins 0 .. 2^sbits - 1 written from its unpadded
+// start, and records where each starts: fine_start[(b << sbits) + sub] (the
+// last CTA also writes the end, n).
 template <int NC>
-__global__ void __launch_bounds__(kPartThreads, 1)
-bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, const int32_t* __restrict__ in,
-                   uint32_t* __restrict__ fine_start, int32_t* __restrict__ out) {
+__global__ void __launch_bounds__(PassShape<NC>::kThreads, 1)
+bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ p1_pad, const uint32_t* __restrict__ p1_unp,
+                   const int32_t* __restrict__ in, int64_t in_stride, uint32_t* __restrict__ fine_start,
+                   int32_t* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   const int sbits = a.bits - a.cbits;
   const int nsub = 1 << sbits;
-  const RoundSmem S = carve_round(smem, NC, nsub);
+  const RoundSmem S = carve_round(smem, NC, nsub, PassShape<NC>::kRows);
   const int b = blockIdx.x;
-  const uint32_t r0 = p1_start[b], r1 = p1_start[b + 1];
+  const uint32_t r0 = p1_pad[b], cnt = p1_unp[b + 1] - p1_unp[b], r1 = r0 + cnt;
+  const uint32_t o0 = p1_unp[b];
   for (int i = threadIdx.x; i < nsub; i += blockDim.x) S.lcount[i] = 0u;
   __syncthreads();
   const uint32_t mask = (uint32_t)(nsub - 1);
@@ -424,34 +495,37 @@ bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, const int
   const uint32_t c = (int)threadIdx.x < nsub ? S.lcount[threadIdx.x] : 0u;
   const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
   if ((int)threadIdx.x < nsub) {
-    S.cursor[threadIdx.x] = r0 + ex;
-    fine_start[((int64_t)b << sbits) + threadIdx.x] = r0 + ex;
+    S.cursor[threadIdx.x] = o0 + ex;
+    fine_start[((int64_t)b << sbits) + threadIdx.x] = o0 + ex;
     S.lcount[threadIdx.x] = 0u;
   }
   if (b == (int)gridDim.x - 1 && threadIdx.x == 0)
-    fine_start[(int64_t)gridDim.x << sbits] = r1;
+    fine_start[(int64_t)gridDim.x << sbits] = p1_unp[gridDim.x];
   __syncthreads();
-  const int32_t* src[NC];
-  int32_t* dst[NC];
+  ColPtrs<NC> src;
+  OutPtrs<NC> dst;
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
-    src[q] = in + (int64_t)q * a.n;
-    dst[q] = out + (int64_t)q * a.n;
+    src.p[q] = in + (int64_t)q * in_stride;
+    dst.p[q] = out + (int64_t)q * a.n;
   }
-  stream_rounds<NC>(S, src, r0, r1, r1, nsub, dst, s_warp, &s_total,
+  stream_rounds<NC>(S, src, r0, r1, r1, nsub, dst, true, s_warp, &s_total,
                     [=](int32_t key, uint32_t) { return top_bits(key, bits) & mask; });
 }
 
 // Launches of the templated passes for a group's column count.
 template <int NC>
 void launch_pass1(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t st,
-                  const uint32_t* p1_start, int32_t* out) {
-  bpart_pass1_kernel<NC><<<grid, kPartThreads, smem, st>>>(pa, p1_start, out);
+                  const uint32_t* p1_start, int32_t* out, int64_t out_stride, bool aligned) {
+  bpart_pass1_kernel<NC><<<grid, PassShape<NC>::kThreads, smem, st>>>(pa, p1_start, out, out_stride,
+                                                                      aligned ? 1 : 0);
 }
 template <int NC>
 void launch_pass2(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t st,
-                  const uint32_t* p1_start, const int32_t* in, uint32_t* fstart, int32_t* out) {
-  bpart_pass2_kernel<NC><<<grid, kPartThreads, smem, st>>>(pa, p1_start, in, fstart, out);
+                  const uint32_t* p1_pad, const uint32_t* p1_unp, const int32_t* in, int64_t in_stride,
+                  uint32_t* fstart, int32_t* out) {
+  bpart_pass2_kernel<NC><<<grid, PassShape<NC>::kThreads, smem, st>>>(pa, p1_pad, p1_unp, in, in_stride,
+                                                                      fstart, out);
 }
 template <int NC>
 cudaError_t set_pass_smem(size_t smem1, size_t smem2) {
@@ -549,13 +623,6 @@ size_t eval_smem_bytes(int num_lits, int max_cols) {
          sizeof(int32_t) * (size_t)max_cols * kTile + sizeof(uint32_t) * kSlots +
          sizeof(uint32_t) * 2 * (kMaxGroupLits + 1) + sizeof(uint16_t) * 2 * kTile;
 }
-
-__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
-  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem_dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
   const int lane = lane_id();
@@ -1074,8 +1141,10 @@ struct PreparedStep {
   unsigned pgrid = 0;
   size_t p1_smem = 0, p2_smem = 0;
   uint32_t* p1_tot = nullptr;
-  uint32_t* p1_start = nullptr;
+  uint32_t* p1_start = nullptr;   // padded bin starts (two passes)
+  uint32_t* p1_unp = nullptr;     // unpadded bin starts (two passes)
   int32_t* tmp_cols = nullptr;
+  int64_t tmp_stride = 0;
   std::vector<PartJob> parts;
   std::vector<LaunchJob> launches;
   std::vector<unsigned char> blob;  // descriptors, to be copied to blob_dev
@@ -1119,18 +1188,23 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     part_words += g.cols.size() * (size_t)nb;
     max_ncols = std::max(max_ncols, (int)g.cols.size());
   }
-  const size_t tmp_words = ps->two_pass ? (size_t)max_ncols * (size_t)nb : 0;
+  // Pass-1 output: bins padded to multiples of 4 rows, 16-byte aligned columns.
+  ps->tmp_stride = ps->two_pass ? (((int64_t)nb + 3) & ~int64_t(3)) + 4 * (int64_t)ps->np1 : 0;
+  const size_t tmp_off = (part_words + 63) & ~size_t(63);
+  const size_t tmp_words = ps->two_pass ? (size_t)max_ncols * (size_t)ps->tmp_stride : 0;
   const size_t fs_words = (size_t)nfine + 1;
-  const size_t bins_words = (size_t)ps->np1 + 1 + (size_t)ps->pgrid * ps->np1 + (size_t)ps->np1 + 1;
-  QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * (part_words + tmp_words)));
+  const size_t bins_words =
+      (size_t)ps->np1 + 1 + (size_t)ps->pgrid * ps->np1 + 2 * ((size_t)ps->np1 + 1);
+  QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * (tmp_off + tmp_words)));
   QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(
       ctx, sizeof(uint32_t) * (groups.size() * fs_words + bins_words)));
   int32_t* part_base = ctx->scratch[kScrBindPart].as<int32_t>();
-  ps->tmp_cols = part_base + part_words;
+  ps->tmp_cols = part_base + tmp_off;
   uint32_t* fstarts = ctx->scratch[kScrBindOffsets].as<uint32_t>();
   ps->p1_tot = fstarts + groups.size() * fs_words;
   uint32_t* p1_base = ps->p1_tot + ps->np1 + 1;
   ps->p1_start = p1_base + (size_t)ps->pgrid * ps->np1;
+  ps->p1_unp = ps->p1_start + ps->np1 + 1;
   for (auto& g : groups) {
     const int nc = (int)g.cols.size();
     const size_t s1 = round_smem_bytes(nc, ps->np1), s2 = round_smem_bytes(nc, 1 << ps->sbits);
@@ -1287,19 +1361,23 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
     const int nc = job.pa.ncols;
     const size_t s1 = round_smem_bytes(nc, ps.np1), s2 = round_smem_bytes(nc, 1 << ps.sbits);
     if (ps.two_pass) {
-      QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, ps.p1_start, ps.np1, ps.p1_start + ps.np1));
-#define QFG_P1(N) launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, ps.p1_start, ps.tmp_cols)
+      pad_scan_kernel<<<1, 512, 0, ctx->stream>>>(ps.p1_tot, ps.np1, ps.p1_start, ps.p1_unp);
+      QFG_LAUNCHED(ctx);
+#define QFG_P1(N) \
+  launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, ps.p1_start, ps.tmp_cols, ps.tmp_stride, job.vec)
       QFG_NC_SWITCH(nc, QFG_P1)
 #undef QFG_P1
       QFG_LAUNCHED(ctx);
-#define QFG_P2(N) \
-  launch_pass2<N>(job.pa, (unsigned)ps.np1, s2, ctx->stream, ps.p1_start, ps.tmp_cols, job.fstart, job.final_out)
+#define QFG_P2(N)                                                                                  \
+  launch_pass2<N>(job.pa, (unsigned)ps.np1, s2, ctx->stream, ps.p1_start, ps.p1_unp, ps.tmp_cols, \
+                  ps.tmp_stride, job.fstart, job.final_out)
       QFG_NC_SWITCH(nc, QFG_P2)
 #undef QFG_P2
       QFG_LAUNCHED(ctx);
     } else {
       QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, job.fstart, ps.np1, job.fstart + ps.np1));
-#define QFG_P1(N) launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, job.fstart, job.final_out)
+#define QFG_P1(N) \
+  launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, job.fstart, job.final_out, job.pa.n, job.vec)
       QFG_NC_SWITCH(nc, QFG_P1)
 #undef QFG_P1
       QFG_LAUNCHED(ctx);
@@ -1345,7 +1423,7 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
     words += (int64_t)g.cols.size() * nb + (2 << bits) + 1;
     max_ncols = std::max(max_ncols, (int)g.cols.size());
   }
-  if (two_pass) words += (int64_t)max_ncols * nb;
+  if (two_pass) words += (int64_t)max_ncols * (nb + 4 + 4 * np1) + 64;
   words += (int64_t)np1 * (ctx->num_sms * 2 + 3);
   int64_t units = (int64_t)plan.groups.size() << bits;
   for (KeyTable* kt : plan.tables) units += kt->num_entries / kChunk + 1;
