@@ -553,29 +553,29 @@ static_assert(kGroupCols == 8, "column-count dispatch covers 1..8");
 // Persistent evaluation kernel.
 //
 // Work unit = a range of at most kChunk relation entries of one (group,
-// partition) item.  A planning kernel lists the units of a launch: it reads
-// each item's segment bounds and the number of relation entries its literals
-// hold in the partition's key range, drops items without rows or entries,
-// and splits items with more than kChunk entries (hot join keys of skewed
-// relations) into several units so that no single CTA is left with a long
-// tail.  The evaluation CTA then repeatedly
-//   1. takes a unit (its record was prefetched while the previous unit ran),
-//   2. starts asynchronous copies (cp.async) of the partition's binding rows
-//      -- join column and the carried atom columns -- into shared memory,
-//   3. meanwhile forms the literal-major entry space of the item (one
-//      offsets pair per literal, block scan) and loads the key tuples and
-//      multiplicities of its own two entries into registers,
-//   4. builds the tile's distinct-key table: one 64-bit word per slot,
-//      (key << 32 | positive count | negative count << 16), claimed by a
-//      single atomicCAS, so a slot with a zero count is empty,
-//   5. for groups with atom literals, groups the tile's rows by key --
-//      positives first -- with a scan of the slot counts and permutes the atom
-//      columns into that order, so that the rows of a key are one contiguous
-//      range per label,
-//   6. probes the table with its entries and, for atom literals, compares the
-//      key's rows with the entry's further keys,
-//   7. combines per-literal sums with a segmented warp scan into per-CTA
-//      accumulators, flushed to global memory when the CTA retires.
+// partition) item.  Three launches per literal batch:
+//   plan_units   lists the units: each item's segment bounds and the number
+//                of relation entries its literals hold in the item's key
+//                range; items without rows or entries are dropped, items
+//                with more than kChunk entries (hot join keys of skewed
+//                relations) are split so no CTA is left with a long tail,
+//                and every unit gets a block of entry records;
+//   gather       one warp per unit forms the item's literal-major entry
+//                space and writes the unit's entry records (join key, up to
+//                two further keys, multiplicity, literal and check columns)
+//                into its block, so the evaluation loads them with one
+//                coalesced round trip;
+//   eval         per unit (its record prefetched while the previous unit
+//                ran): the partition's binding rows arrive by cp.async while
+//                each thread loads its two entry records; a key table of the
+//                tile is built with one 32-bit atomicCAS per new key, whose
+//                count atomics also give every row its rank within its key
+//                and label; for groups with atom literals a scan of the slot
+//                counts turns those ranks into per-key row lists (positives
+//                first); the entries probe the table and check the key's rows
+//                against their further keys; per-literal sums are combined
+//                with a segmented warp scan into per-CTA int64 accumulators,
+//                flushed to global memory when the CTA retires.
 
 struct GroupDesc {
   const int32_t* cols;      // ncols SoA columns of n rows, partitioned
@@ -601,7 +601,23 @@ struct LitDesc {
 struct WorkUnit {
   uint32_t group, p;
   uint32_t ps, Pp, ns, Np;   // positive / negative segment of the partition
-  uint32_t f0, f1;           // entry range in the item's literal-major space
+  uint32_t f0, ecnt;         // entries [f0, f0 + ecnt) of the item's literal-major space
+  uint32_t eoff;             // first record of the unit's entry block (multiple of 4)
+  uint32_t pad[3];
+};
+
+// Entry records, SoA over the launch's entry blocks.  meta packs the
+// literal within its group (bits 0-7), the number of columns to check
+// (bits 8-9; 3 = more than two, read the keys from the key table), "keys
+// compared with the join column itself all equal the join key" (bit 10),
+// and the group columns of the first two checks (bits 12-14, 16-18).  For
+// an entry with more than two checks kA holds its key-table index.
+struct EntryRecs {
+  int32_t* k0;
+  int32_t* kA;
+  int32_t* kB;
+  uint32_t* meta;
+  int32_t* mult;
 };
 
 struct EvalArgs {
@@ -612,16 +628,18 @@ struct EvalArgs {
   int max_cols;
   int64_t total_items;
   WorkUnit* units;
-  uint32_t* unit_count;
+  uint32_t* unit_count;      // [units, entry records]
   uint32_t unit_cap;
+  uint32_t entry_cap;
+  EntryRecs rec;
   unsigned int* work_counter;
   unsigned long long* counts;
 };
 
 size_t eval_smem_bytes(int num_lits, int max_cols) {
-  return sizeof(unsigned long long) * (4 * (size_t)num_lits + kSlots) +
-         sizeof(int32_t) * (size_t)max_cols * kTile + sizeof(uint32_t) * kSlots +
-         sizeof(uint32_t) * 2 * (kMaxGroupLits + 1) + sizeof(uint16_t) * 2 * kTile;
+  return sizeof(unsigned long long) * 4 * (size_t)num_lits +
+         sizeof(int32_t) * (size_t)max_cols * kTile + sizeof(uint32_t) * 3 * kSlots +
+         sizeof(uint16_t) * 3 * kTile;
 }
 
 __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
@@ -629,7 +647,7 @@ __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < a.total_items;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t item = base + threadIdx.x;
-    uint32_t nch = 0, E = 0;
+    uint32_t nch = 0, E = 0, espace = 0;
     WorkUnit u{};
     if (item < a.total_items) {
       int lo = 0, hi = a.num_groups - 1;  // largest g with item_begin <= item
@@ -656,25 +674,119 @@ __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
           E += __ldg(off + q1) - __ldg(off + q0);
         }
         nch = (E + kChunk - 1) / kChunk;
+        if (nch > 0) espace = (nch - 1) * kChunk + ((E - (nch - 1) * kChunk + 3u) & ~3u);
       }
     }
-    uint32_t x = nch;
+    // Warp-aggregated reservation of unit slots and entry records.
+    uint32_t x = nch, y = espace;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(kFullMask, x, o);
-      if (lane >= o) x += y;
+      const uint32_t xu = __shfl_up_sync(kFullMask, x, o), yu = __shfl_up_sync(kFullMask, y, o);
+      if (lane >= o) {
+        x += xu;
+        y += yu;
+      }
     }
-    const uint32_t warp_total = __shfl_sync(kFullMask, x, 31);
-    uint32_t wbase = 0;
-    if (lane == 31 && warp_total > 0) wbase = atomicAdd(a.unit_count, warp_total);
-    wbase = __shfl_sync(kFullMask, wbase, 31);
-    const uint32_t pos = wbase + x - nch;
+    const uint32_t tu = __shfl_sync(kFullMask, x, 31), te = __shfl_sync(kFullMask, y, 31);
+    uint32_t ub = 0, eb = 0;
+    if (lane == 31 && tu > 0) {
+      ub = atomicAdd(&a.unit_count[0], tu);
+      eb = atomicAdd(&a.unit_count[1], te);
+    }
+    ub = __shfl_sync(kFullMask, ub, 31) + x - nch;
+    eb = __shfl_sync(kFullMask, eb, 31) + y - espace;
     for (uint32_t k = 0; k < nch; ++k) {
-      if (pos + k >= a.unit_cap) break;
+      if (ub + k >= a.unit_cap) break;  // never read: the evaluation stops at unit_cap
       u.f0 = k * kChunk;
-      u.f1 = umin(E, (k + 1) * kChunk);
-      a.units[pos + k] = u;
+      u.ecnt = umin(E - k * kChunk, (uint32_t)kChunk);
+      u.eoff = eb + k * kChunk;
+      if ((uint64_t)u.eoff + ((u.ecnt + 3u) & ~3u) > a.entry_cap) {
+        // Out of entry records (the capacity is an upper bound, so this does
+        // not happen): an empty unit keeps the list well formed.
+        u.ecnt = 0;
+        u.Pp = u.Np = 0;
+      }
+      a.units[ub + k] = u;
     }
+  }
+}
+
+constexpr int kGatherWarps = 8;
+
+// One warp per unit: the item's literal-major entry space (offsets pair per
+// literal, warp scan), then the unit's entry records.
+__global__ void __launch_bounds__(32 * kGatherWarps) gather_entries_kernel(EvalArgs a) {
+  __shared__ uint32_t s_lstart[kGatherWarps][kMaxGroupLits + 1];
+  __shared__ uint32_t s_le0[kGatherWarps][kMaxGroupLits];
+  const int lane = lane_id(), w = warp_id();
+  uint32_t* lstart = s_lstart[w];
+  uint32_t* le0 = s_le0[w];
+  const uint32_t nunits = umin(a.unit_count[0], a.unit_cap);
+  for (uint32_t ui = blockIdx.x * kGatherWarps + w; ui < nunits; ui += gridDim.x * kGatherWarps) {
+    const WorkUnit U = a.units[ui];
+    if (U.eoff + U.ecnt > a.entry_cap) continue;
+    const GroupDesc& G = a.groups[U.group];
+    const int m = G.lit_end - G.lit_begin;
+    const int rshift = kRelPartitionBits - G.bits;
+    const uint32_t q0 = U.p << rshift, q1 = (U.p + 1) << rshift;
+    uint32_t run = 0;
+    for (int L0 = 0; L0 < m; L0 += 32) {
+      const int L = L0 + lane;
+      uint32_t c = 0;
+      if (L < m) {
+        const uint32_t* off = a.lits[G.lit_begin + L].offsets;
+        const uint32_t e0 = __ldg(off + q0);
+        c = __ldg(off + q1) - e0;
+        le0[L] = e0;
+      }
+      uint32_t x = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFullMask, x, o);
+        if (lane >= o) x += y;
+      }
+      if (L < m) lstart[L] = run + x - c;
+      run += __shfl_sync(kFullMask, x, 31);
+    }
+    if (lane == 0) lstart[m] = run;
+    __syncwarp();
+    for (uint32_t j = lane; j < U.ecnt; j += 32) {
+      const uint32_t f = U.f0 + j;
+      int lo = 0, hi = m - 1;  // largest L with lstart[L] <= f
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (lstart[mid] <= f) lo = mid; else hi = mid - 1;
+      }
+      const LitDesc& d = a.lits[G.lit_begin + lo];
+      const uint32_t e = le0[lo] + (f - lstart[lo]);
+      const int32_t* kp = d.keys;
+      const int nk = d.nk;
+      const int32_t k0 = __ldg(kp + e);
+      int32_t kA = 0, kB = 0;
+      uint32_t nchk = 0, colA = 0, colB = 0, ok0 = 1;
+      for (int q = 1; q < nk; ++q) {
+        const int ac = d.atom_col[q];
+        const int32_t kq = __ldg(kp + q * d.stride + e);
+        if (ac == 0) {
+          ok0 &= kq == k0 ? 1u : 0u;
+        } else {
+          if (nchk == 0) { kA = kq; colA = (uint32_t)ac; }
+          else if (nchk == 1) { kB = kq; colB = (uint32_t)ac; }
+          ++nchk;
+        }
+      }
+      if (nchk > 2) {
+        nchk = 3;
+        kA = (int32_t)e;
+      }
+      const uint32_t r = U.eoff + j;
+      a.rec.k0[r] = k0;
+      a.rec.kA[r] = kA;
+      a.rec.kB[r] = kB;
+      a.rec.mult[r] = __ldg(d.mult + e);
+      a.rec.meta[r] = (uint32_t)lo | (nchk << 8) | (ok0 << 10) | (colA << 12) | (colB << 16);
+    }
+    __syncwarp();
   }
 }
 
@@ -698,36 +810,28 @@ __device__ __forceinline__ void flush_acc(unsigned long long* dst, long long cp,
   if (bn) atomicAdd(dst + 3, as_ull(bn));
 }
 
-// One relation entry held in registers.
-struct Entry {
-  int L;                 // literal within the group, -1 = none
-  int nk;
-  int32_t k0, kA, kB;    // join key, keys of the first two checked columns
-  int cA, cB, nchk;      // checked columns (smem column offsets), their count
-  bool ok0;              // keys compared with the join column itself match k0
-  uint32_t e;
-  long long mult;
-};
-
 __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem);
-  unsigned long long* tbl = acc + 4 * a.num_lits;                     // kSlots
-  int32_t* raw = reinterpret_cast<int32_t*>(tbl + kSlots);            // max_cols * kTile
-  uint32_t* cur = reinterpret_cast<uint32_t*>(raw + a.max_cols * kTile);  // kSlots
-  uint32_t* lstart = cur + kSlots;                                    // kMaxGroupLits + 1
-  uint32_t* le0 = lstart + kMaxGroupLits + 1;                         // kMaxGroupLits + 1
-  uint16_t* rslot = reinterpret_cast<uint16_t*>(le0 + kMaxGroupLits + 1);  // kTile
-  uint16_t* rpos = rslot + kTile;                                     // kTile
+  int32_t* raw = reinterpret_cast<int32_t*>(acc + 4 * a.num_lits);   // max_cols * kTile
+  uint32_t* owner = reinterpret_cast<uint32_t*>(raw + a.max_cols * kTile);  // kSlots
+  uint32_t* cnt = owner + kSlots;                                     // kSlots
+  uint32_t* sstart = cnt + kSlots;                                    // kSlots
+  uint16_t* rslot = reinterpret_cast<uint16_t*>(sstart + kSlots);     // kTile
+  uint16_t* rrank = rslot + kTile;                                    // kTile
+  uint16_t* rows = rrank + kTile;                                     // kTile
   __shared__ WorkUnit s_unit;
   __shared__ uint32_t s_idx, s_count;
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
 
   for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) acc[i] = 0ull;
-  for (int i = threadIdx.x; i < kSlots; i += blockDim.x) tbl[i] = 0ull;
+  for (int i = threadIdx.x; i < kSlots; i += blockDim.x) {
+    owner[i] = 0u;
+    cnt[i] = 0u;
+  }
   if (threadIdx.x == 0) {
-    s_count = umin(*a.unit_count, a.unit_cap);
+    s_count = umin(a.unit_count[0], a.unit_cap);
     s_idx = atomicAdd(a.work_counter, 1u);
     if (s_idx < s_count) s_unit = a.units[s_idx];
   }
@@ -749,11 +853,24 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     const int64_t gn = G.n;
     const int ncols = G.ncols;
     const int lit_begin = G.lit_begin;
-    const int m = G.lit_end - lit_begin;
     const bool has_atoms = G.has_atoms != 0;
     const uint32_t total = U.Pp + U.Np;
 
-    Entry ent[2];
+    // This thread's two entry records (a pair of consecutive records).
+    const uint32_t j0 = 2u * threadIdx.x;
+    const bool have = j0 < U.ecnt && U.eoff + U.ecnt <= a.entry_cap;
+    int2 e_k0 = make_int2(0, 0), e_kA = e_k0, e_kB = e_k0, e_mult = e_k0;
+    uint2 e_meta = make_uint2(0u, 0u);
+    if (have) {
+      const uint32_t r = U.eoff + j0;  // even, and the block is padded to a multiple of 4
+      e_k0 = __ldg(reinterpret_cast<const int2*>(a.rec.k0 + r));
+      e_kA = __ldg(reinterpret_cast<const int2*>(a.rec.kA + r));
+      e_kB = __ldg(reinterpret_cast<const int2*>(a.rec.kB + r));
+      e_mult = __ldg(reinterpret_cast<const int2*>(a.rec.mult + r));
+      e_meta = __ldg(reinterpret_cast<const uint2*>(a.rec.meta + r));
+    }
+    const bool have1 = have && j0 + 1 < U.ecnt;
+
     long long bp = 0, bn = 0, cp = 0, cn = 0;
     int Lrun = -1;
     for (uint32_t t0 = 0; t0 < total; t0 += kTile) {
@@ -768,189 +885,137 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         }
       }
       cp_async_commit();
-      if (t0 == 0) {
-        // Literal-major entry space of the item, then this thread's entries.
-        const int rshift = kRelPartitionBits - G.bits;
-        const uint32_t q0 = U.p << rshift, q1 = (U.p + 1) << rshift;
-        uint32_t c = 0;
-        if ((int)threadIdx.x < m) {
-          const uint32_t* off = a.lits[lit_begin + threadIdx.x].offsets;
-          const uint32_t e0 = __ldg(off + q0), e1 = __ldg(off + q1);
-          le0[threadIdx.x] = e0;
-          c = e1 - e0;
-        }
-        const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
-        if ((int)threadIdx.x < m) lstart[threadIdx.x] = ex;
-        if (threadIdx.x == 0) lstart[m] = s_total;
-        __syncthreads();
-        const uint32_t fbase = U.f0 + 2u * threadIdx.x;
-        int L = -1;
-        if (fbase < U.f1) {
-          int lo = 0, hi = m - 1;  // largest L with lstart[L] <= fbase
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (lstart[mid] <= fbase) lo = mid; else hi = mid - 1;
-          }
-          L = lo;
-        }
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-          const uint32_t f = fbase + j;
-          Entry& x = ent[j];
-          x.L = -1;
-          if (L < 0 || f >= U.f1) continue;
-          while (f >= lstart[L + 1]) ++L;
-          const LitDesc& d = a.lits[lit_begin + L];
-          const int32_t* __restrict__ kp = d.keys;
-          x.L = L;
-          x.nk = d.nk;
-          x.e = le0[L] + (f - lstart[L]);
-          x.k0 = __ldg(kp + x.e);
-          x.mult = __ldg(d.mult + x.e);
-          x.ok0 = true;
-          x.nchk = 0;
-          x.kA = x.kB = 0;
-          x.cA = x.cB = 0;
-          for (int q = 1; q < x.nk; ++q) {
-            const int ac = d.atom_col[q];
-            const int32_t kq = __ldg(kp + q * d.stride + x.e);
-            if (ac == 0) {
-              x.ok0 = x.ok0 && kq == x.k0;
-            } else {
-              if (x.nchk == 0) { x.kA = kq; x.cA = ac * kTile; }
-              else if (x.nchk == 1) { x.kB = kq; x.cB = ac * kTile; }
-              ++x.nchk;
-            }
-          }
-        }
-      }
       cp_async_wait_all();
       __syncthreads();
-      // Distinct join keys of the tile.
+      // Distinct join keys of the tile: owner = first row + 1, claimed by
+      // CAS; the count atomics return each row's rank within its key and
+      // label (positive count low half, negative count high half).
       for (int i = threadIdx.x; i < nt; i += blockDim.x) {
         const int32_t key = raw[i];
-        const uint32_t inc = i < npos ? 1u : 0x10000u;
-        const unsigned long long mine = ((unsigned long long)(uint32_t)key << 32) | inc;
+        const bool posr = i < npos;
         uint32_t slot = mix32((uint32_t)key) & (kSlots - 1);
         for (int probe = 0; probe < kSlots; ++probe) {
-          unsigned long long w = *reinterpret_cast<volatile unsigned long long*>(&tbl[slot]);
-          if (w == 0ull) {
-            w = atomicCAS(&tbl[slot], 0ull, mine);
-            if (w == 0ull) break;
-          }
-          if ((uint32_t)(w >> 32) == (uint32_t)key) {
-            atomicAdd(&tbl[slot], (unsigned long long)inc);
-            break;
-          }
+          const uint32_t o = atomicCAS(&owner[slot], 0u, (uint32_t)i + 1u);
+          if (o == 0u || raw[o - 1u] == key) break;
           slot = (slot + 1) & (kSlots - 1);
         }
+        const uint32_t old = atomicAdd(&cnt[slot], posr ? 1u : 0x10000u);
         rslot[i] = (uint16_t)slot;
+        rrank[i] = (uint16_t)(posr ? (old & 0xffffu) : (old >> 16));
       }
       __syncthreads();
-      if (has_atoms) {
-        // Rows grouped by key, positives first: cur[s] packs the positive
-        // cursor (low half) and the negative cursor (high half); after the
-        // fill its high half is the end of slot s's rows.
+      {
+        // Owners become keys (probes compare keys directly); with atom
+        // literals, slot starts for per-key row lists, positives first.
         constexpr int kPer = kSlots / kEvalThreads;
-        uint32_t v[kPer], pc[kPer];
+        uint32_t v[kPer], key[kPer];
         uint32_t sum = 0;
 #pragma unroll
         for (int k = 0; k < kPer; ++k) {
-          const uint32_t w = (uint32_t)tbl[threadIdx.x * kPer + k];
-          pc[k] = w & 0xffffu;
-          v[k] = pc[k] + (w >> 16);
+          const int sl = threadIdx.x * kPer + k;
+          const uint32_t w = cnt[sl];
+          v[k] = (w & 0xffffu) + (w >> 16);
+          key[k] = w != 0u ? (uint32_t)raw[owner[sl] - 1u] : 0u;
           sum += v[k];
         }
-        uint32_t run = block_scan_excl(sum, s_warp, &s_total);
+        if (has_atoms) {
+          uint32_t run = block_scan_excl(sum, s_warp, &s_total);
 #pragma unroll
-        for (int k = 0; k < kPer; ++k) {
-          cur[threadIdx.x * kPer + k] = run | ((run + pc[k]) << 16);
-          run += v[k];
+          for (int k = 0; k < kPer; ++k) {
+            sstart[threadIdx.x * kPer + k] = run;
+            run += v[k];
+          }
+        } else {
+          __syncthreads();  // every owner read before any is overwritten
         }
-        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kPer; ++k)
+          if (v[k] != 0u) owner[threadIdx.x * kPer + k] = key[k];
+      }
+      __syncthreads();
+      if (has_atoms) {
         for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-          const uint32_t old = atomicAdd(&cur[rslot[i]], i < npos ? 1u : 0x10000u);
-          rpos[i] = (uint16_t)(i < npos ? (old & 0xffffu) : (old >> 16));
-        }
-        // Permute the atom columns into key order, in place: every thread
-        // holds its rows' values of one column across a barrier.
-        constexpr int kRowsPer = (kTile + kEvalThreads - 1) / kEvalThreads;
-        for (int q = 1; q < ncols; ++q) {
-          int32_t* col = raw + q * kTile;
-          int32_t val[kRowsPer];
-#pragma unroll
-          for (int k = 0; k < kRowsPer; ++k) {
-            const int i = threadIdx.x + k * kEvalThreads;
-            if (i < nt) val[k] = col[i];
-          }
-          __syncthreads();
-#pragma unroll
-          for (int k = 0; k < kRowsPer; ++k) {
-            const int i = threadIdx.x + k * kEvalThreads;
-            if (i < nt) col[rpos[i]] = val[k];
-          }
+          const int sl = rslot[i];
+          const uint32_t off = i < npos ? rrank[i] : (cnt[sl] & 0xffffu) + rrank[i];
+          rows[sstart[sl] + off] = (uint16_t)i;
         }
         __syncthreads();
       }
       // This thread's entries against the tile.
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
-        const Entry& x = ent[j];
-        if (x.L < 0) continue;
-        if (x.L != Lrun) {
+        if (!(j == 0 ? have : have1)) continue;
+        const int32_t k0 = j == 0 ? e_k0.x : e_k0.y;
+        const uint32_t meta = j == 0 ? e_meta.x : e_meta.y;
+        const int L = (int)(meta & 0xffu);
+        if (L != Lrun) {
           if (Lrun >= 0 && (cp | cn | bp | bn) != 0)
             flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
           bp = bn = cp = cn = 0;
-          Lrun = x.L;
+          Lrun = L;
         }
-        if (!x.ok0) continue;
-        uint32_t slot = mix32((uint32_t)x.k0) & (kSlots - 1);
-        unsigned long long w = 0;
+        if (!((meta >> 10) & 1u)) continue;
+        uint32_t slot = mix32((uint32_t)k0) & (kSlots - 1);
+        uint32_t w = 0;
         for (int probe = 0; probe < kSlots; ++probe) {
-          w = tbl[slot];
-          if ((uint32_t)w == 0u || (int32_t)(w >> 32) == x.k0) break;
+          w = cnt[slot];
+          if (w == 0u || (int32_t)owner[slot] == k0) break;
           slot = (slot + 1) & (kSlots - 1);
         }
-        const uint32_t P = (uint32_t)w & 0xffffu, N = ((uint32_t)w >> 16) & 0xffffu;
-        if (P + N == 0u) continue;
+        if (w == 0u) continue;
+        const uint32_t P = w & 0xffffu, N = w >> 16;
+        const uint32_t nchk = (meta >> 8) & 3u;
         uint32_t hp = 0, hn = 0;
-        if (x.nchk == 0) {
+        if (nchk == 0) {
           hp = P;
           hn = N;
         } else {
-          const uint32_t end = cur[slot] >> 16;
-          const uint32_t mid = end - N;
-          const uint32_t beg = mid - P;
-          if (x.nchk == 1) {
-            const int32_t* ca = raw + x.cA;
-            for (uint32_t r = beg; r < mid; ++r) hp += ca[r] == x.kA;
-            for (uint32_t r = mid; r < end; ++r) hn += ca[r] == x.kA;
-          } else if (x.nchk == 2) {
-            const int32_t* ca = raw + x.cA;
-            const int32_t* cb = raw + x.cB;
-            for (uint32_t r = beg; r < mid; ++r) hp += (ca[r] == x.kA) & (cb[r] == x.kB);
-            for (uint32_t r = mid; r < end; ++r) hn += (ca[r] == x.kA) & (cb[r] == x.kB);
+          const uint32_t beg = sstart[slot], mid = beg + P, end = mid + N;
+          const int32_t kA = j == 0 ? e_kA.x : e_kA.y;
+          if (nchk == 1) {
+            const int32_t* ca = raw + ((meta >> 12) & 7u) * kTile;
+            for (uint32_t x = beg; x < mid; ++x) hp += ca[rows[x]] == kA;
+            for (uint32_t x = mid; x < end; ++x) hn += ca[rows[x]] == kA;
+          } else if (nchk == 2) {
+            const int32_t kB = j == 0 ? e_kB.x : e_kB.y;
+            const int32_t* ca = raw + ((meta >> 12) & 7u) * kTile;
+            const int32_t* cb = raw + ((meta >> 16) & 7u) * kTile;
+            for (uint32_t x = beg; x < mid; ++x) {
+              const int r = rows[x];
+              hp += (ca[r] == kA) & (cb[r] == kB);
+            }
+            for (uint32_t x = mid; x < end; ++x) {
+              const int r = rows[x];
+              hn += (ca[r] == kA) & (cb[r] == kB);
+            }
           } else {
-            const LitDesc& d = a.lits[lit_begin + x.L];
-            for (uint32_t r = beg; r < end; ++r) {
+            // More than two checked columns: keys from the key table.
+            const LitDesc& d = a.lits[lit_begin + L];
+            const uint32_t e = (uint32_t)kA;
+            for (uint32_t x = beg; x < end; ++x) {
+              const int r = rows[x];
               bool pass = true;
-              for (int q = 1; q < x.nk && pass; ++q) {
+              for (int q = 1; q < d.nk && pass; ++q) {
                 const int ac = d.atom_col[q];
-                if (ac != 0) pass = raw[ac * kTile + r] == __ldg(d.keys + q * d.stride + x.e);
+                if (ac != 0) pass = raw[ac * kTile + r] == __ldg(d.keys + q * d.stride + e);
               }
               if (pass) {
-                if (r < mid) ++hp; else ++hn;
+                if (x < mid) ++hp; else ++hn;
               }
             }
           }
         }
-        bp += x.mult * hp;
-        bn += x.mult * hn;
+        const long long mlt = j == 0 ? e_mult.x : e_mult.y;
+        bp += mlt * hp;
+        bn += mlt * hn;
         cp += hp;
         cn += hn;
       }
       __syncthreads();
-      for (int i = threadIdx.x; i < nt; i += blockDim.x) tbl[rslot[i]] = 0ull;
+      for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        owner[rslot[i]] = 0u;
+        cnt[rslot[i]] = 0u;
+      }
       __syncthreads();
     }
     // Threads' entries are contiguous and increasing, so equal literals sit
@@ -1133,6 +1198,7 @@ struct LaunchJob {
   size_t smem;
   int grid;
   int plan_grid;
+  int gather_grid;
 };
 
 struct PreparedStep {
@@ -1149,7 +1215,7 @@ struct PreparedStep {
   std::vector<LaunchJob> launches;
   std::vector<unsigned char> blob;  // descriptors, to be copied to blob_dev
   void* blob_dev = nullptr;
-  unsigned int* counter = nullptr;  // [work counter, unit count]
+  unsigned int* counter = nullptr;  // [work counter, unit count, entry-record count]
 };
 
 int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
@@ -1301,18 +1367,37 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   memcpy(ps->blob.data(), sub_all.data(), gbytes);
   memcpy(ps->blob.data() + gbytes, ldesc.data(), lbytes);
   QFG_TRY(ctx->scratch[kScrLits].reserve(ctx, ps->blob.size() + 64));
-  // Work units: at most one per item plus one per kChunk entries.
-  std::vector<int64_t> caps;
-  int64_t max_cap = 1;
+  // Work units: at most one per item plus one per kChunk entries; entry
+  // records: every entry once, each unit's block padded to 4 records.
+  std::vector<int64_t> caps, ecaps;
+  int64_t max_cap = 1, max_ecap = 4;
   for (const Span& S : spans) {
-    int64_t cap = 1;
+    int64_t cap = 1, ecap = 4;
     for (size_t g = S.gbeg; g < S.gend; ++g) cap += (int64_t)(shard_hi - shard_lo);
-    for (int l = S.lit0; l < S.lit0 + S.nl; ++l) cap += ldesc[l].stride / kChunk + 1;
-    if (cap > (int64_t)UINT32_MAX) return set_error(ctx, QFG_ERR_INVALID, "too many work units");
+    for (int l = S.lit0; l < S.lit0 + S.nl; ++l) {
+      cap += ldesc[l].stride / kChunk + 1;
+      ecap += ldesc[l].stride;
+    }
+    ecap += 4 * cap;
+    ecap = (ecap + 3) & ~int64_t(3);
+    if (cap > (int64_t)UINT32_MAX || ecap > (int64_t)UINT32_MAX)
+      return set_error(ctx, QFG_ERR_INVALID, "too many work units");
     caps.push_back(cap);
+    ecaps.push_back(ecap);
     max_cap = std::max(max_cap, cap);
+    max_ecap = std::max(max_ecap, ecap);
   }
   QFG_TRY(ctx->scratch[kScrWork].reserve(ctx, sizeof(WorkUnit) * (size_t)max_cap));
+  QFG_TRY(ctx->scratch[kScrEntries].reserve(ctx, sizeof(int32_t) * 5 * (size_t)max_ecap));
+  EntryRecs recs;
+  {
+    int32_t* eb = ctx->scratch[kScrEntries].as<int32_t>();
+    recs.k0 = eb;
+    recs.kA = eb + max_ecap;
+    recs.kB = eb + 2 * max_ecap;
+    recs.meta = reinterpret_cast<uint32_t*>(eb + 3 * max_ecap);
+    recs.mult = eb + 4 * max_ecap;
+  }
   GroupDesc* gdev = ctx->scratch[kScrLits].as<GroupDesc>();
   LitDesc* ldev = reinterpret_cast<LitDesc*>(gdev + sub_all.size());
   ps->blob_dev = gdev;
@@ -1330,6 +1415,8 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     ea.units = ctx->scratch[kScrWork].as<WorkUnit>();
     ea.unit_count = ps->counter + 1;
     ea.unit_cap = (uint32_t)caps[si];
+    ea.entry_cap = (uint32_t)ecaps[si];
+    ea.rec = recs;
     ea.counts = counts;
     ea.max_cols = 1;
     for (size_t g = S.gbeg; g < S.gend; ++g) ea.max_cols = std::max(ea.max_cols, gdesc[g].ncols);
@@ -1340,6 +1427,7 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_batched_kernel,
                                                                kEvalThreads, L.smem));
     L.grid = ctx->num_sms * std::max(per_sm, 1);
+    L.gather_grid = ctx->num_sms * 8;
     L.plan_grid = (int)std::max<int64_t>(
         1, std::min<int64_t>((ea.total_items + 255) / 256, (int64_t)ctx->num_sms * 8));
     ps->launches.push_back(L);
@@ -1386,8 +1474,10 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
   QFG_TRY(stage_end(ctx, QFG_STAGE_BIND_PARTITION));
   QFG_TRY(stage_begin(ctx, QFG_STAGE_EVALUATE));
   for (const LaunchJob& L : ps.launches) {
-    QFG_CUDA(ctx, cudaMemsetAsync(ps.counter, 0, 2 * sizeof(unsigned int), ctx->stream));
+    QFG_CUDA(ctx, cudaMemsetAsync(ps.counter, 0, 3 * sizeof(unsigned int), ctx->stream));
     plan_units_kernel<<<L.plan_grid, 256, 0, ctx->stream>>>(L.ea);
+    QFG_LAUNCHED(ctx);
+    gather_entries_kernel<<<L.gather_grid, 32 * kGatherWarps, 0, ctx->stream>>>(L.ea);
     QFG_LAUNCHED(ctx);
     eval_batched_kernel<<<L.grid, kEvalThreads, L.smem, ctx->stream>>>(L.ea);
     QFG_LAUNCHED(ctx);
@@ -1426,8 +1516,12 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
   if (two_pass) words += (int64_t)max_ncols * (nb + 4 + 4 * np1) + 64;
   words += (int64_t)np1 * (ctx->num_sms * 2 + 3);
   int64_t units = (int64_t)plan.groups.size() << bits;
-  for (KeyTable* kt : plan.tables) units += kt->num_entries / kChunk + 1;
-  words += units * (int64_t)(sizeof(WorkUnit) / 4);
+  int64_t entries = 0;
+  for (KeyTable* kt : plan.tables) {
+    units += kt->num_entries / kChunk + 1;
+    entries += std::max<int64_t>(kt->num_entries, 1);
+  }
+  words += units * (int64_t)(sizeof(WorkUnit) / 4) + 5 * (entries + 4 * units + 8);
   *bytes = 4 * words + (int64_t)(sizeof(GroupDesc) + sizeof(LitDesc)) * n + 32 * (int64_t)n;
   return QFG_OK;
 }

@@ -65,6 +65,9 @@ __device__ __forceinline__ unsigned long long as_ull(long long v) {
 
 struct Ctx;
 
+// Grow-only scratch buffers per context (and per workspace); see ScratchSlot.
+constexpr int kNumScratch = 17;
+
 // A device allocation charged against the context's HBM budget.
 class DevBuf {
  public:
@@ -148,7 +151,7 @@ struct Ctx {
   // Released binding-set storage kept for reuse (still charged to `used`).
   std::vector<std::pair<void*, size_t>> binding_pool;
   // Grow-only scratch, reused by every call on this context.
-  DevBuf scratch[16];
+  DevBuf scratch[kNumScratch];
   // Double-buffered pinned staging for small host->device uploads
   // (descriptors), so an upload never waits on the stream.
   void* staging_host[2] = {nullptr, nullptr};
@@ -189,14 +192,16 @@ enum ScratchSlot {
   kScrJoin = 13,
   kScrJoin2 = 14,
   kScrLits = 15,
+  kScrEntries = 16,
 };
+static_assert(kScrEntries + 1 == kNumScratch, "scratch slot count");
 
 // An independent set of scratch buffers and a stream.  Evaluation code uses
 // ctx->scratch and ctx->stream; a WorkspaceScope swaps a workspace's buffers
 // and stream in for its lifetime, so that a captured graph or a serving slot
 // owns scratch that no other call touches.
 struct Workspace {
-  DevBuf scratch[16];
+  DevBuf scratch[kNumScratch];
   cudaStream_t stream = nullptr;
   int64_t bytes() const {
     int64_t t = 0;

@@ -120,12 +120,12 @@ int DevBuf::reserve(Ctx* ctx, size_t bytes) {
 }
 
 WorkspaceScope::WorkspaceScope(Ctx* ctx, Workspace* ws) : ctx_(ctx), ws_(ws) {
-  for (int i = 0; i < 16; ++i) std::swap(ctx_->scratch[i], ws_->scratch[i]);
+  for (int i = 0; i < kNumScratch; ++i) std::swap(ctx_->scratch[i], ws_->scratch[i]);
   std::swap(ctx_->stream, ws_->stream);
 }
 
 WorkspaceScope::~WorkspaceScope() {
-  for (int i = 0; i < 16; ++i) std::swap(ctx_->scratch[i], ws_->scratch[i]);
+  for (int i = 0; i < kNumScratch; ++i) std::swap(ctx_->scratch[i], ws_->scratch[i]);
   std::swap(ctx_->stream, ws_->stream);
 }
 
