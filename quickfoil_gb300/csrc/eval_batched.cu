@@ -436,72 +436,139 @@ bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* 
                     });
 }
 
+// Rows of a pass-2 work chunk: coarse bins (up to 9x apart in size, since
+// negatives outnumber positives) are cut into chunks so the persistent pass
+// 2 stays balanced.
+constexpr uint32_t kP2Chunk = 16384;
+
 // Bin starts of pass 1, twice: padded to multiples of 4 rows (where pass 1
 // writes and pass 2 reads, so that pass 2's copies are 16-byte aligned) and
-// unpadded (where pass 2 writes).  One block, nbins <= blockDim.x.
+// unpadded (where pass 2 writes); and the first pass-2 chunk of every bin
+// (chunk_start[nbins] = number of chunks).  One block, nbins <= blockDim.x.
 __global__ void pad_scan_kernel(const uint32_t* __restrict__ tot, int nbins, uint32_t* __restrict__ pad,
-                                uint32_t* __restrict__ unp) {
+                                uint32_t* __restrict__ unp, uint32_t* __restrict__ chunk_start) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   const uint32_t c = (int)threadIdx.x < nbins ? tot[threadIdx.x] : 0u;
   const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
   const uint32_t total = s_total;
   const uint32_t exp = block_scan_excl((c + 3u) & ~3u, s_warp, &s_total);
+  const uint32_t total_pad = s_total;
+  const uint32_t exc = block_scan_excl((c + kP2Chunk - 1u) / kP2Chunk, s_warp, &s_total);
   if ((int)threadIdx.x < nbins) {
     unp[threadIdx.x] = ex;
     pad[threadIdx.x] = exp;
+    chunk_start[threadIdx.x] = exc;
   }
   if (threadIdx.x == 0) {
     unp[nbins] = total;
-    pad[nbins] = s_total;
+    pad[nbins] = total_pad;
+    chunk_start[nbins] = s_total;
   }
 }
 
-// Pass 2: CTA b splits pass-1 bin b = (hash prefix c, label), read from its
-// padded range, into sub-bins 0 .. 2^sbits - 1 written from its unpadded
-// start, and records where each starts: fine_start[(b << sbits) + sub] (the
-// last CTA also writes the end, n).
-template <int NC>
-__global__ void __launch_bounds__(PassShape<NC>::kThreads, 1)
-bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ p1_pad, const uint32_t* __restrict__ p1_unp,
-                   const int32_t* __restrict__ in, int64_t in_stride, uint32_t* __restrict__ fine_start,
-                   int32_t* __restrict__ out) {
-  extern __shared__ __align__(16) unsigned char smem[];
+// Pass-2 chunk c: its coarse bin (the last bin whose first chunk is <= c;
+// bins without rows own no chunk) and row range in the padded layout.
+struct P2Chunk {
+  int bin;
+  uint32_t r0, r1;
+};
+__device__ __forceinline__ P2Chunk p2_chunk(const uint32_t* __restrict__ chunk_start, int nbins,
+                                            const uint32_t* __restrict__ pad,
+                                            const uint32_t* __restrict__ unp, uint32_t c) {
+  int lo = 0, hi = nbins - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (chunk_start[mid] <= c) lo = mid; else hi = mid - 1;
+  }
+  const uint32_t k = c - chunk_start[lo];
+  const uint32_t cnt = unp[lo + 1] - unp[lo];
+  P2Chunk r;
+  r.bin = lo;
+  r.r0 = pad[lo] + k * kP2Chunk;
+  r.r1 = pad[lo] + umin(cnt, (k + 1) * kP2Chunk);
+  return r;
+}
+
+// Sub-bin counts of every pass-2 chunk: h2[c * nsub + sub].
+__global__ void __launch_bounds__(512) bpart_p2hist_kernel(BPartArgs a, const uint32_t* __restrict__ pad,
+                                                           const uint32_t* __restrict__ unp,
+                                                           const uint32_t* __restrict__ chunk_start,
+                                                           const int32_t* __restrict__ keys,
+                                                           uint32_t* __restrict__ h2) {
+  __shared__ uint32_t cntr[1 << kMaxSubBits];
+  const int np1 = 2 << a.cbits;
+  const int bits = a.bits;
+  const int nsub = 1 << (a.bits - a.cbits);
+  const uint32_t mask = (uint32_t)(nsub - 1);
+  const uint32_t nch = chunk_start[np1];
+  for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
+    const P2Chunk ch = p2_chunk(chunk_start, np1, pad, unp, c);
+    for (int i = threadIdx.x; i < nsub; i += blockDim.x) cntr[i] = 0u;
+    __syncthreads();
+    uint32_t r = ch.r0 + threadIdx.x;
+    for (; r + 7 * blockDim.x < ch.r1; r += 8 * blockDim.x) {
+      int32_t k[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) k[j] = __ldg(keys + r + j * blockDim.x);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) atomicAdd(&cntr[top_bits(k[j], bits) & mask], 1u);
+    }
+    for (; r < ch.r1; r += blockDim.x) atomicAdd(&cntr[top_bits(__ldg(keys + r), bits) & mask], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nsub; i += blockDim.x) h2[(int64_t)c * nsub + i] = cntr[i];
+    __syncthreads();
+  }
+}
+
+// Per coarse bin b (one block, nsub <= blockDim.x): turns its chunks' sub-bin
+// counts into output cursors (sub-bin start + the counts of the bin's earlier
+// chunks) and records where each sub-bin starts: fine_start[(b << sbits) +
+// sub] (the last block also writes the end, n).
+__global__ void __launch_bounds__(512) bpart_p2scan_kernel(BPartArgs a, const uint32_t* __restrict__ unp,
+                                                           const uint32_t* __restrict__ chunk_start,
+                                                           uint32_t* __restrict__ h2,
+                                                           uint32_t* __restrict__ fine_start) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   const int sbits = a.bits - a.cbits;
   const int nsub = 1 << sbits;
-  const RoundSmem S = carve_round(smem, NC, nsub, PassShape<NC>::kRows);
+  const int np1 = 2 << a.cbits;
   const int b = blockIdx.x;
-  const uint32_t r0 = p1_pad[b], cnt = p1_unp[b + 1] - p1_unp[b], r1 = r0 + cnt;
-  const uint32_t o0 = p1_unp[b];
-  for (int i = threadIdx.x; i < nsub; i += blockDim.x) S.lcount[i] = 0u;
-  __syncthreads();
+  const uint32_t c0 = chunk_start[b], c1 = chunk_start[b + 1];
+  const int sub = threadIdx.x;
+  uint32_t run = 0;
+  if (sub < nsub) {
+    for (uint32_t c = c0; c < c1; ++c) {
+      const uint32_t v = h2[(int64_t)c * nsub + sub];
+      h2[(int64_t)c * nsub + sub] = run;
+      run += v;
+    }
+  }
+  const uint32_t ex = block_scan_excl(sub < nsub ? run : 0u, s_warp, &s_total);
+  if (sub < nsub) {
+    const uint32_t base = unp[b] + ex;
+    fine_start[((int64_t)b << sbits) + sub] = base;
+    for (uint32_t c = c0; c < c1; ++c) h2[(int64_t)c * nsub + sub] += base;
+  }
+  if (b == np1 - 1 && threadIdx.x == 0) fine_start[(int64_t)np1 << sbits] = unp[np1];
+}
+
+// Pass 2, persistent over chunks: each chunk of a coarse bin, read from the
+// padded layout, is split into sub-bins 0 .. 2^sbits - 1 at its cursors.
+template <int NC>
+__global__ void __launch_bounds__(PassShape<NC>::kThreads, 1)
+bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ pad, const uint32_t* __restrict__ unp,
+                   const uint32_t* __restrict__ chunk_start, const uint32_t* __restrict__ h2,
+                   const int32_t* __restrict__ in, int64_t in_stride, int32_t* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
+  const int np1 = 2 << a.cbits;
+  const int nsub = 1 << (a.bits - a.cbits);
+  const RoundSmem S = carve_round(smem, NC, nsub, PassShape<NC>::kRows);
   const uint32_t mask = (uint32_t)(nsub - 1);
   const int bits = a.bits;
-  {
-    // Eight independent key loads per thread per iteration.
-    uint32_t r = r0 + threadIdx.x;
-    for (; r + 7 * blockDim.x < r1; r += 8 * blockDim.x) {
-      int32_t k[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) k[j] = __ldg(in + r + j * blockDim.x);
-#pragma unroll
-      for (int j = 0; j < 8; ++j) atomicAdd(&S.lcount[top_bits(k[j], bits) & mask], 1u);
-    }
-    for (; r < r1; r += blockDim.x) atomicAdd(&S.lcount[top_bits(__ldg(in + r), bits) & mask], 1u);
-  }
-  __syncthreads();
-  const uint32_t c = (int)threadIdx.x < nsub ? S.lcount[threadIdx.x] : 0u;
-  const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
-  if ((int)threadIdx.x < nsub) {
-    S.cursor[threadIdx.x] = o0 + ex;
-    fine_start[((int64_t)b << sbits) + threadIdx.x] = o0 + ex;
-    S.lcount[threadIdx.x] = 0u;
-  }
-  if (b == (int)gridDim.x - 1 && threadIdx.x == 0)
-    fine_start[(int64_t)gridDim.x << sbits] = p1_unp[gridDim.x];
-  __syncthreads();
   ColPtrs<NC> src;
   OutPtrs<NC> dst;
 #pragma unroll
@@ -509,8 +576,16 @@ bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ p1_pad, const uint3
     src.p[q] = in + (int64_t)q * in_stride;
     dst.p[q] = out + (int64_t)q * a.n;
   }
-  stream_rounds<NC>(S, src, r0, r1, r1, nsub, dst, true, s_warp, &s_total,
-                    [=](int32_t key, uint32_t) { return top_bits(key, bits) & mask; });
+  for (int i = threadIdx.x; i < nsub; i += blockDim.x) S.lcount[i] = 0u;
+  const uint32_t nch = chunk_start[np1];
+  for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
+    const P2Chunk ch = p2_chunk(chunk_start, np1, pad, unp, c);
+    for (int i = threadIdx.x; i < nsub; i += blockDim.x) S.cursor[i] = h2[(int64_t)c * nsub + i];
+    __syncthreads();
+    stream_rounds<NC>(S, src, ch.r0, ch.r1, ch.r1, nsub, dst, true, s_warp, &s_total,
+                      [=](int32_t key, uint32_t) { return top_bits(key, bits) & mask; });
+    __syncthreads();
+  }
 }
 
 // Launches of the templated passes for a group's column count.
@@ -521,11 +596,11 @@ void launch_pass1(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t 
                                                                       aligned ? 1 : 0);
 }
 template <int NC>
-void launch_pass2(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t st,
-                  const uint32_t* p1_pad, const uint32_t* p1_unp, const int32_t* in, int64_t in_stride,
-                  uint32_t* fstart, int32_t* out) {
-  bpart_pass2_kernel<NC><<<grid, PassShape<NC>::kThreads, smem, st>>>(pa, p1_pad, p1_unp, in, in_stride,
-                                                                      fstart, out);
+void launch_pass2(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t st, const uint32_t* pad,
+                  const uint32_t* unp, const uint32_t* chunk_start, const uint32_t* h2,
+                  const int32_t* in, int64_t in_stride, int32_t* out) {
+  bpart_pass2_kernel<NC><<<grid, PassShape<NC>::kThreads, smem, st>>>(pa, pad, unp, chunk_start, h2, in,
+                                                                      in_stride, out);
 }
 template <int NC>
 cudaError_t set_pass_smem(size_t smem1, size_t smem2) {
@@ -841,13 +916,11 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     const uint32_t idx = s_idx;
     if (idx >= s_count) break;
     const WorkUnit U = s_unit;
-    // The next unit's record loads while this one runs.
+    // The next unit's index is claimed now and its record loaded after the
+    // key table is built, so neither wait sits on this unit's path.
     uint32_t nidx = 0;
     WorkUnit nu{};
-    if (threadIdx.x == 0) {
-      nidx = atomicAdd(a.work_counter, 1u);
-      if (nidx < s_count) nu = a.units[nidx];
-    }
+    if (threadIdx.x == 0) nidx = atomicAdd(a.work_counter, 1u);
     const GroupDesc& G = a.groups[U.group];
     const int32_t* __restrict__ gcols = G.cols;
     const int64_t gn = G.n;
@@ -876,13 +949,10 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     for (uint32_t t0 = 0; t0 < total; t0 += kTile) {
       const int nt = (int)umin((uint32_t)kTile, total - t0);
       const int npos = (int)umin((uint32_t)nt, U.Pp > t0 ? U.Pp - t0 : 0u);
-      for (int q = 0; q < ncols; ++q) {
-        const int32_t* src = gcols + (int64_t)q * gn;
-        int32_t* dst = raw + q * kTile;
-        for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-          const uint32_t v = t0 + i;
-          cp_async4(dst + i, src + (v < U.Pp ? U.ps + v : U.ns + (v - U.Pp)));
-        }
+      for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        const uint32_t v = t0 + i;
+        const int32_t* src = gcols + (v < U.Pp ? U.ps + v : U.ns + (v - U.Pp));
+        for (int q = 0; q < ncols; ++q) cp_async4(raw + q * kTile + i, src + (int64_t)q * gn);
       }
       cp_async_commit();
       cp_async_wait_all();
@@ -903,6 +973,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         rslot[i] = (uint16_t)slot;
         rrank[i] = (uint16_t)(posr ? (old & 0xffffu) : (old >> 16));
       }
+      if (threadIdx.x == 0 && t0 == 0 && nidx < s_count) nu = a.units[nidx];
       __syncthreads();
       {
         // Owners become keys (probes compare keys directly); with atom
@@ -1209,6 +1280,8 @@ struct PreparedStep {
   uint32_t* p1_tot = nullptr;
   uint32_t* p1_start = nullptr;   // padded bin starts (two passes)
   uint32_t* p1_unp = nullptr;     // unpadded bin starts (two passes)
+  uint32_t* chunk_start = nullptr;  // first pass-2 chunk of every bin
+  uint32_t* h2 = nullptr;         // pass-2 chunk sub-bin counts, then cursors
   int32_t* tmp_cols = nullptr;
   int64_t tmp_stride = 0;
   std::vector<PartJob> parts;
@@ -1259,8 +1332,10 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   const size_t tmp_off = (part_words + 63) & ~size_t(63);
   const size_t tmp_words = ps->two_pass ? (size_t)max_ncols * (size_t)ps->tmp_stride : 0;
   const size_t fs_words = (size_t)nfine + 1;
-  const size_t bins_words =
-      (size_t)ps->np1 + 1 + (size_t)ps->pgrid * ps->np1 + 2 * ((size_t)ps->np1 + 1);
+  const size_t h2_words =
+      ps->two_pass ? ((size_t)nb / kP2Chunk + (size_t)ps->np1 + 1) * ((size_t)1 << ps->sbits) : 0;
+  const size_t bins_words = (size_t)ps->np1 + 1 + (size_t)ps->pgrid * ps->np1 +
+                            3 * ((size_t)ps->np1 + 1) + h2_words;
   QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * (tmp_off + tmp_words)));
   QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(
       ctx, sizeof(uint32_t) * (groups.size() * fs_words + bins_words)));
@@ -1271,6 +1346,8 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   uint32_t* p1_base = ps->p1_tot + ps->np1 + 1;
   ps->p1_start = p1_base + (size_t)ps->pgrid * ps->np1;
   ps->p1_unp = ps->p1_start + ps->np1 + 1;
+  ps->chunk_start = ps->p1_unp + ps->np1 + 1;
+  ps->h2 = ps->chunk_start + ps->np1 + 1;
   for (auto& g : groups) {
     const int nc = (int)g.cols.size();
     const size_t s1 = round_smem_bytes(nc, ps->np1), s2 = round_smem_bytes(nc, 1 << ps->sbits);
@@ -1449,16 +1526,23 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
     const int nc = job.pa.ncols;
     const size_t s1 = round_smem_bytes(nc, ps.np1), s2 = round_smem_bytes(nc, 1 << ps.sbits);
     if (ps.two_pass) {
-      pad_scan_kernel<<<1, 512, 0, ctx->stream>>>(ps.p1_tot, ps.np1, ps.p1_start, ps.p1_unp);
+      pad_scan_kernel<<<1, 512, 0, ctx->stream>>>(ps.p1_tot, ps.np1, ps.p1_start, ps.p1_unp,
+                                                  ps.chunk_start);
       QFG_LAUNCHED(ctx);
 #define QFG_P1(N) \
   launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, ps.p1_start, ps.tmp_cols, ps.tmp_stride, job.vec)
       QFG_NC_SWITCH(nc, QFG_P1)
 #undef QFG_P1
       QFG_LAUNCHED(ctx);
+      bpart_p2hist_kernel<<<ps.pgrid * 2, 512, 0, ctx->stream>>>(job.pa, ps.p1_start, ps.p1_unp,
+                                                                 ps.chunk_start, ps.tmp_cols, ps.h2);
+      QFG_LAUNCHED(ctx);
+      bpart_p2scan_kernel<<<ps.np1, 512, 0, ctx->stream>>>(job.pa, ps.p1_unp, ps.chunk_start, ps.h2,
+                                                           job.fstart);
+      QFG_LAUNCHED(ctx);
 #define QFG_P2(N)                                                                                  \
-  launch_pass2<N>(job.pa, (unsigned)ps.np1, s2, ctx->stream, ps.p1_start, ps.p1_unp, ps.tmp_cols, \
-                  ps.tmp_stride, job.fstart, job.final_out)
+  launch_pass2<N>(job.pa, ps.pgrid, s2, ctx->stream, ps.p1_start, ps.p1_unp, ps.chunk_start, ps.h2, \
+                  ps.tmp_cols, ps.tmp_stride, job.final_out)
       QFG_NC_SWITCH(nc, QFG_P2)
 #undef QFG_P2
       QFG_LAUNCHED(ctx);
@@ -1514,7 +1598,8 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
     max_ncols = std::max(max_ncols, (int)g.cols.size());
   }
   if (two_pass) words += (int64_t)max_ncols * (nb + 4 + 4 * np1) + 64;
-  words += (int64_t)np1 * (ctx->num_sms * 2 + 3);
+  words += (int64_t)np1 * (ctx->num_sms * 2 + 5);
+  if (two_pass) words += (nb / kP2Chunk + np1 + 1) << (bits - kMaxCoarseBits);
   int64_t units = (int64_t)plan.groups.size() << bits;
   int64_t entries = 0;
   for (KeyTable* kt : plan.tables) {
