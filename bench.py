@@ -8,11 +8,17 @@ synthetic data.  ``--workload single_literal`` runs the 16M x 4 binding set /
 4M-tuple relation single-literal operator bench instead.
 
 A step = one batched evaluation of all the step's literals (exact counts).
-``value`` is literals/s with the binding set resident in HBM; ``e2e`` is the
-same metric through the C ABI from pinned host buffers (binding-set upload
-and count download inside the timed region); the plain per-literal GPU path
-is timed beside it (``per_literal``).  Inputs (768 MB of binding columns)
-are larger than the 129 MB L2, so no flush is needed between steps.
+The partition bits are first chosen by the engine's autotuner.  ``value`` is
+literals/s with the binding set resident in HBM, the step replayed from its
+captured CUDA graph (``direct`` gives the same step through the plain API
+call, with per-stage CUDA-event times); ``e2e`` is the same metric through the
+C ABI from pinned host buffers (binding-set upload and count download inside
+the timed region); the plain per-literal GPU path is timed beside it
+(``per_literal``).  ``serving`` runs the serving loop on 64 requests of
+concurrent rule searches (binding sets log-uniform over 10K-20M rows), first
+as a burst and then with Poisson arrivals at about 80% load, with p50/p99
+latency.  Inputs (768 MB of binding columns) are larger than the 129 MB L2,
+so no flush is needed between steps.
 
 ``--impl reference`` times the CPU restatement of the reference's operator
 chain (the oracle; the reference itself cannot be built on the GPU host) on
@@ -52,6 +58,7 @@ def parse_args():
     ap.add_argument("--no-per-literal", action="store_true")
     ap.add_argument("--eval-bits", type=int, default=0,
                     help="binding partition bits of the batched engine (0 = autotuned)")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop leg")
     return ap.parse_args()
 
 
@@ -136,7 +143,7 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(w, nthreads: int, sample: int, budget_s: float = 20.0):
+def cpu_baseline(w, nthreads: int, sample: int, budget_s: float = 12.0):
     """The oracle (CPU restatement of the reference chain) on a bounded
     sample of the step's literals; returns (literals/s, sample description)."""
     import oracle
@@ -233,6 +240,11 @@ def run_gb300(args):
     torch.cuda.synchronize()
     first_touch_ms = (time.perf_counter() - t0) * 1e3
     traffic = eng.step_traffic(b, w.literals)
+    tune = None
+    if not args.eval_bits:
+        bits, tms = eng.autotune_step(b, w.literals)
+        eng.set_option(C.QFG_OPT_AUTOTUNE, 1)
+        tune = {"partition_bits": bits, "ms_per_step": tms}
 
     for _ in range(args.warmup):
         eng.evaluate_step_device(b, lits_c, n, counts.data_ptr())
@@ -262,6 +274,29 @@ def run_gb300(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     batched_counts = counts.cpu().numpy().copy()
+
+    # The same step replayed from its captured CUDA graph (one launch a step).
+    eng.set_option(C.QFG_OPT_USE_GRAPHS, 1)
+    for _ in range(args.warmup):
+        eng.evaluate_step_device(b, lits_c, n, counts.data_ptr())
+    torch.cuda.synchronize()
+    glaunch0 = eng.kernel_launches()
+    barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        eng.evaluate_step_device(b, lits_c, n, counts.data_ptr())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    glaunches = eng.kernel_launches() - glaunch0
+    gms = ev0.elapsed_time(ev1) / args.steps
+    if dist is not None:
+        t = torch.tensor([gms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        gms = float(t.item())
+    graph_equal = bool(np.array_equal(counts.cpu().numpy(), batched_counts))
+    eng.set_option(C.QFG_OPT_USE_GRAPHS, 0)
 
     # Plain per-literal GPU path (one operator chain per literal).
     per_lit = None
@@ -302,6 +337,10 @@ def run_gb300(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
 
+    serving = None
+    if not args.no_serving and args.workload == "batched_step":
+        serving = run_serving(eng, w, dev, torch)
+
     if rank == 0:
         peak, peak_kind = measured_peak_hbm()
         st_ms = {k: v[0] / max(v[1], 1) * (v[1] / args.steps) for k, v in stages.items()}
@@ -310,8 +349,8 @@ def run_gb300(args):
         achieved = traffic[dominant] / (kernel_ms * 1e-3) / 1e9 if kernel_ms > 0 else 0.0
         line = {
             "metric": "candidate literals scored/s (batched persistent evaluation, exact counts)",
-            "value": n * world / (ms * 1e-3), "unit": "literals/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "value": n * world / (gms * 1e-3), "unit": "literals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": gms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32 keys / int64 counts", "data": "synthetic (seeded)",
             "config": workload_config(args, w),
@@ -319,15 +358,21 @@ def run_gb300(args):
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_s * 1e3,
                     "counts_equal_device_path": bool(np.array_equal(e2e_counts, batched_counts))},
-            "gpu_launches": launches,
+            "gpu_launches": glaunches,
+            "path": "step replayed from its CUDA graph",
+            "direct": {"value": n * world / (ms * 1e-3), "unit": "literals/s", "ms_per_step": ms,
+                       "gpu_launches": launches, "counts_equal_graph": graph_equal},
             "stages_ms_per_step": {k: round(v, 4) for k, v in st_ms.items() if v > 0},
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "algorithmic_bytes": traffic[dominant],
                          "peak_source": peak_kind},
             "first_touch_ms": first_touch_ms,
+            "autotune": tune,
             "algorithmic_bytes_per_step": traffic,
         }
+        if serving is not None:
+            line["serving"] = serving
         if per_lit is not None:
             line["per_literal"] = per_lit
             line["batched_over_per_literal"] = line["value"] / (per_lit["value"] * world)
@@ -347,6 +392,63 @@ def run_gb300(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def run_serving(eng, w, dev, torch, n_requests: int = 64, lits_per_request: int = 64, slots: int = 8):
+    """The serving loop (config 5): 64 rule searches' literal batches over
+    device-resident binding sets of log-uniform 10K-20M rows x 6 columns
+    (10% positive), against the step's relations; a burst (all requests at
+    once), then Poisson arrivals at ~80% of the burst throughput."""
+    from quickfoil_gb300 import workloads
+    rng = np.random.default_rng(11)
+    sizes = np.exp(rng.uniform(np.log(10_000), np.log(20_000_000), n_requests)).astype(np.int64)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(11)
+    reqs = []
+    for nrows in sizes:
+        cols = [torch.randint(0, w.domain, (int(nrows),), dtype=torch.int32, device=dev, generator=gen)
+                for _ in range(6)]
+        lits = workloads.random_literals(lits_per_request, w.relations, 6, rng)
+        b = eng.bindings(cols, int(nrows) // 10)
+        eng.step_scratch_bytes(b, lits)  # builds any key tables these literals need
+        reqs.append((b, lits, cols))
+    order = np.argsort(sizes)
+    check = [int(order[0]), int(order[n_requests // 2]), int(order[-1])]
+    alone = {i: eng.evaluate_step(reqs[i][0], reqs[i][1]) for i in check}
+    torch.cuda.synchronize()
+
+    def run(arrivals):
+        srv = eng.server(slots=slots)
+        t0 = time.perf_counter()
+        ids = []
+        for i, (b, lits, _) in enumerate(reqs):
+            while arrivals is not None and time.perf_counter() - t0 < arrivals[i]:
+                srv.poll()
+                time.sleep(0.0001)
+            ids.append(srv.submit(b, lits))
+        srv.drain()
+        dt = time.perf_counter() - t0
+        st = srv.stats()
+        equal = all(np.array_equal(srv.result(ids[i]), alone[i]) for i in check)
+        srv.close()
+        return dt, st, equal
+
+    burst_s, st_b, eq_b = run(None)
+    arrivals = np.cumsum(rng.exponential(burst_s / n_requests / 0.8, n_requests))
+    pois_s, st_p, eq_p = run(arrivals)
+    for b, _, _ in reqs:
+        b.close()
+    total = n_requests * lits_per_request
+    return {"requests": n_requests, "literals_per_request": lits_per_request, "slots": slots,
+            "binding_rows": {"min": int(sizes.min()), "median": int(np.median(sizes)),
+                             "max": int(sizes.max()), "total": int(sizes.sum())},
+            "burst": {"literals_per_s": total / burst_s, "makespan_ms": burst_s * 1e3,
+                      "p50_ms": st_b["p50_ms"], "p99_ms": st_b["p99_ms"],
+                      "peak_in_flight": st_b["peak_in_flight"]},
+            "poisson": {"literals_per_s": total / pois_s, "makespan_ms": pois_s * 1e3,
+                        "offered_load": 0.8, "p50_ms": st_p["p50_ms"], "p99_ms": st_p["p99_ms"],
+                        "peak_in_flight": st_p["peak_in_flight"]},
+            "counts_equal_alone": bool(eq_b and eq_p)}
 
 
 def main():

@@ -56,12 +56,13 @@ enum {
 /* Context options (qfg_ctx_set_option). */
 enum {
   QFG_OPT_NUM_RADIX_BITS = 1,   /* FLAGS_num_radix_bits for qfg_radix_partition defaults (5) */
-  QFG_OPT_EVAL_BITS = 2,        /* 0 = autotuned partition bits of the evaluation kernels */
+  QFG_OPT_EVAL_BITS = 2,        /* fixed partition bits of the batched path; 0 = automatic */
   QFG_OPT_WAIT_LIMIT = 3,       /* iteration limit of bounded device-side waits */
-  QFG_OPT_USE_GRAPHS = 4,       /* 1 = replay batched steps from captured CUDA graphs */
+  QFG_OPT_USE_GRAPHS = 4,       /* 1 = qfg_evaluate_step replays cached CUDA graphs (see below) */
   QFG_OPT_STAGE_TIMING = 5,     /* 1 = time each evaluation stage with CUDA events */
   QFG_OPT_SHARD_INDEX = 6,      /* this context's shard of the partition space (default 0) */
-  QFG_OPT_SHARD_COUNT = 7       /* number of shards (default 1); see qfg_evaluate_step */
+  QFG_OPT_SHARD_COUNT = 7,      /* number of shards (default 1); see qfg_evaluate_step */
+  QFG_OPT_AUTOTUNE = 8          /* 1 = use the partition bits qfg_autotune_step chose per size class */
 };
 
 /* Evaluation stages timed under QFG_OPT_STAGE_TIMING (the GPU counterpart of
@@ -187,6 +188,17 @@ int qfg_step_traffic(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_lit
 int qfg_step_scratch_bytes(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
                            const qfg_literal* literals, int64_t* bytes);
 
+/* Autotuner.  No reference counterpart (the reference reads FLAGS_num_radix_bits).
+ * Times the batched step over `bindings` at a few partition-bit settings
+ * around the automatic choice -- the bits fix the partition pass count
+ * (one pass up to 8 bits, two above) and the rows per shared-memory table --
+ * and records the fastest for the binding set's size class (floor(log2(rows))).
+ * Under QFG_OPT_AUTOTUNE = 1 every batched step of that size class uses the
+ * recorded bits (QFG_OPT_EVAL_BITS > 0 still overrides).  Counts do not depend
+ * on the bits.  Returns the chosen bits and their time per step. */
+int qfg_autotune_step(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
+                      const qfg_literal* literals, int32_t* best_bits, double* best_ms);
+
 /* ---- batched steps replayed from CUDA graphs ---------------------------- */
 /* No reference counterpart.  Captures the batched evaluation of `literals`
  * over `bindings` (as qfg_evaluate_step) into a CUDA graph with its own
@@ -196,7 +208,12 @@ int qfg_step_scratch_bytes(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t n
  * counts_dev (device memory).  The graph reads the binding set's columns at
  * replay time, so binding data refilled in place (same binding set, same
  * sizes) is evaluated by a replay.  The binding set, the relations and
- * counts_dev must outlive the graph. */
+ * counts_dev must outlive the graph.
+ * Under QFG_OPT_USE_GRAPHS = 1, qfg_evaluate_step itself keeps such graphs in
+ * a per-context cache keyed by the binding set's shape (handle, column
+ * pointers, sizes), the literal list and the partition options, and replays
+ * the cached graph when a step repeats; registering or releasing a relation
+ * empties the cache.  Stage timing does not apply to replayed steps. */
 typedef struct qfg_step_graph qfg_step_graph;
 int qfg_step_graph_create(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
                           const qfg_literal* literals, int64_t* counts_dev,

@@ -1112,8 +1112,19 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
   }
 }
 
+// Binding-size class of the autotuner: floor(log2(rows)).
+int size_class(int64_t n) {
+  int c = 0;
+  while ((n >> (c + 1)) > 0) ++c;
+  return c;
+}
+
 int auto_group_bits(Ctx* ctx, int64_t n) {
   if (ctx->eval_bits > 0) return std::min(ctx->eval_bits, kMaxPartitionBits);
+  if (ctx->autotune) {
+    auto it = ctx->tuned_bits.find(size_class(n));
+    if (it != ctx->tuned_bits.end()) return it->second;
+  }
   int bits = 1;
   while (bits < kMaxPartitionBits && (n >> bits) > kTargetRows) ++bits;
   return bits;
@@ -1620,6 +1631,8 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
   return enqueue_step(ctx, &ps);
 }
 
+int step_partition_bits(Ctx* ctx, int64_t nb) { return auto_group_bits(ctx, nb); }
+
 }  // namespace qfg
 
 using namespace qfg;
@@ -1631,8 +1644,66 @@ extern "C" int qfg_evaluate_step(qfg_ctx* c, const qfg_bindings* b, int32_t n,
   QFG_TRY(validate_literals(ctx, b, n, lits));
   unsigned long long* dev = nullptr;
   QFG_TRY(counts_begin(ctx, n, counts, flags, &dev));
-  QFG_TRY(evaluate_batched(ctx, b, n, lits, dev));
+  if (ctx->use_graphs)
+    QFG_TRY(evaluate_step_cached(ctx, b, n, lits, dev));
+  else
+    QFG_TRY(evaluate_batched(ctx, b, n, lits, dev));
   return counts_end(ctx, n, counts, flags, dev);
+}
+
+extern "C" int qfg_autotune_step(qfg_ctx* c, const qfg_bindings* b, int32_t n,
+                                 const qfg_literal* lits, int32_t* best_bits, double* best_ms) {
+  if (c == nullptr || b == nullptr) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  QFG_TRY(validate_literals(ctx, b, n, lits));
+  const int64_t nb = b->num_positive + b->num_negative;
+  const int saved_bits = ctx->eval_bits;
+  const bool saved_tune = ctx->autotune, saved_timing = ctx->stage_timing;
+  ctx->eval_bits = 0;
+  ctx->autotune = false;
+  const int base = auto_group_bits(ctx, nb);
+  QFG_TRY(ctx->scratch[kScrCounts].reserve(ctx, sizeof(int64_t) * 4 * (size_t)std::max(n, 1)));
+  unsigned long long* dev = ctx->scratch[kScrCounts].as<unsigned long long>();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int st = QFG_OK;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    st = cuda_error(ctx, cudaGetLastError(), "cudaEventCreate");
+  int best = base;
+  float best_t = -1.0f;
+  ctx->stage_timing = false;
+  for (int cand = std::max(1, base - 2); st == QFG_OK && cand <= std::min(kMaxPartitionBits, base + 1);
+       ++cand) {
+    ctx->eval_bits = cand;
+    st = evaluate_batched(ctx, b, n, lits, dev);  // sizes the scratch of this setting
+    if (st != QFG_OK) break;
+    if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) {
+      st = cuda_error(ctx, cudaGetLastError(), "cudaEventRecord");
+      break;
+    }
+    for (int rep = 0; rep < 2 && st == QFG_OK; ++rep) st = evaluate_batched(ctx, b, n, lits, dev);
+    if (st != QFG_OK) break;
+    float ms = 0.0f;
+    if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      st = cuda_error(ctx, cudaGetLastError(), "timing");
+      break;
+    }
+    ms *= 0.5f;
+    if (best_t < 0.0f || ms < best_t) {
+      best_t = ms;
+      best = cand;
+    }
+  }
+  if (e0 != nullptr) cudaEventDestroy(e0);
+  if (e1 != nullptr) cudaEventDestroy(e1);
+  ctx->eval_bits = saved_bits;
+  ctx->autotune = saved_tune;
+  ctx->stage_timing = saved_timing;
+  if (st != QFG_OK) return st;
+  ctx->tuned_bits[size_class(nb)] = best;
+  if (best_bits != nullptr) *best_bits = best;
+  if (best_ms != nullptr) *best_ms = best_t;
+  return QFG_OK;
 }
 
 extern "C" int qfg_step_traffic(qfg_ctx* c, const qfg_bindings* b, int32_t n,

@@ -35,6 +35,14 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
 int upload_prepared(Ctx* ctx, const PreparedStep* ps, bool sync);
 int enqueue_step(Ctx* ctx, const PreparedStep* ps);
 bool prepared_is_empty(const PreparedStep* ps);
+// Partition bits a batched step over nb binding rows uses (option, tuned
+// table or the automatic rule).
+int step_partition_bits(Ctx* ctx, int64_t nb);
+// qfg_evaluate_step under QFG_OPT_USE_GRAPHS: replays (building on first use)
+// the cached graph of this step, then copies its counts to `counts`.
+int evaluate_step_cached(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
+                         unsigned long long* counts);
+void graph_cache_clear(Ctx* ctx);
 // Device scratch bytes a batched step over these literals needs.
 int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
                        int64_t* bytes);

@@ -16,6 +16,8 @@
 
 #include "../../include/qfgpu.h"
 
+struct qfg_step_graph;
+
 namespace qfg {
 
 constexpr unsigned kFullMask = 0xffffffffu;
@@ -144,6 +146,11 @@ struct Ctx {
   int eval_bits = 0;
   int64_t wait_limit = 1 << 26;
   int use_graphs = 0;
+  // QFG_OPT_USE_GRAPHS: captured steps by key (see step_runtime.cu).
+  std::map<std::string, qfg_step_graph*> graph_cache;
+  // QFG_OPT_AUTOTUNE: partition bits chosen per binding-size class.
+  bool autotune = false;
+  std::map<int, int> tuned_bits;
   int shard_index = 0;
   int shard_count = 1;
   int64_t launches = 0;
@@ -172,6 +179,8 @@ struct Ctx {
 // stage timing is on).  stage_end folds the previous measurement of that
 // stage in before re-arming, so a stage may run many times per call.
 int stage_begin(Ctx* ctx, int stage);
+// Drops the graphs cached under QFG_OPT_USE_GRAPHS (relations changed).
+void graph_cache_clear(Ctx* ctx);
 int stage_end(Ctx* ctx, int stage);
 int stage_collect(Ctx* ctx);
 

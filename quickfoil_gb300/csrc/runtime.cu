@@ -362,6 +362,7 @@ extern "C" int qfg_ctx_destroy(qfg_ctx* c) {
   if (c == nullptr) return QFG_ERR_INVALID;
   Ctx* ctx = &c->impl;
   cudaStreamSynchronize(ctx->stream);
+  graph_cache_clear(ctx);
   ctx->relations.clear();
   for (auto& s : ctx->scratch) s.release();
   free_binding_pool(ctx);
@@ -426,6 +427,9 @@ extern "C" int qfg_ctx_set_option(qfg_ctx* c, int option, int64_t value) {
       if (value < 1 || value > 65536)
         return set_error(ctx, QFG_ERR_INVALID, "shard count out of range [1, 65536]");
       ctx->shard_count = (int)value;
+      return QFG_OK;
+    case QFG_OPT_AUTOTUNE:
+      ctx->autotune = value != 0;
       return QFG_OK;
     default:
       return set_error(ctx, QFG_ERR_INVALID, "unknown option " + std::to_string(option));
@@ -509,6 +513,7 @@ extern "C" int qfg_relation_register(qfg_ctx* c, int32_t relation_id, int32_t nu
   QFG_TRY(load_columns(ctx, num_columns, columns, num_tuples, 0, num_tuples, flags,
                        &rel->storage, &rel->columns));
   QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->relations.count(relation_id)) graph_cache_clear(ctx);
   ctx->relations[relation_id] = std::move(rel);
   return QFG_OK;
 }
@@ -520,6 +525,7 @@ extern "C" int qfg_relation_release(qfg_ctx* c, int32_t relation_id) {
   if (it == ctx->relations.end())
     return set_error(ctx, QFG_ERR_NOT_FOUND, "unknown relation id " + std::to_string(relation_id));
   cudaStreamSynchronize(ctx->stream);
+  graph_cache_clear(ctx);
   ctx->relations.erase(it);
   return QFG_OK;
 }

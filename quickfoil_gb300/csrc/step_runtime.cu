@@ -43,38 +43,32 @@ struct qfg_step_graph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int64_t launches_per_replay = 0;
+  DevBuf own_counts;  // counts of a graph kept in the context's cache
 };
 
-extern "C" int qfg_step_graph_destroy(qfg_ctx* c, qfg_step_graph* g) {
-  if (c == nullptr || g == nullptr) return QFG_ERR_INVALID;
-  Ctx* ctx = &c->impl;
+namespace qfg {
+
+void step_graph_free(Ctx* ctx, qfg_step_graph* g) {
+  if (g == nullptr) return;
   cudaStreamSynchronize(ctx->stream);
   if (g->exec != nullptr) cudaGraphExecDestroy(g->exec);
   if (g->graph != nullptr) cudaGraphDestroy(g->graph);
   if (g->capture_stream != nullptr) cudaStreamSynchronize(g->capture_stream);
   g->ws.release();
+  g->own_counts.release();
   if (g->capture_stream != nullptr) cudaStreamDestroy(g->capture_stream);
   delete g;
-  return QFG_OK;
 }
 
-extern "C" int qfg_step_graph_create(qfg_ctx* c, const qfg_bindings* b, int32_t n,
-                                     const qfg_literal* lits, int64_t* counts_dev,
-                                     qfg_step_graph** out) {
-  if (c == nullptr || b == nullptr || out == nullptr) return QFG_ERR_INVALID;
-  Ctx* ctx = &c->impl;
-  *out = nullptr;
-  QFG_TRY(validate_literals(ctx, b, n, lits));
-  if (n > 0 && counts_dev == nullptr) return set_error(ctx, QFG_ERR_INVALID, "null counts");
-  auto g = new qfg_step_graph();
-  auto fail = [&](int st) {
-    qfg_step_graph_destroy(c, g);
-    return st;
-  };
+// Prepares the step in the graph's own workspace, runs it once uncaptured
+// (which sizes every scratch buffer it touches, so the captured run
+// allocates nothing), then captures the zeroing of the counts and the step's
+// device work.
+int step_graph_build(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
+                     unsigned long long* counts, qfg_step_graph* g) {
   if (cudaStreamCreateWithFlags(&g->capture_stream, cudaStreamNonBlocking) != cudaSuccess)
-    return fail(cuda_error(ctx, cudaGetLastError(), "cudaStreamCreate"));
+    return cuda_error(ctx, cudaGetLastError(), "cudaStreamCreate");
   g->ws.stream = g->capture_stream;
-  unsigned long long* counts = reinterpret_cast<unsigned long long*>(counts_dev);
   const bool timing = ctx->stage_timing;
   int st = QFG_OK;
   {
@@ -82,8 +76,6 @@ extern "C" int qfg_step_graph_create(qfg_ctx* c, const qfg_bindings* b, int32_t 
     PreparedStep* ps = prepared_step_new();
     st = prepare_step(ctx, b, n, lits, counts, ps);
     if (st == QFG_OK) st = upload_prepared(ctx, ps, true);
-    // One uncaptured run sizes every scratch buffer the step touches, so the
-    // captured run allocates nothing.
     if (st == QFG_OK) {
       ctx->stage_timing = false;
       st = enqueue_step(ctx, ps);
@@ -109,20 +101,99 @@ extern "C" int qfg_step_graph_create(qfg_ctx* c, const qfg_bindings* b, int32_t 
     ctx->stage_timing = timing;
     prepared_step_free(ps);
   }
-  if (st != QFG_OK) return fail(st);
-  cudaError_t e = cudaGraphInstantiate(&g->exec, g->graph, 0);
-  if (e != cudaSuccess) return fail(cuda_error(ctx, e, "cudaGraphInstantiate"));
+  if (st != QFG_OK) return st;
+  QFG_CUDA(ctx, cudaGraphInstantiate(&g->exec, g->graph, 0));
+  return QFG_OK;
+}
+
+int step_graph_replay(Ctx* ctx, qfg_step_graph* g) {
+  if (g->exec == nullptr) return QFG_OK;
+  QFG_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+  ctx->launches += g->launches_per_replay;
+  return QFG_OK;
+}
+
+void graph_cache_clear(Ctx* ctx) {
+  for (auto& kv : ctx->graph_cache) step_graph_free(ctx, kv.second);
+  ctx->graph_cache.clear();
+}
+
+namespace {
+
+constexpr size_t kGraphCacheEntries = 8;
+
+template <typename T>
+void append_bytes(std::string* key, const T& v) {
+  key->append(reinterpret_cast<const char*>(&v), sizeof(T));
+}
+
+}  // namespace
+
+int evaluate_step_cached(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
+                         unsigned long long* counts) {
+  const int64_t nb = b->num_positive + b->num_negative;
+  std::string key;
+  append_bytes(&key, b);
+  append_bytes(&key, b->num_positive);
+  append_bytes(&key, b->num_negative);
+  for (const int32_t* c : b->columns) append_bytes(&key, c);
+  append_bytes(&key, n);
+  key.append(reinterpret_cast<const char*>(lits), sizeof(qfg_literal) * (size_t)n);
+  append_bytes(&key, step_partition_bits(ctx, nb));
+  append_bytes(&key, ctx->shard_index);
+  append_bytes(&key, ctx->shard_count);
+  auto it = ctx->graph_cache.find(key);
+  qfg_step_graph* g = nullptr;
+  if (it != ctx->graph_cache.end()) {
+    g = it->second;
+  } else {
+    if (ctx->graph_cache.size() >= kGraphCacheEntries) graph_cache_clear(ctx);
+    g = new qfg_step_graph();
+    int st = g->own_counts.reserve(ctx, sizeof(int64_t) * 4 * (size_t)std::max(n, 1));
+    if (st == QFG_OK)
+      st = step_graph_build(ctx, b, n, lits, g->own_counts.as<unsigned long long>(), g);
+    if (st != QFG_OK) {
+      step_graph_free(ctx, g);
+      return st;
+    }
+    ctx->graph_cache[key] = g;
+  }
+  QFG_TRY(step_graph_replay(ctx, g));
+  if (n > 0)
+    QFG_CUDA(ctx, cudaMemcpyAsync(counts, g->own_counts.ptr(), sizeof(int64_t) * 4 * (size_t)n,
+                                  cudaMemcpyDeviceToDevice, ctx->stream));
+  return QFG_OK;
+}
+
+}  // namespace qfg
+
+extern "C" int qfg_step_graph_destroy(qfg_ctx* c, qfg_step_graph* g) {
+  if (c == nullptr || g == nullptr) return QFG_ERR_INVALID;
+  step_graph_free(&c->impl, g);
+  return QFG_OK;
+}
+
+extern "C" int qfg_step_graph_create(qfg_ctx* c, const qfg_bindings* b, int32_t n,
+                                     const qfg_literal* lits, int64_t* counts_dev,
+                                     qfg_step_graph** out) {
+  if (c == nullptr || b == nullptr || out == nullptr) return QFG_ERR_INVALID;
+  Ctx* ctx = &c->impl;
+  *out = nullptr;
+  QFG_TRY(validate_literals(ctx, b, n, lits));
+  if (n > 0 && counts_dev == nullptr) return set_error(ctx, QFG_ERR_INVALID, "null counts");
+  auto g = new qfg_step_graph();
+  const int st = step_graph_build(ctx, b, n, lits, reinterpret_cast<unsigned long long*>(counts_dev), g);
+  if (st != QFG_OK) {
+    step_graph_free(ctx, g);
+    return st;
+  }
   *out = g;
   return QFG_OK;
 }
 
 extern "C" int qfg_step_graph_launch(qfg_ctx* c, qfg_step_graph* g) {
   if (c == nullptr || g == nullptr) return QFG_ERR_INVALID;
-  Ctx* ctx = &c->impl;
-  if (g->exec == nullptr) return QFG_OK;
-  QFG_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
-  ctx->launches += g->launches_per_replay;
-  return QFG_OK;
+  return step_graph_replay(&c->impl, g);
 }
 
 // ---------------------------------------------------------------------------

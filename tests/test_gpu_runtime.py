@@ -135,3 +135,52 @@ def test_server_budget_serialises_requests(engine):
     srv.close()
     for _, b, _, _ in reqs:
         b.close()
+
+
+def test_cached_graphs_give_the_same_counts_and_follow_relation_changes(engine):
+    from quickfoil_gb300._capi import QFG_OPT_USE_GRAPHS
+    w = workloads.small_random(7, n_bindings=30000, max_tuples=6000, num_literals=40)
+    lits = _register(engine, w)
+    cols = _dev_columns(w.binding_columns)
+    b = engine.bindings(cols, w.num_positive)
+    want = engine.evaluate_step(b, lits)
+    engine.set_option(QFG_OPT_USE_GRAPHS, 1)
+    try:
+        for _ in range(3):  # first call captures, the others replay
+            np.testing.assert_array_equal(engine.evaluate_step(b, lits), want)
+        # refilled in place: the replay reads the new contents
+        new_cols = [np.random.default_rng(5).permutation(c) for c in w.binding_columns]
+        torch.cuda.synchronize()
+        for c, n in zip(cols, new_cols):
+            c.copy_(torch.from_numpy(n))
+        torch.cuda.synchronize()
+        got = engine.evaluate_step(b, lits)
+        engine.set_option(QFG_OPT_USE_GRAPHS, 0)
+        np.testing.assert_array_equal(got, engine.evaluate_step(b, lits))
+        engine.set_option(QFG_OPT_USE_GRAPHS, 1)
+        # a relation registered again under the same id with other tuples
+        rid = lits[0].relation
+        rel = w.relations[rid - lits[0].relation + next(iter(dict.fromkeys(w.literals))).relation]
+        engine.register_relation(rid, [np.asarray(c)[::-1].copy() + 1 for c in rel])
+        got = engine.evaluate_step(b, lits)
+        engine.set_option(QFG_OPT_USE_GRAPHS, 0)
+        np.testing.assert_array_equal(got, engine.evaluate_step(b, lits))
+    finally:
+        engine.set_option(QFG_OPT_USE_GRAPHS, 0)
+    b.close()
+
+
+def test_autotuner_picks_bits_and_keeps_counts(engine):
+    from quickfoil_gb300._capi import QFG_OPT_AUTOTUNE
+    w = workloads.small_random(8, n_bindings=400_000, max_tuples=20000, num_literals=30)
+    lits = _register(engine, w)
+    b = engine.bindings(_dev_columns(w.binding_columns), w.num_positive)
+    want = engine.evaluate_step(b, lits)
+    bits, ms = engine.autotune_step(b, lits)
+    assert 1 <= bits <= 16 and ms > 0
+    engine.set_option(QFG_OPT_AUTOTUNE, 1)
+    try:
+        np.testing.assert_array_equal(engine.evaluate_step(b, lits), want)
+    finally:
+        engine.set_option(QFG_OPT_AUTOTUNE, 0)
+    b.close()
