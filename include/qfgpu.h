@@ -70,9 +70,10 @@ enum {
 enum {
   QFG_STAGE_KEY_TABLES = 0,     /* relation partitions / key tables (first touch only) */
   QFG_STAGE_BIND_PARTITION = 1, /* binding-set partitioning */
-  QFG_STAGE_EVALUATE = 2,       /* build + probe + count */
+  QFG_STAGE_EVALUATE = 2,       /* the persistent build + probe + count kernel */
   QFG_STAGE_PER_LITERAL = 3,    /* plain per-literal join-count kernels */
-  QFG_NUM_STAGES = 4
+  QFG_STAGE_UNIT_PLAN = 4,      /* work units and entry records of the batched step */
+  QFG_NUM_STAGES = 5
 };
 
 typedef struct qfg_ctx qfg_ctx;

@@ -39,7 +39,7 @@ QFG_OPT_SHARD_INDEX = 6
 QFG_OPT_SHARD_COUNT = 7
 QFG_OPT_AUTOTUNE = 8
 
-STAGES = ("key_tables", "bind_partition", "evaluate", "per_literal")
+STAGES = ("key_tables", "bind_partition", "evaluate", "per_literal", "unit_plan")
 
 
 class QfgLiteral(ctypes.Structure):

@@ -1567,17 +1567,19 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
     }
   }
   QFG_TRY(stage_end(ctx, QFG_STAGE_BIND_PARTITION));
-  QFG_TRY(stage_begin(ctx, QFG_STAGE_EVALUATE));
   for (const LaunchJob& L : ps.launches) {
+    QFG_TRY(stage_begin(ctx, QFG_STAGE_UNIT_PLAN));
     QFG_CUDA(ctx, cudaMemsetAsync(ps.counter, 0, 3 * sizeof(unsigned int), ctx->stream));
     plan_units_kernel<<<L.plan_grid, 256, 0, ctx->stream>>>(L.ea);
     QFG_LAUNCHED(ctx);
     gather_entries_kernel<<<L.gather_grid, 32 * kGatherWarps, 0, ctx->stream>>>(L.ea);
     QFG_LAUNCHED(ctx);
+    QFG_TRY(stage_end(ctx, QFG_STAGE_UNIT_PLAN));
+    QFG_TRY(stage_begin(ctx, QFG_STAGE_EVALUATE));
     eval_batched_kernel<<<L.grid, kEvalThreads, L.smem, ctx->stream>>>(L.ea);
     QFG_LAUNCHED(ctx);
+    QFG_TRY(stage_end(ctx, QFG_STAGE_EVALUATE));
   }
-  QFG_TRY(stage_end(ctx, QFG_STAGE_EVALUATE));
   return QFG_OK;
 }
 
@@ -1716,6 +1718,7 @@ extern "C" int qfg_step_traffic(qfg_ctx* c, const qfg_bindings* b, int32_t n,
   if (n == 0) return QFG_OK;
   StepPlan plan;
   QFG_TRY(plan_step(ctx, n, lits, &plan));
+  const int bits_for_traffic = auto_group_bits(ctx, nb);
   // Key tables: read the projected relation columns once, write the table.
   std::map<const KeyTable*, int> seen;
   for (int i = 0; i < n; ++i) {
@@ -1732,9 +1735,18 @@ extern "C" int qfg_step_traffic(qfg_ctx* c, const qfg_bindings* b, int32_t n,
     bytes[QFG_STAGE_BIND_PARTITION] += 8 * nb * (int64_t)g.cols.size();
     // Evaluate: partitioned columns read once, every literal's key tuples
     // and multiplicities read once, four int64 counts written.
+    // Work units: each literal's offsets pair per partition read; entry
+    // records written once (join key, two further keys, meta, multiplicity)
+    // after the key tables' keys and multiplicities were read.
+    // Evaluation kernel: partitioned columns read once, entry records read
+    // once, four int64 counts per literal written.
     bytes[QFG_STAGE_EVALUATE] += 4 * nb * (int64_t)g.cols.size();
-    for (int i : g.lits)
-      bytes[QFG_STAGE_EVALUATE] += 4 * plan.tables[i]->num_entries * (plan.tables[i]->num_keys + 1) + 32;
+    for (int i : g.lits) {
+      const int64_t ne = plan.tables[i]->num_entries;
+      bytes[QFG_STAGE_UNIT_PLAN] += 8 * ((int64_t)1 << bits_for_traffic) +
+                                    4 * ne * (plan.tables[i]->num_keys + 1) + 20 * ne;
+      bytes[QFG_STAGE_EVALUATE] += 20 * ne + 32;
+    }
   }
   // The plain path re-partitions the join column per literal (value +
   // tuple id, 12 bytes a row), reads the relation partition (8 bytes a
