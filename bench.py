@@ -353,6 +353,34 @@ def run_gb300(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
 
+    # End to end, pipelined through the serving API: step i+1's binding set
+    # uploads on the context stream while step i evaluates on a server slot.
+    def pipelined(steps):
+        srv = eng.server(slots=2)
+        prev, got = None, None
+        for _ in range(steps):
+            be = eng.bindings(pinned, w.num_positive)
+            rid = srv.submit(be, w.literals)
+            if prev is not None:
+                got = srv.result(prev[0]).copy()
+                prev[1].close()
+            prev = (rid, be)
+        got = srv.result(prev[0]).copy()
+        prev[1].close()
+        srv.close()
+        return got
+
+    pipelined(max(2, min(args.warmup, 3)))
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    pipe_counts = pipelined(args.steps)
+    pipe_s = (time.perf_counter() - t0) / args.steps
+    if dist is not None:
+        t = torch.tensor([pipe_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        pipe_s = float(t.item())
+
     serving = None
     if not args.no_serving and args.workload == "batched_step":
         serving = run_serving(eng, w, dev, torch)
@@ -377,10 +405,17 @@ def run_gb300(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32 keys / int64 counts", "data": "synthetic (seeded)",
             "config": workload_config(args, w),
-            "e2e": {"value": n * world / e2e_s, "unit": "literals/s",
+            "e2e": {"value": n * world / pipe_s, "unit": "literals/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": e2e_s * 1e3,
-                    "counts_equal_device_path": bool(np.array_equal(e2e_counts, batched_counts))},
+                    "ms_per_step": pipe_s * 1e3,
+                    "mode": "pipelined through qfg_server: each step uploads its binding set "
+                            "from pinned host memory (qfg_bindings_create) while the previous "
+                            "step evaluates, counts read back to the host every step",
+                    "counts_equal_device_path": bool(np.array_equal(pipe_counts, batched_counts))},
+            "e2e_serial": {"value": n * world / e2e_s, "unit": "literals/s",
+                           "ms_per_step": e2e_s * 1e3,
+                           "mode": "upload, qfg_evaluate_step, release, one step after another",
+                           "counts_equal_device_path": bool(np.array_equal(e2e_counts, batched_counts))},
             "gpu_launches": glaunches,
             "path": "step replayed from its CUDA graph",
             "direct": {"value": n * world / (ms * 1e-3), "unit": "literals/s", "ms_per_step": ms,

@@ -234,8 +234,11 @@ int qfg_step_graph_destroy(qfg_ctx* ctx, qfg_step_graph* graph);
  * arrays given at submission), returns up to max_ids ids retired and not yet
  * returned, and admits queued ones; qfg_server_wait blocks
  * for one request; qfg_server_drain for all.  qfg_server_stats reports
- * latency percentiles (submission to completion).  While a server is alive
- * the context is used through it only. */
+ * latency percentiles (submission to completion).  A request is ordered
+ * after the work queued on the context's stream when it was submitted, so a
+ * binding set uploaded with qfg_bindings_create just before its submission
+ * is complete when the request starts (and the next upload can overlap the
+ * request).  While a server is alive the context runs no other evaluation. */
 typedef struct qfg_server qfg_server;
 int qfg_server_create(qfg_ctx* ctx, int32_t slots, int64_t hbm_budget_bytes, qfg_server** out);
 int qfg_server_submit(qfg_server* server, const qfg_bindings* bindings, int32_t num_literals,

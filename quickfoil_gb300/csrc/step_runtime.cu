@@ -214,6 +214,12 @@ struct Request {
   std::atomic<int> done{0};  // set by the stream callback after `finished`
   int slot = -1;
   int status = QFG_OK;
+  // Recorded on the context stream at submission: work queued there before
+  // (e.g. the upload of this request's binding set) precedes the request.
+  cudaEvent_t ready = nullptr;
+  ~Request() {
+    if (ready != nullptr) cudaEventDestroy(ready);
+  }
 };
 
 struct Slot {
@@ -294,6 +300,10 @@ int server_admit(qfg_server* s) {
                                     sizeof(int64_t) * 4 * (size_t)std::max(n, 1), cudaHostAllocDefault);
       if (e != cudaSuccess) st = cuda_error(ctx, e, "cudaHostAlloc");
       else slot.pinned_cap = (size_t)std::max(n, 1) * 4;
+    }
+    if (st == QFG_OK && r->ready != nullptr) {
+      const cudaError_t e = cudaStreamWaitEvent(slot.stream, r->ready, 0);
+      if (e != cudaSuccess) st = cuda_error(ctx, e, "cudaStreamWaitEvent");
     }
     if (st == QFG_OK) {
       WorkspaceScope scope(ctx, &slot.ws);
@@ -384,6 +394,11 @@ extern "C" int qfg_server_submit(qfg_server* s, const qfg_bindings* b, int32_t n
   r->host_counts = host_counts;
   r->submitted = Clock::now();
   int st = step_scratch_bytes(ctx, b, n, lits, &r->scratch_bytes);
+  if (st == QFG_OK) {
+    cudaError_t e = cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(r->ready, ctx->stream);
+    if (e != cudaSuccess) st = cuda_error(ctx, e, "cudaEventRecord");
+  }
   if (st != QFG_OK) {
     delete r;
     return st;

@@ -184,3 +184,26 @@ def test_autotuner_picks_bits_and_keeps_counts(engine):
     finally:
         engine.set_option(QFG_OPT_AUTOTUNE, 0)
     b.close()
+
+
+def test_served_request_waits_for_its_binding_upload(engine):
+    """Binding sets uploaded from host memory right before submission: the
+    request starts after the upload, and the next upload overlaps it."""
+    reqs = []
+    for seed in (50, 51, 52):
+        w = workloads.small_random(seed, n_bindings=300_000, max_tuples=8000, num_literals=30)
+        lits = _register(engine, w)
+        b = engine.bindings(w.binding_columns, w.num_positive)
+        reqs.append((w, lits, engine.evaluate_step(b, lits)))
+        b.close()
+    srv = engine.server(slots=2)
+    ids, keep = [], []
+    for w, lits, _ in reqs * 2:
+        b = engine.bindings(w.binding_columns, w.num_positive)  # host upload on the context stream
+        ids.append(srv.submit(b, lits))
+        keep.append(b)
+    for rid, (_, _, want) in zip(ids, reqs * 2):
+        np.testing.assert_array_equal(srv.result(rid), want)
+    srv.close()
+    for b in keep:
+        b.close()
