@@ -193,3 +193,52 @@ def kinship(seed: int = 1, persons: int = 200, generations: int = 4, max_positiv
     target = positives + negatives
     return LearnTask("kinship", relations, ["parent", "male", "female", "sibling"],
                      [cols(target, 0), cols(target, 1)], len(positives), 3)
+
+
+def bongard(seed: int = 1, pictures: int = 300, mean_objects: float = 10.0,
+            inside_per_object: float = 2.0, max_positive: int = 100,
+            max_clause_length: int = 4) -> LearnTask:
+    """Bongard-like knowledge base (the planted-rule learn loop, scaled down):
+    `pictures` picture ids and object ids in disjoint ranges (one argument
+    type, as the learner sees them); element(picture, object) with
+    Poisson(mean_objects) objects per picture; circle/triangle/square(object)
+    unary, each object one shape uniformly; inside(object, object) random
+    ordered pairs of distinct objects of the same picture, about
+    `inside_per_object` per object.  The target pos(picture) holds for the
+    pictures with a circle inside a triangle: up to `max_positive` of them
+    are positives, every other picture is a negative."""
+    rng = np.random.default_rng(seed)
+    counts = rng.poisson(mean_objects, pictures)
+    counts = np.maximum(counts, 1)
+    obj_pic = np.repeat(np.arange(pictures), counts)
+    nobj = len(obj_pic)
+    obj_ids = (pictures + np.arange(nobj)).astype(np.int32)
+    shape = rng.integers(0, 3, nobj)
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    inside = set()
+    for p in range(pictures):
+        c = int(counts[p])
+        if c < 2:
+            continue
+        m = int(rng.poisson(inside_per_object * c))
+        for _ in range(m):
+            a, b = rng.integers(0, c, 2)
+            if a != b:
+                inside.add((int(obj_ids[starts[p] + a]), int(obj_ids[starts[p] + b])))
+    inside = sorted(inside)
+    shape_of = {int(o): int(s) for o, s in zip(obj_ids, shape)}
+    pic_of = {int(o): int(p) for o, p in zip(obj_ids, obj_pic)}
+    hit = sorted({pic_of[a] for a, b in inside if shape_of[a] == 0 and shape_of[b] == 1})
+    pos = set(int(v) for v in rng.permutation(hit)[:max_positive])
+    positives = sorted(pos)
+    negatives = [p for p in range(pictures) if p not in set(hit)]
+    cols = lambda pairs, k: np.array([x[k] for x in pairs], dtype=np.int32)
+    element = [(int(p), int(o)) for p, o in zip(obj_pic, obj_ids)]
+    relations = [[cols(element, 0), cols(element, 1)],
+                 [obj_ids[shape == 0].copy()],
+                 [obj_ids[shape == 1].copy()],
+                 [obj_ids[shape == 2].copy()],
+                 [cols(inside, 0), cols(inside, 1)]]
+    target = np.array(positives + negatives, dtype=np.int32)
+    return LearnTask("bongard", relations, ["element", "circle", "triangle", "square", "inside"],
+                     [target], len(positives), max_clause_length)

@@ -47,10 +47,18 @@ def eval_cases():
 
 
 def kinship():
-    """(relations, calls, clauses); calls are
+    return learn_trace("kinship")
+
+
+def bongard():
+    return learn_trace("bongard")
+
+
+def learn_trace(name):
+    """(relations, calls, clauses) of a learn-loop fixture; calls are
     ("evaluate", join_var, binding_columns, P, literals, counts) and
     ("extend", (npos, nneg), binding_columns, P, [literal], output_columns)."""
-    z = np.load(os.path.join(HERE, "kinship.npz"))
+    z = np.load(os.path.join(HERE, f"{name}.npz"))
     rels = unpack_relations(z, "r")
     calls = []
     for j in range(int(z["num_calls"][0])):

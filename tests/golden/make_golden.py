@@ -16,6 +16,9 @@ code (oracle/_ref, built from the reference sources by oracle/build_ref.sh).
                       every CreateLabelAwareBindingTables call (binding set,
                       literal, announced counts, output columns), plus the
                       learnt clauses.
+* bongard.npz      -- the same for a Bongard-like knowledge base (2000
+                      pictures, planted rule "a circle inside a triangle",
+                      clauses up to 4 literals).
 
 Only this script reads the reference; the tests read the fixtures, so they
 also run where the reference sources are absent.
@@ -144,9 +147,8 @@ def parse_trace(path):
     return calls, clauses
 
 
-def kinship():
-    task = workloads.kinship(seed=1)
-    trace = os.path.join(HERE, "_kinship_trace.txt")
+def learn_fixture(task, name):
+    trace = os.path.join(HERE, f"_{name}_trace.txt")
     clauses = ref.learn(task.relations, task.target_columns, task.num_positive,
                         task.max_clause_length, trace)
     calls, traced_clauses = parse_trace(trace)
@@ -172,13 +174,22 @@ def kinship():
             for k, c in enumerate(result):
                 out[f"k{j}_out{k}"] = c
     out["clauses"] = np.array(clauses)
-    np.savez_compressed(os.path.join(HERE, "kinship.npz"), **out)
-    print("kinship.npz:", len(calls), "calls;", clauses)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"{name}.npz:", len(calls), "calls;", clauses)
+
+
+def kinship():
+    learn_fixture(workloads.kinship(seed=1), "kinship")
+
+
+def bongard():
+    learn_fixture(workloads.bongard(seed=1, pictures=2000, max_positive=300), "bongard")
 
 
 if __name__ == "__main__" and "--batched-step" not in sys.argv:
     eval_cases()
     kinship()
+    bongard()
 
 
 def batched_step_reference():

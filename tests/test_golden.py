@@ -1,6 +1,6 @@
 """The oracle against golden fixtures produced by the reference's own code
 (tests/golden/make_golden.py): evaluation counts of seeded cases, and a full
-replay of the reference learner's kinship run (every Evaluate call's counts,
+replay of the reference learner's kinship and Bongard-like runs (every Evaluate call's counts,
 every binding-set extension's rows in order, the score of every candidate and
 the choice of the literal that was added)."""
 import numpy as np
@@ -49,6 +49,13 @@ def test_kinship_learns_the_planted_rule():
     assert clauses == ["target(0, 1) :-  r1(0), r3(2, 0), r0(2, 1)"]
 
 
+def test_bongard_learns_the_planted_rule():
+    _, calls, clauses = golden.bongard()
+    # pos(P) :- element(P, A), circle(A), inside(A, B), triangle(B)
+    assert clauses == ["target(0) :-  r0(0, 1), r1(1), r4(1, 2), r2(2)"]
+    assert sum(c[0] == "extend" for c in calls) == 3
+
+
 def best_literals_by_step(calls, counts_of):
     """For every extension, the candidates evaluated on the same binding set
     before it, scored with the reference formula from counts_of(call)."""
@@ -71,8 +78,9 @@ def best_literals_by_step(calls, counts_of):
     return out
 
 
-def test_kinship_trace_replays_on_the_oracle():
-    rels, calls, _ = golden.kinship()
+@pytest.mark.parametrize("name", ["kinship", "bongard"])
+def test_learn_trace_replays_on_the_oracle(name):
+    rels, calls, _ = golden.learn_trace(name)
     o = oracle.Oracle(rels)
     for call in calls:
         kind, key, cols, P, lits, result = call
@@ -89,8 +97,9 @@ def test_kinship_trace_replays_on_the_oracle():
     o.close()
 
 
-def test_added_literals_have_the_best_reference_score():
-    _, calls, _ = golden.kinship()
+@pytest.mark.parametrize("name", ["kinship", "bongard"])
+def test_added_literals_have_the_best_reference_score(name):
+    _, calls, _ = golden.learn_trace(name)
     steps = best_literals_by_step(calls, lambda ev: ev[5])
     assert steps
     for lit, (npos, nneg), scored in steps:

@@ -1,6 +1,6 @@
 """The GPU engine against golden fixtures produced by the reference's own code:
-seeded evaluation cases, and the reference learner's kinship run replayed
-call by call through the C ABI -- every Evaluate call (qfg_evaluate_group, the
+seeded evaluation cases, and the reference learner's kinship and Bongard-like
+runs replayed call by call through the C ABI -- every Evaluate call (qfg_evaluate_group, the
 drop-in for CandidateLiteralEvaluator::Evaluate), every binding-set extension
 (qfg_extend_bindings, rows in the reference's order), and the reference score
 of every candidate from GPU counts, with the added literal scoring best.
@@ -37,8 +37,9 @@ def test_engine_matches_reference_counts(engine):
         b.close()
 
 
-def test_kinship_trace_replays_on_the_gpu(engine):
-    rels, calls, _ = golden.kinship()
+@pytest.mark.parametrize("name", ["kinship", "bongard"])
+def test_learn_trace_replays_on_the_gpu(engine, name):
+    rels, calls, _ = golden.learn_trace(name)
     base = _register(engine, rels)
     gpu_counts = {}
     for j, call in enumerate(calls):
