@@ -560,7 +560,8 @@ template <int NC>
 __global__ void __launch_bounds__(PassShape<NC>::kThreads, 1)
 bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ pad, const uint32_t* __restrict__ unp,
                    const uint32_t* __restrict__ chunk_start, const uint32_t* __restrict__ h2,
-                   const int32_t* __restrict__ in, int64_t in_stride, int32_t* __restrict__ out) {
+                   const int32_t* __restrict__ in, int64_t in_stride, int32_t* __restrict__ out,
+                   int64_t out_stride) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
@@ -574,7 +575,7 @@ bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ pad, const uint32_t
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
     src.p[q] = in + (int64_t)q * in_stride;
-    dst.p[q] = out + (int64_t)q * a.n;
+    dst.p[q] = out + (int64_t)q * out_stride;
   }
   for (int i = threadIdx.x; i < nsub; i += blockDim.x) S.lcount[i] = 0u;
   const uint32_t nch = chunk_start[np1];
@@ -598,9 +599,9 @@ void launch_pass1(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t 
 template <int NC>
 void launch_pass2(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t st, const uint32_t* pad,
                   const uint32_t* unp, const uint32_t* chunk_start, const uint32_t* h2,
-                  const int32_t* in, int64_t in_stride, int32_t* out) {
+                  const int32_t* in, int64_t in_stride, int32_t* out, int64_t out_stride) {
   bpart_pass2_kernel<NC><<<grid, PassShape<NC>::kThreads, smem, st>>>(pa, pad, unp, chunk_start, h2, in,
-                                                                      in_stride, out);
+                                                                      in_stride, out, out_stride);
 }
 template <int NC>
 cudaError_t set_pass_smem(size_t smem1, size_t smem2) {
@@ -653,7 +654,7 @@ static_assert(kGroupCols == 8, "column-count dispatch covers 1..8");
 //                flushed to global memory when the CTA retires.
 
 struct GroupDesc {
-  const int32_t* cols;      // ncols SoA columns of n rows, partitioned
+  const int32_t* cols;      // ncols SoA partitioned columns, column stride n (a multiple of 4)
   int64_t n;
   const uint32_t* fstart;   // (2 << bits) + 1 segment starts
   int bits, sbits, ncols;
@@ -674,12 +675,17 @@ struct LitDesc {
 };
 
 struct WorkUnit {
+  const int32_t* cols;       // the group's partitioned columns
+  int64_t stride;            // their column stride (a multiple of 4 rows)
   uint32_t group, p;
   uint32_t ps, Pp, ns, Np;   // positive / negative segment of the partition
   uint32_t f0, ecnt;         // entries [f0, f0 + ecnt) of the item's literal-major space
   uint32_t eoff;             // first record of the unit's entry block (multiple of 4)
-  uint32_t pad[3];
+  uint32_t lit_begin;        // first literal of the group
+  uint32_t flags;            // carried columns | has_atoms << 8
+  uint32_t pad;
 };
+static_assert(sizeof(WorkUnit) == 64, "work unit record");
 
 // Entry records, SoA over the launch's entry blocks.  meta packs the
 // literal within its group (bits 0-7), the number of columns to check
@@ -709,13 +715,70 @@ struct EvalArgs {
   EntryRecs rec;
   unsigned int* work_counter;
   unsigned long long* counts;
+  int* error_flag;           // set when a bounded wait gave up
+  int64_t wait_limit;        // iterations of a bounded wait
 };
+
+// Shared-memory stride of a tile column: room for the alignment shifts of
+// the two segments (bulk copies keep shared and global addresses congruent
+// modulo 16 bytes).
+constexpr int kTileStride = kTile + 8;
 
 size_t eval_smem_bytes(int num_lits, int max_cols) {
   return sizeof(unsigned long long) * 4 * (size_t)num_lits +
-         sizeof(int32_t) * (size_t)max_cols * kTile + sizeof(uint32_t) * 3 * kSlots +
+         sizeof(int32_t) * (size_t)max_cols * kTileStride + sizeof(uint32_t) * 3 * kSlots +
          sizeof(uint16_t) * 3 * kTile;
 }
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0u;
+}
+// Bulk copy (TMA, no tensor map) of `bytes` (a multiple of 16) from global
+// to shared memory, both 16-byte aligned, completing on `bar`.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One segment of a tile column: global rows [g0, g0 + c) to shared index
+// s0 (s0 = g0 modulo 4).  Its 16-byte aligned body goes by one bulk copy;
+// the unaligned head and tail (at most 3 rows each, or all of a short
+// segment) by plain loads.
+struct SegPiece {
+  uint32_t g0, c, s0;
+  __device__ __forceinline__ uint32_t body_lo() const { return (g0 + 3u) & ~3u; }
+  __device__ __forceinline__ uint32_t body_hi() const { return (g0 + c) & ~3u; }
+  __device__ __forceinline__ bool has_body() const { return c > 0 && body_hi() > body_lo(); }
+  __device__ __forceinline__ uint32_t body_bytes() const {
+    return has_body() ? 4u * (body_hi() - body_lo()) : 0u;
+  }
+};
 
 __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
   const int lane = lane_id();
@@ -735,6 +798,10 @@ __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
       const int s = G.sbits;
       const uint32_t hc = p >> s, sub = p & ((1u << s) - 1u);
       const uint32_t ip = ((2u * hc) << s) + sub, in_ = ((2u * hc + 1u) << s) + sub;
+      u.cols = G.cols;
+      u.stride = G.n;
+      u.lit_begin = (uint32_t)G.lit_begin;
+      u.flags = (uint32_t)G.ncols | (G.has_atoms ? 0x100u : 0u);
       u.group = (uint32_t)lo;
       u.p = p;
       u.ps = G.fstart[ip];
@@ -888,13 +955,14 @@ __device__ __forceinline__ void flush_acc(unsigned long long* dst, long long cp,
 __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem);
-  int32_t* raw = reinterpret_cast<int32_t*>(acc + 4 * a.num_lits);   // max_cols * kTile
-  uint32_t* owner = reinterpret_cast<uint32_t*>(raw + a.max_cols * kTile);  // kSlots
+  int32_t* raw = reinterpret_cast<int32_t*>(acc + 4 * a.num_lits);   // max_cols * kTileStride
+  uint32_t* owner = reinterpret_cast<uint32_t*>(raw + a.max_cols * kTileStride);  // kSlots
   uint32_t* cnt = owner + kSlots;                                     // kSlots
   uint32_t* sstart = cnt + kSlots;                                    // kSlots
   uint16_t* rslot = reinterpret_cast<uint16_t*>(sstart + kSlots);     // kTile
   uint16_t* rrank = rslot + kTile;                                    // kTile
-  uint16_t* rows = rrank + kTile;                                     // kTile
+  uint16_t* rows = rrank + kTile;                                     // kTile: shared positions
+  __shared__ __align__(8) uint64_t s_bar;
   __shared__ WorkUnit s_unit;
   __shared__ uint32_t s_idx, s_count;
   __shared__ uint32_t s_warp[32];
@@ -909,8 +977,11 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     s_count = umin(a.unit_count[0], a.unit_cap);
     s_idx = atomicAdd(a.work_counter, 1u);
     if (s_idx < s_count) s_unit = a.units[s_idx];
+    mbar_init(&s_bar, 1);
+    fence_mbar_init();
   }
   __syncthreads();
+  uint32_t phase = 0;
 
   for (;;) {
     const uint32_t idx = s_idx;
@@ -921,12 +992,11 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     uint32_t nidx = 0;
     WorkUnit nu{};
     if (threadIdx.x == 0) nidx = atomicAdd(a.work_counter, 1u);
-    const GroupDesc& G = a.groups[U.group];
-    const int32_t* __restrict__ gcols = G.cols;
-    const int64_t gn = G.n;
-    const int ncols = G.ncols;
-    const int lit_begin = G.lit_begin;
-    const bool has_atoms = G.has_atoms != 0;
+    const int32_t* __restrict__ gcols = U.cols;
+    const int64_t gn = U.stride;
+    const int ncols = (int)(U.flags & 0xffu);
+    const int lit_begin = (int)U.lit_begin;
+    const bool has_atoms = (U.flags & 0x100u) != 0u;
     const uint32_t total = U.Pp + U.Np;
 
     // This thread's two entry records (a pair of consecutive records).
@@ -949,23 +1019,67 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     for (uint32_t t0 = 0; t0 < total; t0 += kTile) {
       const int nt = (int)umin((uint32_t)kTile, total - t0);
       const int npos = (int)umin((uint32_t)nt, U.Pp > t0 ? U.Pp - t0 : 0u);
-      for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-        const uint32_t v = t0 + i;
-        const int32_t* src = gcols + (v < U.Pp ? U.ps + v : U.ns + (v - U.Pp));
-        for (int q = 0; q < ncols; ++q) cp_async4(raw + q * kTile + i, src + (int64_t)q * gn);
+      // The tile's two segments (positives, negatives) of every carried
+      // column: row i sits at shared index i + shP (positives) or baseN +
+      // (i - npos) (negatives), congruent to its global row modulo 4.
+      SegPiece seg[2];
+      seg[0].g0 = U.ps + t0;
+      seg[0].c = (uint32_t)npos;
+      seg[0].s0 = seg[0].g0 & 3u;
+      seg[1].g0 = U.ns + (t0 > U.Pp ? t0 - U.Pp : 0u);
+      seg[1].c = (uint32_t)(nt - npos);
+      seg[1].s0 = seg[0].s0 + (uint32_t)npos + ((seg[1].g0 - (seg[0].s0 + (uint32_t)npos)) & 3u);
+      const uint32_t shP = seg[0].s0, baseN = seg[1].s0;
+      if (threadIdx.x == 0) {
+        fence_proxy_async_smem();  // this tile's copies come after all earlier reads of the buffer
+        mbar_arrive_expect_tx(&s_bar, (uint32_t)ncols * (seg[0].body_bytes() + seg[1].body_bytes()));
+        for (int q = 0; q < ncols; ++q)
+          for (int k = 0; k < 2; ++k)
+            if (seg[k].has_body())
+              bulk_g2s(raw + q * kTileStride + seg[k].s0 + (seg[k].body_lo() - seg[k].g0),
+                       gcols + (int64_t)q * gn + seg[k].body_lo(), seg[k].body_bytes(), &s_bar);
       }
-      cp_async_commit();
-      cp_async_wait_all();
+      if ((int)threadIdx.x < 4 * ncols) {
+        // Unaligned heads and tails: (column, segment, head or tail) per thread.
+        const int q = threadIdx.x >> 2, k = (threadIdx.x >> 1) & 1, tail = threadIdx.x & 1;
+        const SegPiece& sp = seg[k];
+        uint32_t lo, hi;
+        if (!sp.has_body()) {
+          lo = tail ? sp.g0 : sp.g0;
+          hi = tail ? sp.g0 : sp.g0 + sp.c;
+        } else {
+          lo = tail ? sp.body_hi() : sp.g0;
+          hi = tail ? sp.g0 + sp.c : sp.body_lo();
+        }
+        const int32_t* src = gcols + (int64_t)q * gn;
+        int32_t* dst = raw + q * kTileStride + sp.s0;
+        for (uint32_t g = lo; g < hi; ++g) dst[g - sp.g0] = __ldg(src + g);
+      }
+      {
+        // Bounded wait for the bulk copies; a wait that gives up flags the
+        // context and waits once more (bounded) for the copies in flight.
+        int64_t it = 0;
+        while (!mbar_try_wait(&s_bar, phase)) {
+          if (++it > a.wait_limit) {
+            atomicExch(a.error_flag, 1);
+            for (int64_t k2 = 0; k2 < a.wait_limit && !mbar_try_wait(&s_bar, phase); ++k2) {
+            }
+            break;
+          }
+        }
+        phase ^= 1u;
+      }
       __syncthreads();
       // Distinct join keys of the tile: owner = first row + 1, claimed by
       // CAS; the count atomics return each row's rank within its key and
       // label (positive count low half, negative count high half).
       for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-        const int32_t key = raw[i];
         const bool posr = i < npos;
+        const uint32_t pos = posr ? (uint32_t)i + shP : baseN + (uint32_t)(i - npos);
+        const int32_t key = raw[pos];
         uint32_t slot = mix32((uint32_t)key) & (kSlots - 1);
         for (int probe = 0; probe < kSlots; ++probe) {
-          const uint32_t o = atomicCAS(&owner[slot], 0u, (uint32_t)i + 1u);
+          const uint32_t o = atomicCAS(&owner[slot], 0u, pos + 1u);
           if (o == 0u || raw[o - 1u] == key) break;
           slot = (slot + 1) & (kSlots - 1);
         }
@@ -1007,8 +1121,9 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
       if (has_atoms) {
         for (int i = threadIdx.x; i < nt; i += blockDim.x) {
           const int sl = rslot[i];
-          const uint32_t off = i < npos ? rrank[i] : (cnt[sl] & 0xffffu) + rrank[i];
-          rows[sstart[sl] + off] = (uint16_t)i;
+          const bool posr = i < npos;
+          const uint32_t off = posr ? rrank[i] : (cnt[sl] & 0xffffu) + rrank[i];
+          rows[sstart[sl] + off] = (uint16_t)(posr ? (uint32_t)i + shP : baseN + (uint32_t)(i - npos));
         }
         __syncthreads();
       }
@@ -1044,13 +1159,13 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
           const uint32_t beg = sstart[slot], mid = beg + P, end = mid + N;
           const int32_t kA = j == 0 ? e_kA.x : e_kA.y;
           if (nchk == 1) {
-            const int32_t* ca = raw + ((meta >> 12) & 7u) * kTile;
+            const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
             for (uint32_t x = beg; x < mid; ++x) hp += ca[rows[x]] == kA;
             for (uint32_t x = mid; x < end; ++x) hn += ca[rows[x]] == kA;
           } else if (nchk == 2) {
             const int32_t kB = j == 0 ? e_kB.x : e_kB.y;
-            const int32_t* ca = raw + ((meta >> 12) & 7u) * kTile;
-            const int32_t* cb = raw + ((meta >> 16) & 7u) * kTile;
+            const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
+            const int32_t* cb = raw + ((meta >> 16) & 7u) * kTileStride;
             for (uint32_t x = beg; x < mid; ++x) {
               const int r = rows[x];
               hp += (ca[r] == kA) & (cb[r] == kB);
@@ -1068,7 +1183,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
               bool pass = true;
               for (int q = 1; q < d.nk && pass; ++q) {
                 const int ac = d.atom_col[q];
-                if (ac != 0) pass = raw[ac * kTile + r] == __ldg(d.keys + q * d.stride + e);
+                if (ac != 0) pass = raw[ac * kTileStride + r] == __ldg(d.keys + q * d.stride + e);
               }
               if (pass) {
                 if (x < mid) ++hp; else ++hn;
@@ -1295,6 +1410,7 @@ struct PreparedStep {
   uint32_t* h2 = nullptr;         // pass-2 chunk sub-bin counts, then cursors
   int32_t* tmp_cols = nullptr;
   int64_t tmp_stride = 0;
+  int64_t col_stride = 0;   // column stride of the partitioned layout
   std::vector<PartJob> parts;
   std::vector<LaunchJob> launches;
   std::vector<unsigned char> blob;  // descriptors, to be copied to blob_dev
@@ -1332,10 +1448,13 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   const int nfine = 2 << bits;
   ps->np1 = 2 << ps->cbits;
   ps->pgrid = (unsigned)ctx->num_sms;
+  // Partitioned columns: stride a multiple of 4 rows, so every column of a
+  // group has the same 16-byte alignment (the evaluation's bulk copies).
+  ps->col_stride = ((int64_t)nb + 3) & ~int64_t(3);
   size_t part_words = 0;
   int max_ncols = 1;
   for (auto& g : groups) {
-    part_words += g.cols.size() * (size_t)nb;
+    part_words += g.cols.size() * (size_t)ps->col_stride;
     max_ncols = std::max(max_ncols, (int)g.cols.size());
   }
   // Pass-1 output: bins padded to multiples of 4 rows, 16-byte aligned columns.
@@ -1392,7 +1511,7 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
 
     GroupDesc& d = gdesc[gi];
     d.cols = job.final_out;
-    d.n = nb;
+    d.n = ps->col_stride;
     d.fstart = job.fstart;
     d.bits = bits;
     d.sbits = ps->sbits;
@@ -1417,7 +1536,7 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
       ldesc.push_back(ld);
     }
     d.lit_end = (int)ldesc.size();
-    off += g.cols.size() * (size_t)nb;
+    off += g.cols.size() * (size_t)ps->col_stride;
   }
 
   // Launches of at most kMaxLitsPerLaunch literals (groups never straddle a
@@ -1505,6 +1624,8 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     ea.unit_cap = (uint32_t)caps[si];
     ea.entry_cap = (uint32_t)ecaps[si];
     ea.rec = recs;
+    ea.error_flag = ctx->error_flag;
+    ea.wait_limit = ctx->wait_limit;
     ea.counts = counts;
     ea.max_cols = 1;
     for (size_t g = S.gbeg; g < S.gend; ++g) ea.max_cols = std::max(ea.max_cols, gdesc[g].ncols);
@@ -1553,14 +1674,14 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
       QFG_LAUNCHED(ctx);
 #define QFG_P2(N)                                                                                  \
   launch_pass2<N>(job.pa, ps.pgrid, s2, ctx->stream, ps.p1_start, ps.p1_unp, ps.chunk_start, ps.h2, \
-                  ps.tmp_cols, ps.tmp_stride, job.final_out)
+                  ps.tmp_cols, ps.tmp_stride, job.final_out, ps.col_stride)
       QFG_NC_SWITCH(nc, QFG_P2)
 #undef QFG_P2
       QFG_LAUNCHED(ctx);
     } else {
       QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, job.fstart, ps.np1, job.fstart + ps.np1));
 #define QFG_P1(N) \
-  launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, job.fstart, job.final_out, job.pa.n, job.vec)
+  launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, job.fstart, job.final_out, ps.col_stride, job.vec)
       QFG_NC_SWITCH(nc, QFG_P1)
 #undef QFG_P1
       QFG_LAUNCHED(ctx);
@@ -1607,7 +1728,7 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
   int64_t words = 0;
   int max_ncols = 1;
   for (auto& g : plan.groups) {
-    words += (int64_t)g.cols.size() * nb + (2 << bits) + 1;
+    words += (int64_t)g.cols.size() * (nb + 4) + (2 << bits) + 1;
     max_ncols = std::max(max_ncols, (int)g.cols.size());
   }
   if (two_pass) words += (int64_t)max_ncols * (nb + 4 + 4 * np1) + 64;
