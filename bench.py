@@ -258,9 +258,9 @@ def run_gb300(args):
     traffic = eng.step_traffic(b, w.literals)
     tune = None
     if not args.eval_bits:
-        bits, tms = eng.autotune_step(b, w.literals)
+        bits, cbits, tms = eng.autotune_step(b, w.literals)
         eng.set_option(C.QFG_OPT_AUTOTUNE, 1)
-        tune = {"partition_bits": bits, "ms_per_step": tms}
+        tune = {"partition_bits": bits, "pass1_bits": cbits, "ms_per_step": tms}
 
     for _ in range(args.warmup):
         eng.evaluate_step_device(b, lits_c, n, counts.data_ptr())

@@ -62,7 +62,8 @@ enum {
   QFG_OPT_STAGE_TIMING = 5,     /* 1 = time each evaluation stage with CUDA events */
   QFG_OPT_SHARD_INDEX = 6,      /* this context's shard of the partition space (default 0) */
   QFG_OPT_SHARD_COUNT = 7,      /* number of shards (default 1); see qfg_evaluate_step */
-  QFG_OPT_AUTOTUNE = 8          /* 1 = use the partition bits qfg_autotune_step chose per size class */
+  QFG_OPT_AUTOTUNE = 8,         /* 1 = use the partition bits qfg_autotune_step chose per size class */
+  QFG_OPT_PASS1_BITS = 9        /* pass-1 bits of a two-pass partition (0 = automatic, else 1..8) */
 };
 
 /* Evaluation stages timed under QFG_OPT_STAGE_TIMING (the GPU counterpart of
@@ -191,14 +192,17 @@ int qfg_step_scratch_bytes(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t n
 
 /* Autotuner.  No reference counterpart (the reference reads FLAGS_num_radix_bits).
  * Times the batched step over `bindings` at a few partition-bit settings
- * around the automatic choice -- the bits fix the partition pass count
- * (one pass up to 8 bits, two above) and the rows per shared-memory table --
- * and records the fastest for the binding set's size class (floor(log2(rows))).
- * Under QFG_OPT_AUTOTUNE = 1 every batched step of that size class uses the
- * recorded bits (QFG_OPT_EVAL_BITS > 0 still overrides).  Counts do not depend
- * on the bits.  Returns the chosen bits and their time per step. */
+ * around the automatic choice -- the bits fix the partition pass count (one
+ * pass up to 8 bits, two above) and the rows per shared-memory table -- and,
+ * with two passes, both splits of the bits between the passes (7 or 8
+ * pass-1 bits); records the fastest for the binding set's size class
+ * (floor(log2(rows))).  Under QFG_OPT_AUTOTUNE = 1 every batched step of that
+ * size class uses the recorded setting (QFG_OPT_EVAL_BITS > 0 still
+ * overrides).  Counts do not depend on it.  Returns the chosen partition
+ * bits, pass-1 bits (0 = one pass) and time per step. */
 int qfg_autotune_step(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
-                      const qfg_literal* literals, int32_t* best_bits, double* best_ms);
+                      const qfg_literal* literals, int32_t* best_bits, int32_t* best_pass1_bits,
+                      double* best_ms);
 
 /* ---- batched steps replayed from CUDA graphs ---------------------------- */
 /* No reference counterpart.  Captures the batched evaluation of `literals`

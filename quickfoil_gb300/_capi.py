@@ -38,6 +38,7 @@ QFG_OPT_STAGE_TIMING = 5
 QFG_OPT_SHARD_INDEX = 6
 QFG_OPT_SHARD_COUNT = 7
 QFG_OPT_AUTOTUNE = 8
+QFG_OPT_PASS1_BITS = 9
 
 STAGES = ("key_tables", "bind_partition", "evaluate", "per_literal", "unit_plan")
 
@@ -97,7 +98,8 @@ SIGNATURES = [
     ("qfg_step_traffic", ctypes.c_int,
      [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i64p]),
     ("qfg_autotune_step", ctypes.c_int,
-     [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i32p, ctypes.POINTER(ctypes.c_double)]),
+     [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i32p, c_i32p,
+      ctypes.POINTER(ctypes.c_double)]),
     ("qfg_step_scratch_bytes", ctypes.c_int,
      [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i64p]),
     ("qfg_step_graph_create", ctypes.c_int,

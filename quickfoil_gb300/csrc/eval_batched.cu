@@ -47,10 +47,13 @@ constexpr int kMaxLitsPerLaunch = 512;
 constexpr int kChunk = 2 * kEvalThreads;     // relation entries per work unit: two per thread
 constexpr int kMaxGroupLits = kEvalThreads;  // one thread per literal in the per-item prefix
 constexpr int kPartThreads = 1024;
-constexpr int kMaxCoarseBits = 7;      // pass 1 fan-out: 2 << 7 = 256 bins
+constexpr int kDefaultCoarseBits = 7;  // pass 1 fan-out: 2 << 7 = 256 bins (hash prefix, label)
+constexpr int kMaxCoarseBits = 8;      // at most 512 pass-1 bins
 constexpr int kMaxSubBits = 9;         // pass 2 fan-out: up to 512 sub-bins
-constexpr int kMaxPartitionBits = kMaxCoarseBits + kMaxSubBits;
+constexpr int kMaxSinglePassBits = 8;  // one pass up to 2 << 8 = 512 bins
+constexpr int kMaxPartitionBits = 16;
 static_assert(kMaxPartitionBits <= kRelPartitionBits, "relation bins must refine binding bins");
+static_assert(kMaxPartitionBits <= kMaxCoarseBits + kMaxSubBits, "two passes reach every bit count");
 static_assert(kSlots % kEvalThreads == 0 && kSlots > kTile, "slot table shape");
 
 // ----------------------------------------------------------------------------
@@ -999,20 +1002,38 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     const bool has_atoms = (U.flags & 0x100u) != 0u;
     const uint32_t total = U.Pp + U.Np;
 
-    // This thread's two entry records (a pair of consecutive records).
-    const uint32_t j0 = 2u * threadIdx.x;
+    // This thread's entry records.  More entries than threads: a pair of
+    // consecutive records per thread.  At most half as many: `tpe` (2 to
+    // 8) neighbouring threads share one entry and split its row checks
+    // (thread `sub` takes rows sub, sub + tpe, ...).  Otherwise one each.
+    uint32_t tpe = 1, sub = 0;
+    const bool pairs = U.ecnt > (uint32_t)kEvalThreads;
+    if (!pairs && 2u * U.ecnt <= (uint32_t)kEvalThreads) {
+      const uint32_t q = (uint32_t)kEvalThreads / (U.ecnt > 0u ? U.ecnt : 1u);
+      tpe = q >= 8u ? 8u : q >= 4u ? 4u : 2u;
+      sub = threadIdx.x & (tpe - 1u);
+    }
+    const uint32_t j0 = pairs ? 2u * threadIdx.x : threadIdx.x / tpe;
     const bool have = j0 < U.ecnt && U.eoff + U.ecnt <= a.entry_cap;
     int2 e_k0 = make_int2(0, 0), e_kA = e_k0, e_kB = e_k0, e_mult = e_k0;
     uint2 e_meta = make_uint2(0u, 0u);
     if (have) {
-      const uint32_t r = U.eoff + j0;  // even, and the block is padded to a multiple of 4
-      e_k0 = __ldg(reinterpret_cast<const int2*>(a.rec.k0 + r));
-      e_kA = __ldg(reinterpret_cast<const int2*>(a.rec.kA + r));
-      e_kB = __ldg(reinterpret_cast<const int2*>(a.rec.kB + r));
-      e_mult = __ldg(reinterpret_cast<const int2*>(a.rec.mult + r));
-      e_meta = __ldg(reinterpret_cast<const uint2*>(a.rec.meta + r));
+      const uint32_t r = U.eoff + j0;  // pairs: even, and the block is padded to a multiple of 4
+      if (pairs) {
+        e_k0 = __ldg(reinterpret_cast<const int2*>(a.rec.k0 + r));
+        e_kA = __ldg(reinterpret_cast<const int2*>(a.rec.kA + r));
+        e_kB = __ldg(reinterpret_cast<const int2*>(a.rec.kB + r));
+        e_mult = __ldg(reinterpret_cast<const int2*>(a.rec.mult + r));
+        e_meta = __ldg(reinterpret_cast<const uint2*>(a.rec.meta + r));
+      } else {
+        e_k0.x = __ldg(a.rec.k0 + r);
+        e_kA.x = __ldg(a.rec.kA + r);
+        e_kB.x = __ldg(a.rec.kB + r);
+        e_mult.x = __ldg(a.rec.mult + r);
+        e_meta.x = __ldg(a.rec.meta + r);
+      }
     }
-    const bool have1 = have && j0 + 1 < U.ecnt;
+    const bool have1 = pairs && have && j0 + 1 < U.ecnt;
 
     long long bp = 0, bn = 0, cp = 0, cn = 0;
     int Lrun = -1;
@@ -1153,24 +1174,27 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         const uint32_t nchk = (meta >> 8) & 3u;
         uint32_t hp = 0, hn = 0;
         if (nchk == 0) {
-          hp = P;
-          hn = N;
+          if (sub == 0u) {
+            hp = P;
+            hn = N;
+          }
         } else {
           const uint32_t beg = sstart[slot], mid = beg + P, end = mid + N;
           const int32_t kA = j == 0 ? e_kA.x : e_kA.y;
           if (nchk == 1) {
             const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
-            for (uint32_t x = beg; x < mid; ++x) hp += ca[rows[x]] == kA;
-            for (uint32_t x = mid; x < end; ++x) hn += ca[rows[x]] == kA;
+            for (uint32_t x = beg + sub; x < mid; x += tpe) hp += ca[rows[x]] == kA;
+            for (uint32_t x = mid + sub; x < end; x += tpe)
+              hn += ca[rows[x]] == kA;
           } else if (nchk == 2) {
             const int32_t kB = j == 0 ? e_kB.x : e_kB.y;
             const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
             const int32_t* cb = raw + ((meta >> 16) & 7u) * kTileStride;
-            for (uint32_t x = beg; x < mid; ++x) {
+            for (uint32_t x = beg + sub; x < mid; x += tpe) {
               const int r = rows[x];
               hp += (ca[r] == kA) & (cb[r] == kB);
             }
-            for (uint32_t x = mid; x < end; ++x) {
+            for (uint32_t x = mid + sub; x < end; x += tpe) {
               const int r = rows[x];
               hn += (ca[r] == kA) & (cb[r] == kB);
             }
@@ -1178,7 +1202,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
             // More than two checked columns: keys from the key table.
             const LitDesc& d = a.lits[lit_begin + L];
             const uint32_t e = (uint32_t)kA;
-            for (uint32_t x = beg; x < end; ++x) {
+            for (uint32_t x = beg + sub; x < end; x += tpe) {
               const int r = rows[x];
               bool pass = true;
               for (int q = 1; q < d.nk && pass; ++q) {
@@ -1238,11 +1262,26 @@ int auto_group_bits(Ctx* ctx, int64_t n) {
   if (ctx->eval_bits > 0) return std::min(ctx->eval_bits, kMaxPartitionBits);
   if (ctx->autotune) {
     auto it = ctx->tuned_bits.find(size_class(n));
-    if (it != ctx->tuned_bits.end()) return it->second;
+    if (it != ctx->tuned_bits.end()) return it->second.first;
   }
   int bits = 1;
   while (bits < kMaxPartitionBits && (n >> bits) > kTargetRows) ++bits;
   return bits;
+}
+
+// Pass-1 bits of a two-pass partition into `bits` bits: an override, the
+// autotuned choice of the size class, or the default; always leaving pass 2
+// at most kMaxSubBits.
+int coarse_bits(Ctx* ctx, int64_t n, int bits) {
+  int cb = kDefaultCoarseBits;
+  if (ctx->eval_cbits > 0) {
+    cb = ctx->eval_cbits;
+  } else if (ctx->autotune && ctx->eval_bits == 0) {
+    auto it = ctx->tuned_bits.find(size_class(n));
+    if (it != ctx->tuned_bits.end() && it->second.first == bits) cb = it->second.second;
+  }
+  cb = std::min(std::max(cb, bits - kMaxSubBits), std::min(kMaxCoarseBits, bits - 1));
+  return std::max(cb, 1);
 }
 
 struct HostGroup {
@@ -1442,8 +1481,8 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   const uint32_t shard_lo = (uint32_t)(((int64_t)ctx->shard_index << bits) / ctx->shard_count);
   const uint32_t shard_hi = (uint32_t)(((int64_t)(ctx->shard_index + 1) << bits) / ctx->shard_count);
   ps->bits = bits;
-  ps->two_pass = bits > kMaxCoarseBits + 1;
-  ps->cbits = ps->two_pass ? kMaxCoarseBits : bits;
+  ps->two_pass = bits > kMaxSinglePassBits;
+  ps->cbits = ps->two_pass ? coarse_bits(ctx, nb, bits) : bits;
   ps->sbits = bits - ps->cbits;
   const int nfine = 2 << bits;
   ps->np1 = 2 << ps->cbits;
@@ -1723,8 +1762,9 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
   StepPlan plan;
   QFG_TRY(plan_step(ctx, n, lits, &plan));
   const int bits = auto_group_bits(ctx, nb);
-  const bool two_pass = bits > kMaxCoarseBits + 1;
-  const int np1 = 2 << (two_pass ? kMaxCoarseBits : bits);
+  const bool two_pass = bits > kMaxSinglePassBits;
+  const int cb = two_pass ? coarse_bits(ctx, nb, bits) : bits;
+  const int np1 = 2 << cb;
   int64_t words = 0;
   int max_ncols = 1;
   for (auto& g : plan.groups) {
@@ -1733,7 +1773,7 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
   }
   if (two_pass) words += (int64_t)max_ncols * (nb + 4 + 4 * np1) + 64;
   words += (int64_t)np1 * (ctx->num_sms * 2 + 5);
-  if (two_pass) words += (nb / kP2Chunk + np1 + 1) << (bits - kMaxCoarseBits);
+  if (two_pass) words += (nb / kP2Chunk + np1 + 1) << (bits - cb);
   int64_t units = (int64_t)plan.groups.size() << bits;
   int64_t entries = 0;
   for (KeyTable* kt : plan.tables) {
@@ -1775,12 +1815,13 @@ extern "C" int qfg_evaluate_step(qfg_ctx* c, const qfg_bindings* b, int32_t n,
 }
 
 extern "C" int qfg_autotune_step(qfg_ctx* c, const qfg_bindings* b, int32_t n,
-                                 const qfg_literal* lits, int32_t* best_bits, double* best_ms) {
+                                 const qfg_literal* lits, int32_t* best_bits, int32_t* best_pass1_bits,
+                                 double* best_ms) {
   if (c == nullptr || b == nullptr) return QFG_ERR_INVALID;
   Ctx* ctx = &c->impl;
   QFG_TRY(validate_literals(ctx, b, n, lits));
   const int64_t nb = b->num_positive + b->num_negative;
-  const int saved_bits = ctx->eval_bits;
+  const int saved_bits = ctx->eval_bits, saved_cbits = ctx->eval_cbits;
   const bool saved_tune = ctx->autotune, saved_timing = ctx->stage_timing;
   ctx->eval_bits = 0;
   ctx->autotune = false;
@@ -1791,40 +1832,50 @@ extern "C" int qfg_autotune_step(qfg_ctx* c, const qfg_bindings* b, int32_t n,
   int st = QFG_OK;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     st = cuda_error(ctx, cudaGetLastError(), "cudaEventCreate");
-  int best = base;
+  int best = base, best_cb = 0;
   float best_t = -1.0f;
   ctx->stage_timing = false;
   for (int cand = std::max(1, base - 2); st == QFG_OK && cand <= std::min(kMaxPartitionBits, base + 1);
        ++cand) {
-    ctx->eval_bits = cand;
-    st = evaluate_batched(ctx, b, n, lits, dev);  // sizes the scratch of this setting
-    if (st != QFG_OK) break;
-    if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) {
-      st = cuda_error(ctx, cudaGetLastError(), "cudaEventRecord");
-      break;
-    }
-    for (int rep = 0; rep < 2 && st == QFG_OK; ++rep) st = evaluate_batched(ctx, b, n, lits, dev);
-    if (st != QFG_OK) break;
-    float ms = 0.0f;
-    if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
-      st = cuda_error(ctx, cudaGetLastError(), "timing");
-      break;
-    }
-    ms *= 0.5f;
-    if (best_t < 0.0f || ms < best_t) {
-      best_t = ms;
-      best = cand;
+    // Two passes: try both pass-1 widths (how the bits split between passes).
+    const int cb_lo = cand > kMaxSinglePassBits ? kDefaultCoarseBits : 0;
+    const int cb_hi = cand > kMaxSinglePassBits ? kMaxCoarseBits : 0;
+    for (int cb = cb_lo; st == QFG_OK && cb <= cb_hi; ++cb) {
+      if (cb > 0 && cand - cb > kMaxSubBits) continue;
+      ctx->eval_bits = cand;
+      ctx->eval_cbits = cb;
+      st = evaluate_batched(ctx, b, n, lits, dev);  // sizes the scratch of this setting
+      if (st != QFG_OK) break;
+      if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) {
+        st = cuda_error(ctx, cudaGetLastError(), "cudaEventRecord");
+        break;
+      }
+      for (int rep = 0; rep < 2 && st == QFG_OK; ++rep) st = evaluate_batched(ctx, b, n, lits, dev);
+      if (st != QFG_OK) break;
+      float ms = 0.0f;
+      if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        st = cuda_error(ctx, cudaGetLastError(), "timing");
+        break;
+      }
+      ms *= 0.5f;
+      if (best_t < 0.0f || ms < best_t) {
+        best_t = ms;
+        best = cand;
+        best_cb = cb;
+      }
     }
   }
+  ctx->eval_cbits = saved_cbits;
   if (e0 != nullptr) cudaEventDestroy(e0);
   if (e1 != nullptr) cudaEventDestroy(e1);
   ctx->eval_bits = saved_bits;
   ctx->autotune = saved_tune;
   ctx->stage_timing = saved_timing;
   if (st != QFG_OK) return st;
-  ctx->tuned_bits[size_class(nb)] = best;
+  ctx->tuned_bits[size_class(nb)] = std::make_pair(best, best_cb);
   if (best_bits != nullptr) *best_bits = best;
+  if (best_pass1_bits != nullptr) *best_pass1_bits = best_cb;
   if (best_ms != nullptr) *best_ms = best_t;
   return QFG_OK;
 }

@@ -148,9 +148,11 @@ struct Ctx {
   int use_graphs = 0;
   // QFG_OPT_USE_GRAPHS: captured steps by key (see step_runtime.cu).
   std::map<std::string, qfg_step_graph*> graph_cache;
-  // QFG_OPT_AUTOTUNE: partition bits chosen per binding-size class.
+  // QFG_OPT_AUTOTUNE: partition bits and pass-1 bits chosen per
+  // binding-size class; eval_cbits fixes the pass-1 bits (0 = automatic).
   bool autotune = false;
-  std::map<int, int> tuned_bits;
+  std::map<int, std::pair<int, int>> tuned_bits;
+  int eval_cbits = 0;
   int shard_index = 0;
   int shard_count = 1;
   int64_t launches = 0;

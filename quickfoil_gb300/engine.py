@@ -281,15 +281,16 @@ class Engine:
                 self.ctx, "qfg_evaluate_step")
 
     def autotune_step(self, bindings: BindingSet, literals: Sequence[Literal]):
-        """Times the batched step at a few partition-bit settings and records
-        the fastest for the binding set's size class; returns (bits, ms).
-        Used by later steps under QFG_OPT_AUTOTUNE = 1."""
+        """Times the batched step at a few partition settings and records the
+        fastest for the binding set's size class; returns (partition bits,
+        pass-1 bits (0 = one pass), ms).  Used by later steps under
+        QFG_OPT_AUTOTUNE = 1."""
         lits = (C.QfgLiteral * max(1, len(literals)))(*[l.to_c() for l in literals])
-        bits, ms = ctypes.c_int32(), ctypes.c_double()
+        bits, cbits, ms = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_double()
         C.check(self.lib.qfg_autotune_step(self.ctx, bindings.handle, len(literals), lits,
-                                           ctypes.byref(bits), ctypes.byref(ms)),
+                                           ctypes.byref(bits), ctypes.byref(cbits), ctypes.byref(ms)),
                 self.ctx, "qfg_autotune_step")
-        return bits.value, ms.value
+        return bits.value, cbits.value, ms.value
 
     def step_scratch_bytes(self, bindings: BindingSet, literals: Sequence[Literal]) -> int:
         """Device scratch a batched step of these literals needs."""

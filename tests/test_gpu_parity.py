@@ -208,3 +208,23 @@ def test_evaluate_partition_bits_do_not_change_counts(engine, bits):
         np.testing.assert_array_equal(engine.evaluate_step(b, lits), want)
     finally:
         engine.set_option(C.QFG_OPT_EVAL_BITS, 0)
+
+
+@pytest.mark.parametrize("bits,pass1", [(12, 3), (12, 8), (14, 5), (14, 8), (16, 7), (16, 8)])
+def test_evaluate_pass_split_does_not_change_counts(engine, bits, pass1):
+    """The same partition bits split differently between the two passes
+    (pass-1 bits; pass 2 takes the rest): identical counts."""
+    from quickfoil_gb300 import _capi as C
+    w = workloads.batched_step(n_bindings=300_000, num_relations=8, min_tuples=50,
+                               max_tuples=200_000, num_literals=48, domain=20_000, seed=22)
+    base = fresh_ids(len(w.relations))
+    lits = _register(engine, w, base)
+    b = engine.bindings(w.binding_columns, w.num_positive)
+    want = brute_counts([None] * base + w.relations, w.binding_columns, w.num_positive, lits)
+    try:
+        engine.set_option(C.QFG_OPT_EVAL_BITS, bits)
+        engine.set_option(C.QFG_OPT_PASS1_BITS, pass1)
+        np.testing.assert_array_equal(engine.evaluate_step(b, lits), want)
+    finally:
+        engine.set_option(C.QFG_OPT_EVAL_BITS, 0)
+        engine.set_option(C.QFG_OPT_PASS1_BITS, 0)

@@ -176,8 +176,9 @@ def test_autotuner_picks_bits_and_keeps_counts(engine):
     lits = _register(engine, w)
     b = engine.bindings(_dev_columns(w.binding_columns), w.num_positive)
     want = engine.evaluate_step(b, lits)
-    bits, ms = engine.autotune_step(b, lits)
+    bits, cbits, ms = engine.autotune_step(b, lits)
     assert 1 <= bits <= 16 and ms > 0
+    assert cbits == 0 if bits <= 8 else 7 <= cbits <= 8
     engine.set_option(QFG_OPT_AUTOTUNE, 1)
     try:
         np.testing.assert_array_equal(engine.evaluate_step(b, lits), want)
