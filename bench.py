@@ -150,6 +150,20 @@ def profiled_traffic(args):
     return None
 
 
+def host_cpu():
+    """The host CPU's model name and logical core count (lscpu)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() == "Model name" and model is None:
+                model = v.strip()
+    except Exception:
+        pass
+    return {"model": model, "logical_cores": os.cpu_count()}
+
+
 def measured_peak_hbm():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -167,11 +181,12 @@ def cpu_baseline(w, nthreads: int, sample: int, budget_s: float = 12.0):
     lits = [l.as_tuple() for l in w.literals]
     if sample <= 0:
         # grow the sample until the run takes a few seconds, within the budget
-        sample = 2
+        sample = min(2, len(lits))
         t0 = time.perf_counter()
         o.evaluate(w.binding_columns, w.num_positive, lits[:sample], 5, nthreads)
         dt = time.perf_counter() - t0
-        sample = int(max(2, min(len(lits), sample * budget_s / max(dt, 1e-3) / 2)))
+        sample = int(max(1, min(len(lits), sample * budget_s / max(dt, 1e-3) / 2)))
+    sample = max(1, min(sample, len(lits)))
     o.evaluate(w.binding_columns, w.num_positive, lits[:sample], 5, nthreads)  # warm relation cache
     t0 = time.perf_counter()
     o.evaluate(w.binding_columns, w.num_positive, lits[:sample], 5, nthreads)
@@ -205,7 +220,7 @@ def run_reference(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64",
             "data": "synthetic (seeded)", "config": workload_config(args, w),
             "cpu_baseline": {"value": value, "unit": "literals/s", "cores": threads,
-                             "kind": "port",
+                             "kind": "port", "host": host_cpu(),
                              "sample": f"first {sample} of {len(lits)} literals of the step, "
                                        "oracle (C restatement of the reference operator chain), "
                                        f"{threads} threads"},
@@ -442,6 +457,7 @@ def run_gb300(args):
             sample = args.cpu_sample
             v, dt, s = cpu_baseline(w, 1, sample)
             line["cpu_baseline"] = {"value": v, "unit": "literals/s", "cores": 1, "kind": "port",
+                                    "host": host_cpu(),
                                     "sample": f"first {s} of {n} literals of the step "
                                               f"({dt:.1f} s), oracle = C restatement of the "
                                               "reference operator chain, 1 thread like the "
