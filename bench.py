@@ -59,6 +59,7 @@ def parse_args():
     ap.add_argument("--eval-bits", type=int, default=0,
                     help="binding partition bits of the batched engine (0 = autotuned)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop leg")
+    ap.add_argument("--no-coverage", action="store_true", help="skip the coverage leg")
     return ap.parse_args()
 
 
@@ -399,6 +400,9 @@ def run_gb300(args):
     serving = None
     if not args.no_serving and args.workload == "batched_step":
         serving = run_serving(eng, w, dev, torch)
+    coverage = None
+    if args.workload == "batched_step" and not args.no_coverage and rank == 0:
+        coverage = run_coverage(eng, w, b, dev, torch, measured_peak_hbm()[0], args.no_cpu)
 
     if rank == 0:
         peak, peak_kind = measured_peak_hbm()
@@ -448,6 +452,8 @@ def run_gb300(args):
         }
         if serving is not None:
             line["serving"] = serving
+        if coverage is not None:
+            line["coverage"] = coverage
         if per_lit is not None:
             line["per_literal"] = per_lit
             line["batched_over_per_literal"] = line["value"] / (per_lit["value"] * world)
@@ -525,6 +531,91 @@ def run_serving(eng, w, dev, torch, n_requests: int = 64, lits_per_request: int 
                         "offered_load": 0.8, "p50_ms": st_p["p50_ms"], "p99_ms": st_p["p99_ms"],
                         "peak_in_flight": st_p["peak_in_flight"]},
             "counts_equal_alone": bool(eq_b and eq_p)}
+
+
+def run_coverage(eng, w, b, dev, torch, peak, no_cpu: bool, n_lits: int = 16, reps: int = 5):
+    """Coverage on acceptance (qfg_coverage) of the step's first n_lits
+    distinct literals appended to the clause whose binding set is the step's
+    (target = binding columns 0-1): 2M uncovered positives (half the target
+    tuples of sampled positive binding rows, half random) and 4M original
+    negatives (likewise from negative rows), covered counts of both and the
+    positives' bit vector; then the compaction of the uncovered positives
+    with the first literal's bits (qfg_compact_rows).  Every call reads its
+    counts back to the host, as the learner does."""
+    import oracle
+    rng = np.random.default_rng(5)
+    B, P, k = w.binding_columns, w.num_positive, 2
+    n = len(B[0])
+    npos, nneg = min(1_000_000, P // 2), min(2_000_000, (n - P) // 2)
+    pos_rows = rng.choice(P, npos, replace=False)
+    neg_rows = P + rng.choice(n - P, nneg, replace=False)
+    U = [np.concatenate([B[q][pos_rows], rng.integers(0, w.domain, npos).astype(np.int32)])
+         for q in range(k)]
+    Ng = [np.concatenate([B[q][neg_rows], rng.integers(0, w.domain, nneg).astype(np.int32)])
+          for q in range(k)]
+    dU = [torch.from_numpy(c).to(dev) for c in U]
+    dN = [torch.from_numpy(c).to(dev) for c in Ng]
+    lits = list(dict.fromkeys(w.literals))[:n_lits]
+    for _ in range(3):
+        for l in lits:
+            eng.coverage(b, l, k, dU, dN)
+    torch.cuda.synchronize()
+    launches0 = eng.kernel_launches()
+    t0 = time.perf_counter()
+    got = []
+    for _ in range(reps):
+        got = [eng.coverage(b, l, k, dU, dN) for l in lits]
+    torch.cuda.synchronize()
+    call_s = (time.perf_counter() - t0) / (reps * len(lits))
+    cov_launches = (eng.kernel_launches() - launches0) / (reps * len(lits))
+    best = max(range(len(got)), key=lambda i: got[i][0][0])  # the literal covering most
+    bits0 = got[best][1]
+    left = eng.compact_rows(dU, bits0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        left = eng.compact_rows(dU, bits0)
+    torch.cuda.synchronize()
+    comp_s = (time.perf_counter() - t0) / reps
+    # algorithmic bytes of one coverage call: every binding row's bound-key
+    # columns, the relation's bound columns, both example tables, the bits
+    def alg_bytes(l):
+        nb = sum(1 for v in l.vars if v >= 0)
+        rel = w.relations[l.relation]
+        return 4 * (n * nb + len(rel[0]) * nb + k * (len(U[0]) + len(Ng[0]))) + len(U[0]) // 8
+    cov_bytes = float(np.mean([alg_bytes(l) for l in lits]))
+    kept = int(left[0].numel())
+    comp_bytes = 4 * k * (len(U[0]) + kept) + len(U[0]) // 8
+    ok = True
+    cpu = None
+    if not no_cpu:
+        t0 = time.perf_counter()
+        m = 0
+        for l, (counts, bits) in zip(lits, got):
+            want = oracle.coverage(B, P, w.relations[l.relation], l.as_tuple(), k, U, Ng)
+            ok &= counts == want[0] and np.array_equal(bits.cpu().numpy().view(np.uint64), want[1])
+            m += 1
+            if time.perf_counter() - t0 > 6.0:
+                break
+        dt = time.perf_counter() - t0
+        cpu = {"value": m / dt, "unit": "coverage calls/s", "cores": 1, "kind": "port",
+               "sample": f"first {m} of {len(lits)} literals, full size ({dt:.1f} s), also the "
+                         "parity check of those calls"}
+    return {"metric": "literal coverage calls/s (covered positives + negatives + bit vector)",
+            "value": 1.0 / call_s, "unit": "coverage calls/s", "ms_per_call": call_s * 1e3,
+            "gpu_launches_per_call": cov_launches,
+            "workload": {"binding_rows": n, "binding_positive": P, "target_columns": k,
+                         "uncovered_positives": len(U[0]), "negatives": len(Ng[0]),
+                         "literals": len(lits), "repeats": reps},
+            "roofline": {"bound": "hbm", "algorithmic_bytes": cov_bytes,
+                         "achieved": cov_bytes / call_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": cov_bytes / call_s / 1e9 / peak,
+                         "note": "wall time per call including the host read of the counts"},
+            "compaction": {"ms": comp_s * 1e3, "rows_in": len(U[0]), "rows_kept": kept,
+                           "algorithmic_bytes": comp_bytes,
+                           "achieved_gbs": comp_bytes / comp_s / 1e9,
+                           "frac": comp_bytes / comp_s / 1e9 / peak},
+            "cpu_baseline": cpu, "counts_equal_oracle": bool(ok) if cpu is not None else None}
 
 
 def main():

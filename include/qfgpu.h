@@ -74,7 +74,9 @@ enum {
   QFG_STAGE_EVALUATE = 2,       /* the persistent build + probe + count kernel */
   QFG_STAGE_PER_LITERAL = 3,    /* plain per-literal join-count kernels */
   QFG_STAGE_UNIT_PLAN = 4,      /* work units and entry records of the batched step */
-  QFG_NUM_STAGES = 5
+  QFG_STAGE_COVERAGE_SCAN = 5,  /* coverage: the pass over the binding rows */
+  QFG_STAGE_COVERAGE_EXAMPLES = 6, /* coverage: example key sets and bit vectors */
+  QFG_NUM_STAGES = 7
 };
 
 typedef struct qfg_ctx qfg_ctx;
@@ -327,6 +329,64 @@ int qfg_right_semijoin(qfg_ctx* ctx, const int32_t* const* d_probe_keys, int64_t
 int qfg_extend_bindings(qfg_ctx* ctx, const qfg_bindings* bindings, const qfg_literal* literal,
                         int64_t num_out_positive, int64_t num_out_negative,
                         qfg_bindings** out);
+
+/* ---- coverage of a literal appended to the building clause ------------- */
+/* QuickFoil::ComputeCoverageOnUncoveredData (learner/QuickFoil.cpp:471-573)
+ * and LiteralSelector::ComputeCoveredPositives (learner/LiteralSelector.cpp:
+ * 150-210).  `bindings` is the building clause's binding set, its first
+ * num_target_columns columns the target's variables (the clause head).
+ * A label side's binding rows whose bound arguments match some tuple of the
+ * literal's relation project onto those columns; an example is covered when
+ * its tuple is among that side's projections.  The examples are the
+ * uncovered positives (num_uncovered_positive rows of num_target_columns
+ * device columns) against the positive side and the original negatives
+ * against the negative side (d_negative NULL with num_negative 0 skips them:
+ * ComputeCoveredPositives).  num_covered[0] / [1] receive the covered
+ * positive / negative counts.  d_positive_bits (may be NULL) receives one bit
+ * per uncovered positive, set when covered, in 64-bit little-endian blocks
+ * (ceil(n/64) of them, bits past the last row zero): the concatenated
+ * SemiJoinChunk bit vectors of the reference (operations/SemiJoin.hpp:25-37).
+ * The reference keys its projection tables by row ids that are relative to
+ * each 32768-row chunk when a label side is split into chunks (a left
+ * semi-join over a side of more than 32768 rows that is not smaller than
+ * the relation, operations/BuildHashTable.cpp:152-189 with
+ * operations/LeftSemiJoin.hpp:55-83); there its counts are not set
+ * membership.  These are set membership for every size, which equals the
+ * reference wherever its row ids are whole-table.  1 <= num_target_columns
+ * <= 8; the literal needs at least one bound argument. */
+int qfg_coverage(qfg_ctx* ctx, const qfg_bindings* bindings, const qfg_literal* literal,
+                 int32_t num_target_columns, const int32_t* const* d_uncovered_positive,
+                 int64_t num_uncovered_positive, const int32_t* const* d_negative,
+                 int64_t num_negative, uint64_t* d_positive_bits, int64_t* num_covered);
+
+/* No counterpart in the reference: an example table prepared once for many
+ * coverage calls -- the original negatives for a whole run, the uncovered
+ * positives for one clause.  num_columns (1..8) device columns of num_rows
+ * rows are borrowed, not copied, and must stay unchanged while the handle
+ * lives; their key set is built here.  Calls that use one handle are
+ * ordered on the context stream. */
+typedef struct qfg_examples qfg_examples;
+int qfg_examples_create(qfg_ctx* ctx, int32_t num_columns, const int32_t* const* d_columns,
+                        int64_t num_rows, qfg_examples** out);
+int qfg_examples_destroy(qfg_ctx* ctx, qfg_examples* examples);
+
+/* qfg_coverage on prepared example tables: the target columns are the
+ * examples' columns (num_columns of uncovered_positive; negative, which may
+ * be NULL, has the same count).  Same results as qfg_coverage. */
+int qfg_coverage_examples(qfg_ctx* ctx, const qfg_bindings* bindings, const qfg_literal* literal,
+                          const qfg_examples* uncovered_positive, const qfg_examples* negative,
+                          uint64_t* d_positive_bits, int64_t* num_covered);
+
+/* The uncovered-example compaction of learner/QuickFoil.cpp:612-708 (and of
+ * QuickFoilTestRunner::ComputeUnCoveredData, learner/QuickFoilTestRunner.cpp:99-116):
+ * the rows of num_columns device columns whose bit in d_bits (the layout of
+ * qfg_coverage's d_positive_bits) is clear (keep_set 0: the still uncovered
+ * examples) or set (keep_set 1), in row order, written to d_out_columns.
+ * *num_out receives the kept row count; more than out_capacity returns
+ * QFG_ERR_INVALID before anything is written. */
+int qfg_compact_rows(qfg_ctx* ctx, int32_t num_columns, const int32_t* const* d_columns,
+                     int64_t num_rows, const uint64_t* d_bits, int32_t keep_set,
+                     int32_t* const* d_out_columns, int64_t out_capacity, int64_t* num_out);
 
 #ifdef __cplusplus
 }

@@ -90,6 +90,13 @@ def lib():
                                           ctypes.POINTER(_Table), ctypes.POINTER(_Literal),
                                           ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(i32p)]
         L.qfo_extend_bindings.restype = ctypes.c_int
+        L.qfo_coverage.argtypes = [ctypes.POINTER(_Table), ctypes.c_int64, ctypes.POINTER(_Table),
+                                   ctypes.POINTER(_Literal), ctypes.c_int, ctypes.POINTER(_Table),
+                                   ctypes.POINTER(_Table), u64p, i64p]
+        L.qfo_coverage.restype = ctypes.c_int
+        L.qfo_compact_rows.argtypes = [ctypes.c_int, ctypes.POINTER(i32p), ctypes.c_int64, u64p,
+                                       ctypes.c_int, ctypes.POINTER(i32p)]
+        L.qfo_compact_rows.restype = ctypes.c_int64
         _lib = L
     return _lib
 
@@ -244,3 +251,42 @@ def extend_bindings(binding_columns, num_positive, relation_columns, literal,
     if rc != 0:
         raise ValueError(f"extension produced row counts different from the given ones ({rc})")
     return [o[:total] for o in outs]
+
+
+def coverage(binding_columns, num_positive, relation_columns, literal, num_target_columns,
+             uncovered_positive, negative=None):
+    """Covered counts of a literal appended to the building clause and the
+    uncovered positives' bits; returns ((covered positives, covered
+    negatives), uint64 bit blocks)."""
+    b = _TableHandle(binding_columns)
+    r = _TableHandle(relation_columns)
+    u = _TableHandle(uncovered_positive)
+    ng = _TableHandle(negative) if negative is not None else None
+    nu = len(u.cols[0]) if u.cols else 0
+    bits = np.zeros(max(1, (nu + 63) // 64), dtype=np.uint64)
+    counts = np.zeros(2, dtype=np.int64)
+    lit = _literal_struct(literal)
+    rc = lib().qfo_coverage(ctypes.byref(b.struct), num_positive, ctypes.byref(r.struct),
+                            ctypes.byref(lit), num_target_columns, ctypes.byref(u.struct),
+                            ctypes.byref(ng.struct) if ng is not None else None,
+                            bits.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                            counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    if rc != 0:
+        raise ValueError(f"invalid literal for a coverage ({rc})")
+    return (int(counts[0]), int(counts[1])), bits[:(nu + 63) // 64]
+
+
+def compact_rows(columns, bits, keep_set=False):
+    """Rows whose bit is clear (set with keep_set), in order."""
+    cols = _as_cols(columns)
+    n = len(cols[0]) if cols else 0
+    outs = [np.zeros(max(1, n), dtype=np.int32) for _ in cols]
+    bits = np.ascontiguousarray(bits, dtype=np.uint64)
+    if len(bits) < (n + 63) // 64:
+        raise ValueError("fewer bit blocks than rows")
+    if len(bits) == 0:
+        bits = np.zeros(1, dtype=np.uint64)
+    m = lib().qfo_compact_rows(len(cols), _colptrs(cols), n,
+                               bits.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                               1 if keep_set else 0, _colptrs(outs))
+    return [o[:m] for o in outs]

@@ -534,3 +534,70 @@ int qfo_extend_bindings(const qfo_table* bindings, int64_t num_positive,
   produced_neg = c.produced;
   return (produced_pos == num_out_positive && produced_neg == num_out_negative) ? 0 : 3;
 }
+
+int qfo_coverage(const qfo_table* bindings, int64_t num_positive, const qfo_table* relation,
+                 const qfo_literal* literal, int num_target_columns,
+                 const qfo_table* uncovered_positive, const qfo_table* negative,
+                 uint64_t* positive_bits, int64_t* num_covered) {
+  const int k = num_target_columns;
+  if (literal->num_args != relation->num_columns || k < 1 || k > QFO_MAX_ARITY ||
+      k > bindings->num_columns)
+    return 1;
+  const int32_t* rel_keys[QFO_MAX_ARITY];
+  int bound_vars[QFO_MAX_ARITY];
+  int nk = 0;
+  for (int a = 0; a < literal->num_args; ++a) {
+    const int v = literal->vars[a];
+    if (v >= bindings->num_columns || v < -1) return 1;
+    if (v < 0) continue;
+    rel_keys[nk] = relation->columns[a];
+    bound_vars[nk++] = v;
+  }
+  if (nk == 0) return 1;
+  num_covered[0] = num_covered[1] = 0;
+  const int64_t nu = uncovered_positive != NULL ? uncovered_positive->num_tuples : 0;
+  if (positive_bits != NULL) memset(positive_bits, 0, sizeof(uint64_t) * (size_t)((nu + 63) / 64));
+  for (int label = 0; label < 2; ++label) {
+    const qfo_table* ex = label == 0 ? uncovered_positive : negative;
+    if (ex == NULL || ex->num_tuples == 0) continue;
+    const int64_t lo = label == 0 ? 0 : num_positive;
+    const int64_t n = label == 0 ? num_positive : bindings->num_tuples - num_positive;
+    /* binding semi-join: the side's rows against the relation (:515-522) */
+    const int32_t* side_keys[QFO_MAX_ARITY];
+    for (int q = 0; q < nk; ++q) side_keys[q] = bindings->columns[bound_vars[q]] + lo;
+    uint64_t* pass = (uint64_t*)calloc((size_t)((n + 63) / 64) + 1, sizeof(uint64_t));
+    const int64_t npass = qfo_left_semijoin(side_keys, n, rel_keys, relation->num_tuples, nk, pass);
+    /* the passing rows' target tuples (:523-526) */
+    int32_t* proj[QFO_MAX_ARITY];
+    for (int q = 0; q < k; ++q) proj[q] = (int32_t*)malloc(sizeof(int32_t) * (size_t)(npass + 1));
+    int64_t m = 0;
+    for (int64_t r = 0; r < n; ++r) {
+      if (!(pass[r >> 6] >> (r & 63) & 1)) continue;
+      for (int q = 0; q < k; ++q) proj[q][m] = bindings->columns[q][lo + r];
+      ++m;
+    }
+    /* coverage semi-join: the examples against the projections (:528-541) */
+    uint64_t* bits = label == 0 && positive_bits != NULL
+                         ? positive_bits
+                         : (uint64_t*)calloc((size_t)((ex->num_tuples + 63) / 64) + 1,
+                                             sizeof(uint64_t));
+    num_covered[label] = qfo_left_semijoin(ex->columns, ex->num_tuples,
+                                           (const int32_t* const*)proj, m, k, bits);
+    if (bits != positive_bits) free(bits);
+    for (int q = 0; q < k; ++q) free(proj[q]);
+    free(pass);
+  }
+  return 0;
+}
+
+int64_t qfo_compact_rows(int num_columns, const int32_t* const* columns, int64_t n,
+                         const uint64_t* bits, int keep_set, int32_t* const* out) {
+  int64_t m = 0;
+  for (int64_t r = 0; r < n; ++r) {
+    const int set = (int)(bits[r >> 6] >> (r & 63) & 1);
+    if (set != (keep_set != 0)) continue;
+    for (int c = 0; c < num_columns; ++c) out[c][m] = columns[c][r];
+    ++m;
+  }
+  return m;
+}

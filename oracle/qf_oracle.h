@@ -123,6 +123,30 @@ int qfo_extend_bindings(const qfo_table* bindings, int64_t num_positive,
                         int64_t num_out_positive, int64_t num_out_negative,
                         int32_t* const* out_columns);
 
+/* QuickFoil::ComputeCoverageOnUncoveredData (learner/QuickFoil.cpp:471-573):
+ * per label side, the binding rows that pass the left semi-join with the
+ * relation on the literal's bound arguments (:494-522) project onto the
+ * first num_target_columns binding columns (:504-509); an example is covered
+ * when a projection equals it on all of them (:523-541 positives against
+ * uncovered_positive, :544-572 negatives against `negative`, which may be
+ * NULL).  Restated as set membership, the reference's result wherever its
+ * projection table holds whole-table row ids (a label side of at most 32768
+ * rows, or one smaller than the relation; operations/BuildHashTable.cpp:
+ * 152-189).  positive_bits (may be NULL) receives a bit per uncovered
+ * positive (ceil(n/64) blocks).  num_covered[0..1]: covered positives,
+ * covered negatives.  Returns 0, or nonzero for an invalid literal. */
+int qfo_coverage(const qfo_table* bindings, int64_t num_positive, const qfo_table* relation,
+                 const qfo_literal* literal, int num_target_columns,
+                 const qfo_table* uncovered_positive, const qfo_table* negative,
+                 uint64_t* positive_bits, int64_t* num_covered);
+
+/* The compaction of learner/QuickFoil.cpp:655-679 (bit vector flipped, then
+ * AttributeReference::EvaluateWithFilter per column): rows whose bit is clear
+ * (keep_set 0) or set (keep_set 1), in order, into out[c].  Returns the kept
+ * row count. */
+int64_t qfo_compact_rows(int num_columns, const int32_t* const* columns, int64_t n,
+                         const uint64_t* bits, int keep_set, int32_t* const* out);
+
 #ifdef __cplusplus
 }
 #endif

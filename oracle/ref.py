@@ -41,6 +41,13 @@ def lib():
                                   ctypes.c_int64, ctypes.POINTER(i32p), ctypes.c_int,
                                   ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
         L.qfref_learn.restype = ctypes.c_int
+        L.qfref_coverage.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), i64p,
+                                     ctypes.POINTER(i32p), ctypes.c_int, ctypes.c_int64,
+                                     ctypes.c_int64, ctypes.POINTER(i32p), ctypes.c_int,
+                                     ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(i32p), i32p,
+                                     ctypes.c_int64, ctypes.POINTER(i32p), i64p,
+                                     ctypes.POINTER(ctypes.c_uint8)]
+        L.qfref_coverage.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -95,3 +102,36 @@ def learn(relations, target_columns, num_positive: int, max_clause_length: int,
     if rc != 0:
         raise RuntimeError(f"reference learner failed ({rc})")
     return [l for l in out.value.decode().splitlines() if l]
+
+
+def coverage(relations, target_columns, target_num_positive: int, binding_columns,
+             bind_num_positive: int, literal, uncovered_columns):
+    """QuickFoil::ComputeCoverageOnUncoveredData (learner/QuickFoil.cpp:471-573)
+    for `literal` appended to a building clause whose binding set is
+    `binding_columns` (first bind_num_positive rows positive, the first
+    len(target_columns) columns the target's variables).  The target's
+    negatives (rows from target_num_positive on) are the original negative
+    data.  Returns ((covered positives, covered negatives), uint8 flag per
+    uncovered positive row)."""
+    keep_r, rptr, rnc, rnt = _relations(relations)
+    keep_t, tptr = _cols(target_columns)
+    keep_b, bptr = _cols(binding_columns)
+    keep_u, uptr = _cols(uncovered_columns)
+    rel, vars_, _ = literal.as_tuple() if hasattr(literal, "as_tuple") else literal
+    desc = np.full(10, -1, dtype=np.int32)
+    desc[0] = rel
+    desc[1] = len(vars_)
+    desc[2:2 + len(vars_)] = vars_
+    nb = len(keep_b[0])
+    nu = len(keep_u[0])
+    counts = np.zeros(2, dtype=np.int64)
+    covered = np.zeros(max(1, nu), dtype=np.uint8)
+    rc = lib().qfref_coverage(len(relations), rnc, rnt, rptr, len(keep_t), len(keep_t[0]),
+                              target_num_positive, tptr, len(keep_b), bind_num_positive,
+                              nb - bind_num_positive, bptr,
+                              desc.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), nu, uptr,
+                              counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                              covered.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    if rc != 0:
+        raise ValueError(f"reference driver rejected the input ({rc})")
+    return (int(counts[0]), int(counts[1])), covered[:nu].astype(bool)

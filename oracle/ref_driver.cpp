@@ -12,6 +12,11 @@
 //                 through link-time wrappers of Evaluate and
 //                 CreateLabelAwareBindingTables, writes every call's inputs
 //                 and outputs to a trace file.
+// qfref_coverage  runs QuickFoil::ComputeCoverageOnUncoveredData
+//                 (learner/QuickFoil.cpp:471-573) on a given building clause
+//                 (binding set) and uncovered positives: the covered counts
+//                 and which uncovered positives are covered.  The method is
+//                 private; only this driver's view of the class opens it.
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -23,7 +28,13 @@
 
 #include "learner/CandidateLiteralEvaluator.hpp"
 #include "learner/CandidateLiteralInfo.hpp"
+#include "learner/LiteralSelector.hpp"
+#include "learner/QuickFoilState.hpp"
+#include "operations/SemiJoin.hpp"
+#include "storage/FoilHashTable.hpp"
+#define private public
 #include "learner/QuickFoil.hpp"
+#undef private
 #include "memory/Buffer.hpp"
 #include "operations/MultiColumnHashJoin.hpp"
 #include "schema/FoilClause.hpp"
@@ -276,6 +287,60 @@ int qfref_learn(int nrel, const int* rel_ncols, const int64_t* rel_ntuples,
   if (clauses != nullptr && clauses_cap > 0) {
     strncpy(clauses, out.c_str(), (size_t)clauses_cap - 1);
     clauses[clauses_cap - 1] = '\0';
+  }
+  return 0;
+}
+
+// The reference's coverage computation for one literal appended to a
+// building clause: binding set (bind_npos positives then bind_nneg
+// negatives, bind_ncols columns, the first target_ncols of them the target's
+// variables), the uncovered positives (unc_n rows of target_ncols columns),
+// and the target (positives first; its negatives are the reference's
+// original negative data).  Writes covered positive / negative counts and,
+// per uncovered positive, 1 when covered.
+int qfref_coverage(int nrel, const int* rel_ncols, const int64_t* rel_ntuples,
+                   const int32_t* const* rel_cols, int target_ncols, int64_t target_n,
+                   int64_t target_npos, const int32_t* const* target_cols, int bind_ncols,
+                   int64_t bind_npos, int64_t bind_nneg, const int32_t* const* bind_cols,
+                   const int32_t* lit, int64_t unc_n, const int32_t* const* unc_cols,
+                   int64_t* counts, uint8_t* covered) {
+  std::vector<std::unique_ptr<FoilPredicate>> owned;
+  Vector<const FoilPredicate*> background;
+  int off = 0;
+  for (int r = 0; r < nrel; ++r) {
+    Vector<int> types(rel_ncols[r], 0);
+    owned.emplace_back(new FoilPredicate(r, "r" + std::to_string(r), -1, types,
+                                         MakeColumns(rel_ncols[r], rel_cols + off, rel_ntuples[r])));
+    background.push_back(owned.back().get());
+    off += rel_ncols[r];
+  }
+  if (lit[0] < 0 || lit[0] >= nrel || lit[1] != rel_ncols[lit[0]]) return 1;
+  Vector<int> ttypes(target_ncols, 0);
+  FoilPredicate target(nrel, "target", -1, ttypes, MakeColumns(target_ncols, target_cols, target_n));
+  QuickFoil qf((size_type)target_npos, (size_type)(target_n - target_npos), &target, background);
+  FoilLiteral head(&target);
+  for (int c = 0; c < target_ncols; ++c) head.AddVariable(FoilVariable(c, 0));
+  qf.building_state_->building_clause = FoilClause::Create(
+      head, (size_type)bind_npos, (size_type)bind_nneg,
+      MakeColumns(bind_ncols, bind_cols, bind_npos + bind_nneg));
+  Vector<ConstBufferPtr> unc = MakeColumns(target_ncols, unc_cols, unc_n);
+  qf.building_state_->uncovered_positive_data = std::make_shared<TableView>(std::move(unc));
+  Vector<FoilVariable> vars;
+  for (int i = 0; i < lit[1]; ++i) vars.emplace_back(lit[2 + i] >= 0 ? FoilVariable(lit[2 + i], 0) : FoilVariable(0));
+  FoilLiteral literal(owned[lit[0]].get(), vars);
+  std::unique_ptr<FoilHashTable> table;
+  size_type npos = 0, nneg = 0;
+  Vector<SemiJoinChunk*> chunks;
+  qf.ComputeCoverageOnUncoveredData(literal, &table, &npos, &nneg, &chunks);
+  counts[0] = npos;
+  counts[1] = nneg;
+  memset(covered, 0, (size_t)unc_n);
+  const int32_t* base = qf.building_state_->uncovered_positive_data->column_at(0)->as_type<int32_t>();
+  for (SemiJoinChunk* c : chunks) {
+    const int64_t first = c->output_columns[0] - base;
+    for (size_t i = 0; i < c->semi_bitvector.size(); ++i)
+      if (c->semi_bitvector.test(i)) covered[first + (int64_t)i] = 1;
+    delete c;
   }
   return 0;
 }

@@ -40,7 +40,8 @@ QFG_OPT_SHARD_COUNT = 7
 QFG_OPT_AUTOTUNE = 8
 QFG_OPT_PASS1_BITS = 9
 
-STAGES = ("key_tables", "bind_partition", "evaluate", "per_literal", "unit_plan")
+STAGES = ("key_tables", "bind_partition", "evaluate", "per_literal", "unit_plan",
+          "coverage_scan", "coverage_examples")
 
 
 class QfgLiteral(ctypes.Structure):
@@ -131,6 +132,17 @@ SIGNATURES = [
       ctypes.c_int32, c_vp, c_i64p]),
     ("qfg_extend_bindings", ctypes.c_int,
      [c_vp, c_vp, ctypes.POINTER(QfgLiteral), ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(c_vp)]),
+    ("qfg_coverage", ctypes.c_int,
+     [c_vp, c_vp, ctypes.POINTER(QfgLiteral), ctypes.c_int32, ctypes.POINTER(c_vp), ctypes.c_int64,
+      ctypes.POINTER(c_vp), ctypes.c_int64, c_vp, c_i64p]),
+    ("qfg_examples_create", ctypes.c_int,
+     [c_vp, ctypes.c_int32, ctypes.POINTER(c_vp), ctypes.c_int64, ctypes.POINTER(c_vp)]),
+    ("qfg_examples_destroy", ctypes.c_int, [c_vp, c_vp]),
+    ("qfg_coverage_examples", ctypes.c_int,
+     [c_vp, c_vp, ctypes.POINTER(QfgLiteral), c_vp, c_vp, c_vp, c_i64p]),
+    ("qfg_compact_rows", ctypes.c_int,
+     [c_vp, ctypes.c_int32, ctypes.POINTER(c_vp), ctypes.c_int64, c_vp, ctypes.c_int32,
+      ctypes.POINTER(c_vp), ctypes.c_int64, c_i64p]),
 ]
 
 _lib = None

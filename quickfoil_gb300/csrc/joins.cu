@@ -24,60 +24,11 @@
 // than the relation (CollaborateJoin, :172-207), else the relation (:208-250).
 #include <cstring>
 
-#include "qfg_common.cuh"
+#include "keysets.cuh"
 
 namespace qfg {
 
 namespace {
-
-struct KeyCols {
-  const int32_t* c[QFG_MAX_ARITY];
-  int nk;
-};
-
-__device__ __forceinline__ uint32_t keys_hash(const KeyCols& k, int64_t r) {
-  uint32_t h = mix32((uint32_t)k.c[0][r]);
-  for (int q = 1; q < k.nk; ++q) h = mix32(h + 0x9e3779b9u + (uint32_t)k.c[q][r]);
-  return h;
-}
-
-__device__ __forceinline__ bool keys_eq(const KeyCols& a, int64_t x, const KeyCols& b, int64_t y) {
-  for (int q = 0; q < a.nk; ++q)
-    if (a.c[q][x] != b.c[q][y]) return false;
-  return true;
-}
-
-__global__ void keyset_insert_kernel(KeyCols build, int64_t n, int32_t* __restrict__ owner,
-                                     uint32_t mask, int32_t* __restrict__ rep) {
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
-       r += (int64_t)gridDim.x * blockDim.x) {
-    uint32_t slot = keys_hash(build, r) & mask;
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-      const int32_t o = atomicCAS(&owner[slot], -1, (int32_t)r);
-      if (o == -1) {
-        if (rep != nullptr) rep[r] = (int32_t)r;
-        break;
-      }
-      if (keys_eq(build, o, build, r)) {
-        if (rep != nullptr) rep[r] = o;
-        break;
-      }
-      slot = (slot + 1) & mask;
-    }
-  }
-}
-
-__device__ __forceinline__ int32_t keyset_find(const KeyCols& build, const int32_t* __restrict__ owner,
-                                               uint32_t mask, const KeyCols& probe, int64_t i) {
-  uint32_t slot = keys_hash(probe, i) & mask;
-  for (uint32_t p = 0; p <= mask; ++p) {
-    const int32_t o = owner[slot];
-    if (o < 0) return -1;
-    if (keys_eq(build, o, probe, i)) return o;
-    slot = (slot + 1) & mask;
-  }
-  return -1;
-}
 
 __global__ void semijoin_bits_kernel(KeyCols build, const int32_t* __restrict__ owner, uint32_t mask,
                                      KeyCols probe, int64_t n, uint32_t* __restrict__ words,
@@ -90,7 +41,7 @@ __global__ void semijoin_bits_kernel(KeyCols build, const int32_t* __restrict__ 
     const bool hit = i < n && keyset_find(build, owner, mask, probe, i) >= 0;
     const unsigned ball = __ballot_sync(kFullMask, hit);
     if (lane == 0) {
-      words[w] = ball;
+      if (words != nullptr) words[w] = ball;
       if (ball != 0u) atomicAdd(ones, (unsigned long long)__popc(ball));
     }
   }
@@ -153,17 +104,6 @@ __global__ void extend_write_kernel(ExtendArgs a, int64_t n_probe, const int32_t
   }
 }
 
-unsigned rows_grid(Ctx* ctx, int64_t n) {
-  const int64_t blocks = (n + 255) / 256;
-  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)ctx->num_sms * 8));
-}
-
-uint32_t table_mask(int64_t n) {
-  uint32_t cap = 64;
-  while (cap < (uint64_t)(2 * n)) cap <<= 1;
-  return cap - 1;
-}
-
 int make_keycols(Ctx* ctx, const int32_t* const* host_ptrs, int nk, KeyCols* out) {
   if (nk < 1 || nk > QFG_MAX_ARITY || host_ptrs == nullptr)
     return set_error(ctx, QFG_ERR_INVALID, "key column count must be in [1, 8]");
@@ -186,7 +126,7 @@ int semijoin(Ctx* ctx, const KeyCols& set_side, int64_t n_set, const KeyCols& bi
     QFG_TRY(ctx->scratch[kScrJoin].reserve(ctx, sizeof(int32_t) * ((size_t)mask + 1)));
     int32_t* owner = ctx->scratch[kScrJoin].as<int32_t>();
     QFG_CUDA(ctx, cudaMemsetAsync(owner, 0xff, sizeof(int32_t) * ((size_t)mask + 1), ctx->stream));
-    keyset_insert_kernel<<<rows_grid(ctx, n_set), 256, 0, ctx->stream>>>(set_side, n_set, owner,
+    keyset_insert_kernel<0><<<rows_grid(ctx, n_set), 256, 0, ctx->stream>>>(set_side, n_set, owner,
                                                                          mask, nullptr);
     QFG_LAUNCHED(ctx);
     const unsigned grid = (unsigned)std::max<int64_t>(
@@ -220,7 +160,7 @@ int extend_label(Ctx* ctx, const KeyCols& build, int64_t n_build, const KeyCols&
   int32_t* seg_first = rep + n_build;
   int32_t* seg_last = seg_first + n_build;
   QFG_CUDA(ctx, cudaMemsetAsync(owner, 0xff, sizeof(int32_t) * cap, ctx->stream));
-  keyset_insert_kernel<<<rows_grid(ctx, n_build), 256, 0, ctx->stream>>>(build, n_build, owner,
+  keyset_insert_kernel<0><<<rows_grid(ctx, n_build), 256, 0, ctx->stream>>>(build, n_build, owner,
                                                                          mask, rep);
   QFG_LAUNCHED(ctx);
   QFG_TRY(ctx->scratch[kScrSortA].reserve(ctx, 2 * sizeof(uint32_t) * (size_t)n_build));

@@ -123,6 +123,15 @@ struct PartitionedColumn {
   DevBuf offsets;  // 2^bits + 1 int64
 };
 
+// Open-addressing set of the relation's distinct key tuples over a list of
+// argument positions: slot -> a relation row holding the tuple (-1 empty).
+struct KeySet {
+  uint32_t mask = 0;  // slots - 1 (slots >= 2 * tuples, a power of two)
+  DevBuf owner;
+  int64_t distinct = 0;  // distinct key tuples (inline form)
+  DevBuf filter;         // hashed-bit filter of the key tuples, or empty
+};
+
 struct Relation {
   int32_t id = 0;
   int32_t num_columns = 0;
@@ -132,6 +141,7 @@ struct Relation {
   std::vector<const int32_t*> columns;     // device column pointers
   std::map<std::vector<int>, std::unique_ptr<KeyTable>> key_tables;
   std::map<std::pair<int, int>, std::unique_ptr<PartitionedColumn>> partitions;  // (col, bits)
+  std::map<std::vector<int>, std::unique_ptr<KeySet>> key_sets;  // by argument positions
 };
 
 struct Ctx {

@@ -387,6 +387,100 @@ class Engine:
         return BindingSet(self, h, ncols, num_out_positive, num_out_negative)
 
 
+    def coverage(self, bindings: BindingSet, literal: Literal, num_target_columns: int,
+                 uncovered_positive, negative=None, positive_bits: bool = True):
+        """ComputeCoverageOnUncoveredData / ComputeCoveredPositives of
+        ``literal`` appended to the clause whose binding set is ``bindings``.
+        ``uncovered_positive`` and ``negative`` are lists of CUDA int32
+        tensors (``negative`` None: positives only).  Returns ((covered
+        positives, covered negatives), bit blocks over the uncovered positives
+        as an int64 CUDA tensor, or None)."""
+        import torch
+        nu = uncovered_positive[0].numel() if uncovered_positive else 0
+        nn = negative[0].numel() if negative else 0
+        bits = None
+        if positive_bits:
+            bits = torch.empty(max(1, (nu + 63) // 64), dtype=torch.int64, device="cuda")
+        counts = (ctypes.c_int64 * 2)()
+        lit = literal.to_c()
+        up = C.ptr_array([t.data_ptr() for t in uncovered_positive]) if nu else None
+        npt = C.ptr_array([t.data_ptr() for t in negative]) if nn else None
+        C.check(self.lib.qfg_coverage(self.ctx, bindings.handle, ctypes.byref(lit),
+                                      num_target_columns, up, nu, npt, nn,
+                                      bits.data_ptr() if bits is not None else None, counts),
+                self.ctx, "qfg_coverage")
+        if bits is not None:
+            bits = bits[:(nu + 63) // 64]
+        return (counts[0], counts[1]), bits
+
+    def examples(self, columns) -> "ExampleTable":
+        """qfg_examples_create: an example table (CUDA int32 columns, kept
+        unchanged while the handle lives) prepared for many coverage calls."""
+        return ExampleTable(self, columns)
+
+    def coverage_examples(self, bindings: BindingSet, literal: Literal,
+                          uncovered_positive: "ExampleTable",
+                          negative: Optional["ExampleTable"] = None, positive_bits: bool = True):
+        """qfg_coverage_examples: coverage() on prepared example tables."""
+        import torch
+        nu = uncovered_positive.num_rows
+        bits = None
+        if positive_bits:
+            bits = torch.empty(max(1, (nu + 63) // 64), dtype=torch.int64, device="cuda")
+        counts = (ctypes.c_int64 * 2)()
+        lit = literal.to_c()
+        C.check(self.lib.qfg_coverage_examples(
+            self.ctx, bindings.handle, ctypes.byref(lit), uncovered_positive.handle,
+            negative.handle if negative is not None else None,
+            bits.data_ptr() if bits is not None else None, counts),
+            self.ctx, "qfg_coverage_examples")
+        if bits is not None:
+            bits = bits[:(nu + 63) // 64]
+        return (counts[0], counts[1]), bits
+
+    def compact_rows(self, columns, bits, keep_set: bool = False, capacity: Optional[int] = None):
+        """The uncovered-example compaction: rows of the CUDA int32 ``columns``
+        whose bit in ``bits`` is clear (set with ``keep_set``), in order."""
+        import torch
+        n = columns[0].numel() if columns else 0
+        cap = n if capacity is None else capacity
+        outs = [torch.empty(max(1, cap), dtype=torch.int32, device="cuda") for _ in columns]
+        kept = ctypes.c_int64()
+        C.check(self.lib.qfg_compact_rows(
+            self.ctx, len(columns), C.ptr_array([t.data_ptr() for t in columns]), n,
+            bits.data_ptr() if bits is not None else None, 1 if keep_set else 0,
+            C.ptr_array([t.data_ptr() for t in outs]), cap, ctypes.byref(kept)),
+            self.ctx, "qfg_compact_rows")
+        return [o[:kept.value] for o in outs]
+
+
+class ExampleTable:
+    """qfg_examples_*: example columns with their key set, kept for many
+    coverage calls."""
+
+    def __init__(self, engine: Engine, columns):
+        self.engine = engine
+        self._keep = list(columns)
+        self.num_columns = len(self._keep)
+        self.num_rows = self._keep[0].numel() if self._keep else 0
+        h = C.c_vp()
+        C.check(engine.lib.qfg_examples_create(
+            engine.ctx, self.num_columns, C.ptr_array([t.data_ptr() for t in self._keep]),
+            self.num_rows, ctypes.byref(h)), engine.ctx, "qfg_examples_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle is not None:
+            self.engine.lib.qfg_examples_destroy(self.engine.ctx, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class StepGraph:
     """qfg_step_graph_*: one refinement step replayed with a single launch."""
 

@@ -88,3 +88,77 @@ def batched_step_reference():
     batched step (32M x 6 bindings, 32 relations, 256 literals)."""
     z = np.load(os.path.join(HERE, "batched_step_reference.npz"))
     return unpack_literals(z["lits"]), z["counts"], [int(v) for v in z["checksum"]]
+
+
+def coverage_synthetic():
+    """Seeded coverage cases: (relations, target columns, target positives,
+    binding columns, binding positives, literal, uncovered rows of the
+    target, divergent).  Regenerated here rather than stored; the fixture
+    keeps a checksum of each case so a changed generator is caught."""
+    rng = np.random.default_rng(2024)
+    cases = []
+    shapes = [  # (binding rows, relation tuples, domain, target columns, binding columns, arity)
+        (500, 2000, 60, 2, 3, 2), (3000, 800, 80, 1, 3, 3), (4000, 300, 150, 3, 4, 2),
+        (20000, 5000, 300, 2, 3, 2), (900, 900, 20, 2, 5, 3), (60, 40, 10, 1, 2, 1),
+        (70000, 100000, 300, 2, 3, 2),  # sides above 32768 rows, both smaller than the relation
+        (2500, 1500, 100, 3, 3, 3)]
+    for i, (nb, nrel, dom, k, nc, ar) in enumerate(shapes):
+        T = [rng.integers(0, dom, 3000).astype(np.int32) for _ in range(k)]
+        tP = 1400
+        rel = [rng.integers(0, dom, nrel).astype(np.int32) for _ in range(ar)]
+        B = [rng.integers(0, dom, nb).astype(np.int32) for _ in range(nc)]
+        bP = int(rng.integers(1, nb))
+        if i == 6:
+            bP = nb // 2
+        vars_ = [int(rng.integers(-1, nc)) for _ in range(ar)]
+        if i == 4:
+            vars_ = [1, 1, -1]  # repeated variable
+        if i == 7:
+            vars_ = [0, 2, 0]
+        if all(v < 0 for v in vars_):
+            vars_[0] = 0
+        rows = np.flatnonzero(rng.random(tP) < 0.7).astype(np.int32)
+        if i == 5:
+            rows = rows[:0]  # no uncovered positive left
+        cases.append(([rel], T, tP, B, bP, Literal(0, tuple(vars_)), rows, False))
+    # the divergent case: 35000 positive binding rows against 1000 tuples
+    T = [rng.integers(0, 300, 3000).astype(np.int32) for _ in range(2)]
+    rel = [rng.integers(0, 300, 1000).astype(np.int32) for _ in range(2)]
+    B = [rng.integers(0, 300, 70000).astype(np.int32) for _ in range(3)]
+    cases.append(([rel], T, 1500, B, 35000, Literal(0, (1, -1)),
+                  np.arange(0, 1500, 2, dtype=np.int32), True))
+    return cases
+
+
+def coverage_case_checksum(case):
+    rels, T, tP, B, bP, lit, rows, _ = case
+    return input_checksum(_Cols(list(B) + list(T) + [rows], rels)) + [tP, bP]
+
+
+class _Cols:
+    def __init__(self, binding_columns, relations):
+        self.binding_columns = binding_columns
+        self.relations = relations
+
+
+def coverage_cases():
+    """(synthetic, traced): synthetic = [(case, counts, flags, checksum)],
+    traced = [(trace name, call index, literal index, uncovered rows,
+    counts, flags)]; flags are bool per uncovered positive."""
+    z = np.load(os.path.join(HERE, "coverage_cases.npz"))
+    syn = []
+    gen = coverage_synthetic()
+    for i in range(int(z["num_synthetic"][0])):
+        case = gen[i]
+        n = len(case[6])
+        syn.append((case, tuple(int(v) for v in z[f"s{i}_counts"]),
+                    np.unpackbits(z[f"s{i}_flags"], bitorder="little")[:n].astype(bool),
+                    [int(v) for v in z[f"s{i}_checksum"]]))
+    traced = []
+    for i in range(int(z["num_traced"][0])):
+        kb, j, li = (int(v) for v in z[f"t{i}_key"])
+        rows = z[f"t{i}_rows"]
+        traced.append((("kinship", "bongard")[kb], j, li, rows,
+                       tuple(int(v) for v in z[f"t{i}_counts"]),
+                       np.unpackbits(z[f"t{i}_flags"], bitorder="little")[:len(rows)].astype(bool)))
+    return syn, traced

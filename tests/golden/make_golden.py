@@ -1,7 +1,7 @@
 """Generates the golden fixtures in this directory from the reference's own
 code (oracle/_ref, built from the reference sources by oracle/build_ref.sh).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--coverage]   (--coverage: coverage_cases.npz only)
 
 * eval_cases.npz   -- seeded evaluation cases (uniform and Zipf relations,
                       atoms, repeated variables, P = 0 / P = n, no join
@@ -19,6 +19,17 @@ code (oracle/_ref, built from the reference sources by oracle/build_ref.sh).
 * bongard.npz      -- the same for a Bongard-like knowledge base (2000
                       pictures, planted rule "a circle inside a triangle",
                       clauses up to 4 literals).
+* coverage_cases.npz -- the reference's ComputeCoverageOnUncoveredData
+                      (covered counts, covered flag per uncovered positive)
+                      on seeded synthetic cases (repeated and unbound
+                      arguments, 1-3 target columns, no uncovered positive,
+                      label sides above 32768 rows smaller than the
+                      relation) and on every Evaluate call of the kinship
+                      and Bongard traces, each literal appended to that
+                      call's binding set.  One case marked divergent has a
+                      label side of more than 32768 rows that is not smaller
+                      than the relation, where the reference's chunk-relative
+                      row ids make its counts differ from set membership.
 
 Only this script reads the reference; the tests read the fixtures, so they
 also run where the reference sources are absent.
@@ -37,7 +48,7 @@ sys.path.insert(0, ROOT)
 import oracle.ref as ref  # noqa: E402
 from quickfoil_gb300 import workloads  # noqa: E402
 from quickfoil_gb300.engine import Literal  # noqa: E402
-from tests.golden import input_checksum  # noqa: E402
+from tests.golden import coverage_case_checksum, coverage_synthetic, input_checksum  # noqa: E402
 
 
 def pack_relations(relations, prefix, out):
@@ -186,10 +197,64 @@ def bongard():
     learn_fixture(workloads.bongard(seed=1, pictures=2000, max_positive=300), "bongard")
 
 
+def _coverage_from_traces():
+    """(trace name, call index, literal index, uncovered rows) of every
+    literal of every Evaluate call of the kinship and Bongard traces."""
+    from tests.golden import learn_trace
+    out = []
+    for name in ("kinship", "bongard"):
+        rels, calls, _ = learn_trace(name)
+        target = next(c for c in calls if c[0] == "evaluate")
+        P = target[3]
+        rng = np.random.default_rng(len(name))
+        for j, call in enumerate(calls):
+            if call[0] != "evaluate":
+                continue
+            for i in range(len(call[4])):
+                rows = np.arange(P, dtype=np.int32)
+                if (i + j) % 2:
+                    rows = np.flatnonzero(rng.random(P) < 0.5).astype(np.int32)
+                out.append((name, j, i, rows))
+    return out
+
+
+def coverage_cases():
+    from tests.golden import learn_trace
+    out = {}
+    syn = coverage_synthetic()
+    for i, (rels, T, tP, B, bP, lit, rows, divergent) in enumerate(syn):
+        U = [t[rows] for t in T]
+        counts, flags = ref.coverage(rels, T, tP, B, bP, lit, U)
+        out[f"s{i}_checksum"] = np.array(coverage_case_checksum(syn[i]), dtype=np.uint64)
+        out[f"s{i}_counts"] = np.array(counts, dtype=np.int64)
+        out[f"s{i}_flags"] = np.packbits(flags, bitorder="little")
+    out["num_synthetic"] = np.array([len(syn)])
+    traced = _coverage_from_traces()
+    cache = {}
+    for i, (name, j, li, rows) in enumerate(traced):
+        if name not in cache:
+            cache[name] = learn_trace(name)
+        rels, calls, _ = cache[name]
+        target = next(c for c in calls if c[0] == "evaluate")
+        T, tP = target[2], target[3]
+        _, _, B, bP, lits, _ = calls[j]
+        U = [t[rows] for t in T]
+        counts, flags = ref.coverage(rels, T, tP, B, bP, lits[li], U)
+        out[f"t{i}_key"] = np.array([0 if name == "kinship" else 1, j, li])
+        out[f"t{i}_rows"] = rows
+        out[f"t{i}_counts"] = np.array(counts, dtype=np.int64)
+        out[f"t{i}_flags"] = np.packbits(flags, bitorder="little")
+    out["num_traced"] = np.array([len(traced)])
+    np.savez_compressed(os.path.join(HERE, "coverage_cases.npz"), **out)
+    print("coverage_cases.npz:", len(syn), "synthetic,", len(traced), "traced cases")
+
+
 if __name__ == "__main__" and "--batched-step" not in sys.argv:
-    eval_cases()
-    kinship()
-    bongard()
+    if "--coverage" not in sys.argv:
+        eval_cases()
+        kinship()
+        bongard()
+    coverage_cases()
 
 
 def batched_step_reference():
