@@ -377,6 +377,25 @@ int qfg_coverage_examples(qfg_ctx* ctx, const qfg_bindings* bindings, const qfg_
                           const qfg_examples* uncovered_positive, const qfg_examples* negative,
                           uint64_t* d_positive_bits, int64_t* num_covered);
 
+/* QuickFoilTestRunner::RunTest (learner/QuickFoilTestRunner.cpp:128-161) on
+ * device tables: the test rows (num_target_columns device columns of
+ * num_rows rows) that none of the learnt clauses covers.  Clause i has
+ * clause_lengths[i] >= 1 body literals, stored one clause after another in
+ * body_literals; a literal's vars[] names binding columns (the target's
+ * columns first, then one column per unbound argument of each earlier body
+ * literal, in order) and -1 for an argument that introduces a new variable.
+ * For every clause the full test table is extended by all body literals but
+ * the last (CreateBindingTable, operations/MultiColumnHashJoin.cpp:26-115);
+ * the test rows still uncovered whose tuple the last literal's coverage
+ * holds are removed (ComputeUnCoveredData, QuickFoilTestRunner.cpp:40-126).
+ * *num_uncovered receives the rows left; d_uncovered_out (may be NULL)
+ * receives them in order (num_target_columns device columns with room for
+ * num_rows rows).  Coverage is set membership (see qfg_coverage). */
+int qfg_run_test(qfg_ctx* ctx, int32_t num_clauses, const int32_t* clause_lengths,
+                 const qfg_literal* body_literals, int32_t num_target_columns,
+                 const int32_t* const* d_test_columns, int64_t num_rows, int64_t* num_uncovered,
+                 int32_t* const* d_uncovered_out);
+
 /* The uncovered-example compaction of learner/QuickFoil.cpp:612-708 (and of
  * QuickFoilTestRunner::ComputeUnCoveredData, learner/QuickFoilTestRunner.cpp:99-116):
  * the rows of num_columns device columns whose bit in d_bits (the layout of

@@ -290,3 +290,35 @@ def compact_rows(columns, bits, keep_set=False):
                                bits.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
                                1 if keep_set else 0, _colptrs(outs))
     return [o[:m] for o in outs]
+
+
+def run_test(relations, clauses, test_columns):
+    """QuickFoilTestRunner::RunTest (learner/QuickFoilTestRunner.cpp:128-161)
+    composed from the restatements above: per clause the full test table is
+    extended by every body literal but the last (CreateBindingTable as the
+    positive side of the label-aware extension, sized by the evaluation's
+    binding count), then the last literal's coverage removes the test rows it
+    covers from those still uncovered.  clauses: lists of (relation, vars)
+    with vars naming binding columns (-1 new).  Returns the uncovered rows."""
+    test = _as_cols(test_columns)
+    k = len(test)
+    left = [c.copy() for c in test]
+    for body in clauses:
+        if len(left[0]) == 0:
+            break
+        B, empty = [c for c in test], len(test[0]) == 0
+        for rel, vars_ in body[:-1]:
+            lit = (rel, tuple(vars_), next(i for i, v in enumerate(vars_) if v >= 0))
+            npos = int(evaluate(relations, B, len(B[0]), [lit])[0][2])
+            if npos == 0:
+                empty = True
+                break
+            B = extend_bindings(B, len(B[0]), relations[rel], lit, npos, 0)
+        if empty:
+            continue
+        rel, vars_ = body[-1]
+        lit = (rel, tuple(vars_), next(i for i, v in enumerate(vars_) if v >= 0))
+        (cp, _), bits = coverage(B, len(B[0]), relations[rel], lit, k, left)
+        if cp:
+            left = compact_rows(left, bits)
+    return left

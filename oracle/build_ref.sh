@@ -20,7 +20,7 @@ SRCS="operations/RadixPartition operations/BuildHashTable operations/HashJoin op
 operations/CountAggregator operations/PartitionAssigner operations/LeftSemiJoin
 operations/SemiJoinFactory operations/MultiColumnHashJoin storage/FoilHashTable
 learner/CandidateLiteralEvaluator learner/CandidateLiteralEnumerator learner/LiteralSelector
-learner/QuickFoil learner/QuickFoilTimer schema/FoilClause utility/BitVector memory/MemoryUsage
+learner/QuickFoil learner/QuickFoilTestRunner learner/QuickFoilTimer schema/FoilClause utility/BitVector memory/MemoryUsage
 types/Type"
 FLAGS="-std=c++14 -O3 -fPIC -DNDEBUG -w -I$HERE/shims -I$REF"
 pids=()

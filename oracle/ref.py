@@ -48,6 +48,12 @@ def lib():
                                      ctypes.c_int64, ctypes.POINTER(i32p), i64p,
                                      ctypes.POINTER(ctypes.c_uint8)]
         L.qfref_coverage.restype = ctypes.c_int
+        L.qfref_learn_test.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), i64p,
+                                       ctypes.POINTER(i32p), ctypes.c_int, ctypes.c_int64,
+                                       ctypes.c_int64, ctypes.POINTER(i32p), ctypes.c_int,
+                                       ctypes.c_int64, ctypes.POINTER(i32p), ctypes.c_int64,
+                                       ctypes.POINTER(i32p), ctypes.c_char_p, ctypes.c_int, i64p]
+        L.qfref_learn_test.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -135,3 +141,23 @@ def coverage(relations, target_columns, target_num_positive: int, binding_column
     if rc != 0:
         raise ValueError(f"reference driver rejected the input ({rc})")
     return (int(counts[0]), int(counts[1])), covered[:nu].astype(bool)
+
+
+def learn_test(relations, target_columns, num_positive: int, max_clause_length: int,
+               test_positive, test_negative):
+    """Runs the reference learner, then its test runner on the two test
+    tables; returns (learnt clauses, (uncovered test positives, uncovered
+    test negatives))."""
+    keep_r, rptr, rnc, rnt = _relations(relations)
+    keep_t, tptr = _cols(target_columns)
+    keep_p, pptr = _cols(test_positive)
+    keep_n, nptr = _cols(test_negative)
+    out = ctypes.create_string_buffer(1 << 16)
+    unc = np.zeros(2, dtype=np.int64)
+    rc = lib().qfref_learn_test(len(relations), rnc, rnt, rptr, len(keep_t), len(keep_t[0]),
+                                num_positive, tptr, max_clause_length, len(keep_p[0]), pptr,
+                                len(keep_n[0]), nptr, out, len(out),
+                                unc.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    if rc != 0:
+        raise RuntimeError(f"reference learner failed ({rc})")
+    return [l for l in out.value.decode().splitlines() if l], (int(unc[0]), int(unc[1]))

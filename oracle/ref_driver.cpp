@@ -12,6 +12,8 @@
 //                 through link-time wrappers of Evaluate and
 //                 CreateLabelAwareBindingTables, writes every call's inputs
 //                 and outputs to a trace file.
+// qfref_learn_test runs the learner, then QuickFoilTestRunner::RunTest
+//                 (learner/QuickFoilTestRunner.cpp:128-161) on test tables.
 // qfref_coverage  runs QuickFoil::ComputeCoverageOnUncoveredData
 //                 (learner/QuickFoil.cpp:471-573) on a given building clause
 //                 (binding set) and uncovered positives: the covered counts
@@ -30,6 +32,7 @@
 #include "learner/CandidateLiteralInfo.hpp"
 #include "learner/LiteralSelector.hpp"
 #include "learner/QuickFoilState.hpp"
+#include "learner/QuickFoilTestRunner.hpp"
 #include "operations/SemiJoin.hpp"
 #include "storage/FoilHashTable.hpp"
 #define private public
@@ -288,6 +291,46 @@ int qfref_learn(int nrel, const int* rel_ncols, const int64_t* rel_ntuples,
     strncpy(clauses, out.c_str(), (size_t)clauses_cap - 1);
     clauses[clauses_cap - 1] = '\0';
   }
+  return 0;
+}
+
+// Runs the reference learner as qfref_learn does, then its test runner
+// (learner/QuickFoilTestRunner.cpp:128-161) on a positive and a negative
+// test table (test_ncols = target columns): uncovered[0] / [1] receive the
+// test rows no learnt clause covers.
+int qfref_learn_test(int nrel, const int* rel_ncols, const int64_t* rel_ntuples,
+                     const int32_t* const* rel_cols, int target_ncols, int64_t target_n,
+                     int64_t target_npos, const int32_t* const* target_cols,
+                     int max_clause_length, int64_t test_npos,
+                     const int32_t* const* test_pos_cols, int64_t test_nneg,
+                     const int32_t* const* test_neg_cols, char* clauses, int clauses_cap,
+                     int64_t* uncovered) {
+  FLAGS_maximum_clause_length = max_clause_length;
+  std::vector<std::unique_ptr<FoilPredicate>> owned;
+  Vector<const FoilPredicate*> background;
+  int off = 0;
+  for (int r = 0; r < nrel; ++r) {
+    Vector<int> types(rel_ncols[r], 0);
+    owned.emplace_back(new FoilPredicate(r, "r" + std::to_string(r), -1, types,
+                                         MakeColumns(rel_ncols[r], rel_cols + off, rel_ntuples[r])));
+    background.push_back(owned.back().get());
+    off += rel_ncols[r];
+  }
+  Vector<int> ttypes(target_ncols, 0);
+  FoilPredicate target(nrel, "target", -1, ttypes, MakeColumns(target_ncols, target_cols, target_n));
+  QuickFoil qf((size_type)target_npos, (size_type)(target_n - target_npos), &target, background);
+  qf.Learn();
+  std::string out;
+  for (const auto& c : qf.learnt_clauses()) out += c->ToString() + "\n";
+  if (clauses != nullptr && clauses_cap > 0) {
+    strncpy(clauses, out.c_str(), (size_t)clauses_cap - 1);
+    clauses[clauses_cap - 1] = '\0';
+  }
+  QuickFoilTestRunner runner(&target, qf.learnt_clauses());
+  TableView pos(MakeColumns(target_ncols, test_pos_cols, test_npos));
+  TableView neg(MakeColumns(target_ncols, test_neg_cols, test_nneg));
+  uncovered[0] = (int64_t)runner.RunTest(pos);
+  uncovered[1] = (int64_t)runner.RunTest(neg);
   return 0;
 }
 

@@ -140,6 +140,9 @@ SIGNATURES = [
     ("qfg_examples_destroy", ctypes.c_int, [c_vp, c_vp]),
     ("qfg_coverage_examples", ctypes.c_int,
      [c_vp, c_vp, ctypes.POINTER(QfgLiteral), c_vp, c_vp, c_vp, c_i64p]),
+    ("qfg_run_test", ctypes.c_int,
+     [c_vp, ctypes.c_int32, c_i32p, ctypes.POINTER(QfgLiteral), ctypes.c_int32,
+      ctypes.POINTER(c_vp), ctypes.c_int64, c_i64p, ctypes.POINTER(c_vp)]),
     ("qfg_compact_rows", ctypes.c_int,
      [c_vp, ctypes.c_int32, ctypes.POINTER(c_vp), ctypes.c_int64, c_vp, ctypes.c_int32,
       ctypes.POINTER(c_vp), ctypes.c_int64, c_i64p]),

@@ -66,6 +66,26 @@ def join_key(vars_: Sequence[int], var_types: Optional[Sequence[int]] = None) ->
     return best
 
 
+def parse_clause(text: str):
+    """A learnt clause as the reference prints it (FoilClause::ToString,
+    e.g. ``target(0, 1) :-  r1(0), r3(2, 0), r0(2, 1)``, relation ids after
+    the ``r``): (head arity, body literals) with each literal's vars naming
+    binding columns the way the binding tables grow -- a variable id below
+    the column count so far is bound (operations/MultiColumnHashJoin.cpp:
+    37-44), any other argument is new (-1) and appends a column."""
+    import re
+    head, _, body = text.partition(":-")
+    arity = len(re.findall(r"-?\d+", head.split("(", 1)[1]))
+    lits = []
+    ncols = arity
+    for name, args in re.findall(r"r(\d+)\(([^)]*)\)", body):
+        ids = [int(a) for a in args.split(",")]
+        vars_ = tuple(v if v < ncols else -1 for v in ids)
+        ncols += sum(1 for v in vars_ if v < 0)
+        lits.append(Literal(int(name), vars_))
+    return arity, lits
+
+
 @dataclass
 class CandidateLiteralInfo:
     literal: Literal
@@ -437,6 +457,27 @@ class Engine:
         if bits is not None:
             bits = bits[:(nu + 63) // 64]
         return (counts[0], counts[1]), bits
+
+    def run_test(self, clauses: Sequence[Sequence[Literal]], test_columns, rows: bool = False):
+        """qfg_run_test (QuickFoilTestRunner::RunTest): the test rows (CUDA
+        int32 target columns) no clause covers.  Returns the count, or with
+        ``rows`` (count, the rows as CUDA columns)."""
+        import torch
+        n = test_columns[0].numel() if test_columns else 0
+        lens = (ctypes.c_int32 * max(1, len(clauses)))(*[len(c) for c in clauses])
+        flat = [l.to_c() for c in clauses for l in c]
+        lits = (C.QfgLiteral * max(1, len(flat)))(*flat)
+        outs = [torch.empty(max(1, n), dtype=torch.int32, device="cuda") for _ in test_columns] \
+            if rows else None
+        left = ctypes.c_int64()
+        C.check(self.lib.qfg_run_test(
+            self.ctx, len(clauses), lens, lits, len(test_columns),
+            C.ptr_array([t.data_ptr() for t in test_columns]), n, ctypes.byref(left),
+            C.ptr_array([t.data_ptr() for t in outs]) if outs is not None else None),
+            self.ctx, "qfg_run_test")
+        if not rows:
+            return left.value
+        return left.value, [o[:left.value] for o in outs]
 
     def compact_rows(self, columns, bits, keep_set: bool = False, capacity: Optional[int] = None):
         """The uncovered-example compaction: rows of the CUDA int32 ``columns``

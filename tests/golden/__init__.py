@@ -162,3 +162,18 @@ def coverage_cases():
                        tuple(int(v) for v in z[f"t{i}_counts"]),
                        np.unpackbits(z[f"t{i}_flags"], bitorder="little")[:len(rows)].astype(bool)))
     return syn, traced
+
+
+def test_runs():
+    """[(name, learnt clauses, test positive columns, test negative columns,
+    (reference uncovered positives, uncovered negatives))]"""
+    z = np.load(os.path.join(HERE, "test_runs.npz"))
+    out = []
+    for i in range(int(z["num_runs"][0])):
+        k = 0
+        while f"t{i}_pos{k}" in z:
+            k += 1
+        out.append((str(z[f"t{i}_name"][0]), [str(c) for c in z[f"t{i}_clauses"]],
+                    [z[f"t{i}_pos{q}"] for q in range(k)], [z[f"t{i}_neg{q}"] for q in range(k)],
+                    tuple(int(v) for v in z[f"t{i}_uncovered"])))
+    return out

@@ -1,7 +1,8 @@
 """Generates the golden fixtures in this directory from the reference's own
 code (oracle/_ref, built from the reference sources by oracle/build_ref.sh).
 
-    python tests/golden/make_golden.py [--coverage]   (--coverage: coverage_cases.npz only)
+    python tests/golden/make_golden.py [--coverage]
+        (--coverage: coverage_cases.npz and test_runs.npz only)
 
 * eval_cases.npz   -- seeded evaluation cases (uniform and Zipf relations,
                       atoms, repeated variables, P = 0 / P = n, no join
@@ -19,6 +20,11 @@ code (oracle/_ref, built from the reference sources by oracle/build_ref.sh).
 * bongard.npz      -- the same for a Bongard-like knowledge base (2000
                       pictures, planted rule "a circle inside a triangle",
                       clauses up to 4 literals).
+* test_runs.npz    -- the reference learner's clauses and its test runner's
+                      uncovered counts (QuickFoilTestRunner::RunTest) on
+                      held-out test tables of the kinship and Bongard
+                      knowledge bases (every rule-true example as a test
+                      positive, fresh negatives).
 * coverage_cases.npz -- the reference's ComputeCoverageOnUncoveredData
                       (covered counts, covered flag per uncovered positive)
                       on seeded synthetic cases (repeated and unbound
@@ -249,12 +255,46 @@ def coverage_cases():
     print("coverage_cases.npz:", len(syn), "synthetic,", len(traced), "traced cases")
 
 
+def test_runs():
+    out = {}
+    tasks = [("kinship", workloads.kinship(seed=1),
+              workloads.kinship(seed=1, max_positive=10 ** 6, num_negative=2000)),
+             ("bongard", workloads.bongard(seed=1, pictures=2000, max_positive=300),
+              workloads.bongard(seed=1, pictures=2000, max_positive=10 ** 6))]
+    for i, (name, train, test) in enumerate(tasks):
+        assert all(np.array_equal(a, b) for ra, rb in zip(train.relations, test.relations)
+                   for a, b in zip(ra, rb))
+        P = test.num_positive
+        # Mixed test tables: a quarter of each side's rows come from the
+        # other side, so a test table is neither all covered nor all not.
+        rng = np.random.default_rng(7 + i)
+        n = len(test.target_columns[0])
+        pos_rows = np.concatenate([np.arange(P), rng.choice(np.arange(P, n), (n - P) // 4)])
+        neg_rows = np.concatenate([np.arange(P, n), rng.choice(np.arange(P), P // 4)])
+        pos_rows, neg_rows = rng.permutation(pos_rows), rng.permutation(neg_rows)
+        tpos = [c[pos_rows] for c in test.target_columns]
+        tneg = [c[neg_rows] for c in test.target_columns]
+        clauses, unc = ref.learn_test(train.relations, train.target_columns, train.num_positive,
+                                      train.max_clause_length, tpos, tneg)
+        out[f"t{i}_name"] = np.array([name])
+        out[f"t{i}_clauses"] = np.array(clauses)
+        for q, c in enumerate(tpos):
+            out[f"t{i}_pos{q}"] = c
+        for q, c in enumerate(tneg):
+            out[f"t{i}_neg{q}"] = c
+        out[f"t{i}_uncovered"] = np.array(unc, dtype=np.int64)
+        print(name, clauses, "uncovered test rows", unc, "of", len(tpos[0]), len(tneg[0]))
+    out["num_runs"] = np.array([len(tasks)])
+    np.savez_compressed(os.path.join(HERE, "test_runs.npz"), **out)
+
+
 if __name__ == "__main__" and "--batched-step" not in sys.argv:
     if "--coverage" not in sys.argv:
         eval_cases()
         kinship()
         bongard()
     coverage_cases()
+    test_runs()
 
 
 def batched_step_reference():
