@@ -330,6 +330,30 @@ int qfg_extend_bindings(qfg_ctx* ctx, const qfg_bindings* bindings, const qfg_li
                         int64_t num_out_positive, int64_t num_out_negative,
                         qfg_bindings** out);
 
+/* ---- facts from text --------------------------------------------------- */
+/* LoadData (main/main.cpp:49-109), parsed on the device: lines end at '\n';
+ * an empty line or one starting with '#' is skipped; fields split at every
+ * '|' (empty fields kept) must number num_arguments (1..64); every argument
+ * whose skipped[] flag is zero (skipped may be NULL) is converted as
+ * std::stoi does (types/FromString.hpp:23-30: leading white space, an
+ * optional sign, at least one digit, the value within int32, anything after
+ * the digits ignored).  text is host memory (flags QFG_HOST, copied) or
+ * device memory (QFG_DEVICE_BORROW).  The kept columns are written to
+ * d_out_columns (capacity rows each); *num_rows receives the row count,
+ * also when it exceeds capacity (QFG_ERR_INVALID, nothing written).  The
+ * reference aborts on a bad line; here the first one is named in
+ * *error_line (1-based, may be NULL) and the call returns QFG_ERR_INVALID. */
+int qfg_parse_text(qfg_ctx* ctx, const char* text, int64_t num_bytes, int flags,
+                   int32_t num_arguments, const int32_t* skipped, int32_t* const* d_out_columns,
+                   int64_t capacity, int64_t* num_rows, int64_t* error_line);
+
+/* CreateBackgroundPredicate (main/main.cpp:113-132): parses a predicate's
+ * facts as qfg_parse_text does and registers them as relation relation_id
+ * (engine-owned memory).  *num_tuples receives the fact count. */
+int qfg_relation_register_text(qfg_ctx* ctx, int32_t relation_id, const char* text,
+                               int64_t num_bytes, int flags, int32_t num_arguments,
+                               const int32_t* skipped, int64_t* num_tuples, int64_t* error_line);
+
 /* ---- coverage of a literal appended to the building clause ------------- */
 /* QuickFoil::ComputeCoverageOnUncoveredData (learner/QuickFoil.cpp:471-573)
  * and LiteralSelector::ComputeCoveredPositives (learner/LiteralSelector.cpp:

@@ -97,6 +97,9 @@ def lib():
         L.qfo_compact_rows.argtypes = [ctypes.c_int, ctypes.POINTER(i32p), ctypes.c_int64, u64p,
                                        ctypes.c_int, ctypes.POINTER(i32p)]
         L.qfo_compact_rows.restype = ctypes.c_int64
+        L.qfo_parse_text.argtypes = [ctypes.c_char_p, ctypes.c_int64, ctypes.c_int, i32p,
+                                     ctypes.POINTER(i32p), ctypes.c_int64, i64p, i64p]
+        L.qfo_parse_text.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -322,3 +325,26 @@ def run_test(relations, clauses, test_columns):
         if cp:
             left = compact_rows(left, bits)
     return left
+
+
+class TextError(ValueError):
+    """A line the loader rejects: .line (1-based) and .code (2 field count,
+    3 no digits, 4 out of range)."""
+
+    def __init__(self, code, line):
+        super().__init__(f"line {line}: error {code}")
+        self.code, self.line = code, line
+
+
+def parse_text(text: bytes, num_args: int, skipped=None):
+    """LoadData restated: the kept argument columns (int32) of the text."""
+    cap = text.count(b"\n") + 1
+    skip = np.array([int(bool(x)) for x in (skipped or [0] * num_args)], dtype=np.int32)
+    kept = int(num_args - skip.sum())
+    outs = [np.zeros(cap, dtype=np.int32) for _ in range(max(kept, 1))]
+    rows, err = ctypes.c_int64(), ctypes.c_int64()
+    rc = lib().qfo_parse_text(text, len(text), num_args, _i32ptr(skip), _colptrs(outs), cap,
+                              ctypes.byref(rows), ctypes.byref(err))
+    if rc != 0:
+        raise TextError(rc, err.value)
+    return [o[:rows.value] for o in outs[:kept]]

@@ -3,7 +3,9 @@
 # learner sources, read in place from the reference checkout and compiled
 # unmodified against the project-written headers in oracle/shims (glog,
 # gflags, folly, dynamic_bitset, lowest_bit, the configure-generated
-# MemoryConfig.hpp), plus oracle/ref_driver.cpp.  Test infrastructure only:
+# MemoryConfig.hpp, folly::dynamic, boost::split), plus oracle/ref_driver.cpp
+# and oracle/ref_loader.cpp (which compiles the reference's main/main.cpp for
+# its LoadData).  Test infrastructure only:
 # the output is used as a checker (tests/golden/make_golden.py), never by the
 # product.  Compiled like the reference's release build (-O3, NDEBUG).
 # Without the reference checkout (e.g. on the GPU host) it does nothing.
@@ -35,7 +37,12 @@ for p in "${pids[@]}"; do wait "$p"; done
 EVAL=$(nm "$OUT/obj/learner_CandidateLiteralEvaluator.o" | awk '$2 == "T" && $3 ~ /CandidateLiteralEvaluator8Evaluate/ {print $3}')
 EXT=$(nm "$OUT/obj/operations_MultiColumnHashJoin.o" | awk '$2 == "T" && $3 ~ /CreateLabelAwareBindingTables/ {print $3}')
 printf '#define QFREF_EVALUATE "%s"\n#define QFREF_EXTEND "%s"\n' "$EVAL" "$EXT" > "$OUT/wrap_names.h"
-g++ $FLAGS -I"$OUT" -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.o"
+g++ $FLAGS -I"$OUT" -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.o" &
+p1=$!
+g++ $FLAGS -c "$HERE/ref_loader.cpp" -o "$OUT/obj/ref_loader.o" &
+p2=$!
+wait "$p1"
+wait "$p2"
 g++ -shared -o "$OUT/libqfref.so.tmp" "$OUT"/obj/*.o "-Wl,--wrap=$EVAL" "-Wl,--wrap=$EXT"
 mv "$OUT/libqfref.so.tmp" "$OUT/libqfref.so"
 echo "build_ref: $OUT/libqfref.so"

@@ -601,3 +601,74 @@ int64_t qfo_compact_rows(int num_columns, const int32_t* const* columns, int64_t
   }
   return m;
 }
+
+static int c_space(char c) {
+  return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r';
+}
+
+/* std::stoi on [s, e): 0, or 3 (no digits) / 4 (out of int32). */
+static int stoi_field(const char* s, const char* e, int32_t* out) {
+  while (s < e && c_space(*s)) ++s;
+  int neg = 0;
+  if (s < e && (*s == '+' || *s == '-')) {
+    neg = *s == '-';
+    ++s;
+  }
+  if (s >= e || *s < '0' || *s > '9') return 3;
+  uint64_t v = 0;
+  int over = 0;
+  for (; s < e && *s >= '0' && *s <= '9'; ++s) {
+    if (!over) {
+      v = v * 10 + (uint64_t)(*s - '0');
+      over = v > 2147483648ull;
+    }
+  }
+  if (over || (!neg && v > 2147483647ull)) return 4;
+  *out = neg ? (int32_t)(-(int64_t)v) : (int32_t)v;
+  return 0;
+}
+
+int qfo_parse_text(const char* text, int64_t n, int num_args, const int32_t* skipped,
+                   int32_t* const* out, int64_t capacity, int64_t* num_rows,
+                   int64_t* error_line) {
+  int64_t rows = 0, line = 0;
+  *error_line = 0;
+  const char* p = text;
+  const char* end = text + n;
+  while (p < end) {
+    const char* e = memchr(p, '\n', (size_t)(end - p));
+    if (e == NULL) e = end;
+    ++line;
+    if (e > p && *p != '#') {
+      int nf = 1;
+      for (const char* q = p; q < e; ++q) nf += *q == '|';
+      if (nf != num_args) {
+        *error_line = line;
+        *num_rows = rows;
+        return 2;
+      }
+      int field = 0, col = 0;
+      const char* fs = p;
+      for (const char* q = p; q <= e; ++q) {
+        if (q < e && *q != '|') continue;
+        if (!(skipped != NULL && skipped[field])) {
+          int32_t v = 0;
+          const int rc = stoi_field(fs, q, &v);
+          if (rc != 0) {
+            *error_line = line;
+            *num_rows = rows;
+            return rc;
+          }
+          if (rows < capacity) out[col][rows] = v;
+          ++col;
+        }
+        ++field;
+        fs = q + 1;
+      }
+      ++rows;
+    }
+    p = e + 1;
+  }
+  *num_rows = rows;
+  return rows > capacity ? 1 : 0;
+}

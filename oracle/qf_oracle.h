@@ -147,6 +147,20 @@ int qfo_coverage(const qfo_table* bindings, int64_t num_positive, const qfo_tabl
 int64_t qfo_compact_rows(int num_columns, const int32_t* const* columns, int64_t n,
                          const uint64_t* bits, int keep_set, int32_t* const* out);
 
+/* LoadData (main/main.cpp:49-109) on a text buffer: lines end at '\n'
+ * (std::getline); an empty line or one starting with '#' is skipped; fields
+ * split at every '|' (boost::split, empty fields kept) must number
+ * num_args; every argument not skipped is converted as std::stoi does
+ * (FromString<kInt32>, types/FromString.hpp:23-30): leading white space, an
+ * optional sign, at least one digit, the value within int32, anything after
+ * the digits ignored.  Kept columns go to out[c] (capacity rows each).
+ * Returns 0; 1 when capacity is too small (num_rows still set); or, for the
+ * first bad line (its 1-based number in *error_line): 2 a field count that
+ * differs, 3 a field without digits, 4 a value out of range. */
+int qfo_parse_text(const char* text, int64_t n, int num_args, const int32_t* skipped,
+                   int32_t* const* out, int64_t capacity, int64_t* num_rows,
+                   int64_t* error_line);
+
 #ifdef __cplusplus
 }
 #endif

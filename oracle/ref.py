@@ -54,6 +54,9 @@ def lib():
                                        ctypes.c_int64, ctypes.POINTER(i32p), ctypes.c_int64,
                                        ctypes.POINTER(i32p), ctypes.c_char_p, ctypes.c_int, i64p]
         L.qfref_learn_test.restype = ctypes.c_int
+        L.qfref_load_text.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(i32p), ctypes.c_int64, i64p]
+        L.qfref_load_text.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -161,3 +164,20 @@ def learn_test(relations, target_columns, num_positive: int, max_clause_length: 
     if rc != 0:
         raise RuntimeError(f"reference learner failed ({rc})")
     return [l for l in out.value.decode().splitlines() if l], (int(unc[0]), int(unc[1]))
+
+
+def load_text(path: str, num_args: int, skipped=None):
+    """The reference's LoadData (main/main.cpp:49-109) on a file: the kept
+    argument columns.  A line the reference rejects aborts the process, so
+    only valid files are given to it."""
+    with open(path, "rb") as f:
+        cap = f.read().count(b"\n") + 1
+    skip = (ctypes.c_int * num_args)(*[int(bool(x)) for x in (skipped or [0] * num_args)])
+    kept = num_args - sum(1 for x in (skipped or []) if x)
+    outs = [np.zeros(cap, dtype=np.int32) for _ in range(max(kept, 1))]
+    keep, ptrs = _cols(outs)
+    rows = ctypes.c_int64()
+    rc = lib().qfref_load_text(path.encode(), num_args, skip, ptrs, cap, ctypes.byref(rows))
+    if rc != 0:
+        raise RuntimeError(f"reference loader: {rc}")
+    return [o[:rows.value] for o in keep[:kept]]

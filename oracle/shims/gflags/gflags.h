@@ -14,3 +14,6 @@
 #define DECLARE_double(name) extern double FLAGS_##name
 #define DECLARE_bool(name) extern bool FLAGS_##name
 #define DECLARE_string(name) extern std::string FLAGS_##name
+namespace gflags {
+inline void ParseCommandLineFlags(int*, char***, bool) {}
+}  // namespace gflags

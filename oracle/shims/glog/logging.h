@@ -54,3 +54,7 @@ struct FatalStream {
 #define DLOG(severity) qfshim::NullStream()
 #define LOG_IF(severity, cond) qfshim::NullStream()
 #define DLOG_IF(severity, cond) qfshim::NullStream()
+namespace google {
+inline void InitGoogleLogging(const char*) {}
+}  // namespace google
+static int FLAGS_v = 0;

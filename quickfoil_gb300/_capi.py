@@ -143,6 +143,12 @@ SIGNATURES = [
     ("qfg_run_test", ctypes.c_int,
      [c_vp, ctypes.c_int32, c_i32p, ctypes.POINTER(QfgLiteral), ctypes.c_int32,
       ctypes.POINTER(c_vp), ctypes.c_int64, c_i64p, ctypes.POINTER(c_vp)]),
+    ("qfg_parse_text", ctypes.c_int,
+     [c_vp, ctypes.c_char_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int32, c_i32p,
+      ctypes.POINTER(c_vp), ctypes.c_int64, c_i64p, c_i64p]),
+    ("qfg_relation_register_text", ctypes.c_int,
+     [c_vp, ctypes.c_int32, ctypes.c_char_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int32, c_i32p,
+      c_i64p, c_i64p]),
     ("qfg_compact_rows", ctypes.c_int,
      [c_vp, ctypes.c_int32, ctypes.POINTER(c_vp), ctypes.c_int64, c_vp, ctypes.c_int32,
       ctypes.POINTER(c_vp), ctypes.c_int64, c_i64p]),

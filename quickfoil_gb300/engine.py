@@ -433,6 +433,38 @@ class Engine:
             bits = bits[:(nu + 63) // 64]
         return (counts[0], counts[1]), bits
 
+    def parse_text(self, text, num_arguments: int, skipped: Optional[Sequence[bool]] = None):
+        """qfg_parse_text (LoadData): '|'-delimited facts -> CUDA int32
+        columns of the kept arguments.  ``text`` is bytes (host) or a CUDA
+        uint8 tensor.  A bad line raises QfgError naming it."""
+        import torch
+        on_dev = _is_torch(text)
+        n = text.numel() if on_dev else len(text)
+        cap = (int((text == 10).sum().item()) if on_dev else text.count(b"\n")) + 1
+        skip = (ctypes.c_int32 * num_arguments)(*[int(bool(x)) for x in (skipped or [0] * num_arguments)])
+        kept = num_arguments - sum(1 for x in (skipped or []) if x)
+        outs = [torch.empty(max(1, cap), dtype=torch.int32, device="cuda") for _ in range(kept)]
+        rows, err = ctypes.c_int64(), ctypes.c_int64()
+        ptr = ctypes.cast(ctypes.c_void_p(text.data_ptr()), ctypes.c_char_p) if on_dev else text
+        C.check(self.lib.qfg_parse_text(self.ctx, ptr, n, C.QFG_DEVICE_BORROW if on_dev else C.QFG_HOST,
+                                        num_arguments, skip,
+                                        C.ptr_array([o.data_ptr() for o in outs]), cap,
+                                        ctypes.byref(rows), ctypes.byref(err)),
+                self.ctx, "qfg_parse_text")
+        return [o[:rows.value] for o in outs]
+
+    def register_relation_text(self, relation_id: int, text: bytes, num_arguments: int,
+                               skipped: Optional[Sequence[bool]] = None) -> int:
+        """qfg_relation_register_text: a relation straight from its text;
+        returns the fact count."""
+        skip = (ctypes.c_int32 * num_arguments)(*[int(bool(x)) for x in (skipped or [0] * num_arguments)])
+        rows, err = ctypes.c_int64(), ctypes.c_int64()
+        C.check(self.lib.qfg_relation_register_text(self.ctx, relation_id, text, len(text), C.QFG_HOST,
+                                                    num_arguments, skip, ctypes.byref(rows),
+                                                    ctypes.byref(err)),
+                self.ctx, "qfg_relation_register_text")
+        return rows.value
+
     def examples(self, columns) -> "ExampleTable":
         """qfg_examples_create: an example table (CUDA int32 columns, kept
         unchanged while the handle lives) prepared for many coverage calls."""

@@ -177,3 +177,68 @@ def test_runs():
                     [z[f"t{i}_pos{q}"] for q in range(k)], [z[f"t{i}_neg{q}"] for q in range(k)],
                     tuple(int(v) for v in z[f"t{i}_uncovered"])))
     return out
+
+
+def text_texts():
+    """Texts for the loader: (name, text bytes, argument count, skipped
+    flags).  Regenerated here rather than stored; the fixture keeps the
+    reference's columns (small texts) or their checksums."""
+    rng = np.random.default_rng(31)
+    cases = []
+    lines = []
+    for i in range(1000):
+        if i % 97 == 0:
+            lines.append(b"# comment " + str(i).encode())
+        elif i % 89 == 0:
+            lines.append(b"")
+        lines.append(b"%d|%d" % (rng.integers(-10 ** 6, 10 ** 6), rng.integers(0, 10 ** 9)))
+    cases.append(("plain", b"\n".join(lines) + b"\n", 2, None))
+    tricky = [b"  12|\t-7", b"+5|0007", b"12abc|3 4", b"-0|+0", b"2147483647|-2147483648",
+              b"\t \v42|\f9x", b"#|not|a|row", b"8|9\r", b"", b"  -13  |  +21  "]
+    cases.append(("tricky", b"\n".join(tricky) + b"\n", 2, None))
+    cases.append(("crlf", b"1|2\r\n3|4\r\n#c\r\n5|6\r\n", 2, None))
+    cases.append(("skipped", b"1|xyz|3|4\n5||7|8\n9|  |11|12\n", 4, [0, 1, 0, 0]))
+    cases.append(("no_final_newline", b"10|20\n30|40", 2, None))
+    cases.append(("only_comments", b"# a\n#b\n\n", 1, None))
+    cases.append(("one_line", b"-99", 1, None))
+    big = rng.integers(-2 ** 31, 2 ** 31, (200_000, 3))
+    rows = [b"|".join(b"%d" % v for v in r) for r in big]
+    for i in range(0, len(rows), 1000):
+        rows[i] = b"#" + rows[i]
+    cases.append(("random_200k", b"\n".join(rows) + b"\n", 3, None))
+    return cases
+
+
+def text_rejects():
+    """(text, argument count) pairs the loader rejects, with the oracle's
+    error code and first bad line in test_textload.py."""
+    return [(b"1|2\n3\n", 2), (b"1|2|3\n", 2), (b"1|2\n|5\n", 2), (b"1|x\n", 2),
+            (b"+-1|2\n", 2), (b"- 1|2\n", 2), (b"   \n", 1), (b"1\n\r\n", 1),
+            (b"2147483648\n", 1), (b"#x\n-2147483649\n", 1),
+            (b"99999999999999999999999\n", 1), (b"1|2\n3|4|5\n6|x\n", 2)]
+
+
+def column_checksums(cols):
+    """Order-sensitive checksum per column (below 2^61)."""
+    return [input_checksum(_Cols([np.asarray(c)], []))[0] for c in cols]
+
+
+def text_rejects_accepted():
+    """Per text_rejects() entry: whether the reference's LoadData accepted
+    it (it aborts on a rejected text)."""
+    z = np.load(os.path.join(HERE, "text_cases.npz"))
+    return [bool(v) for v in z["rejects_accepted"]]
+
+
+def text_cases():
+    """[(name, text, argument count, skipped flags, reference columns or
+    None, row count, column checksums)]"""
+    z = np.load(os.path.join(HERE, "text_cases.npz"))
+    out = []
+    for i, (name, text, nargs, skipped) in enumerate(text_texts()):
+        assert str(z[f"x{i}_name"][0]) == name
+        ncols = int(z[f"x{i}_ncols"][0])
+        cols = [z[f"x{i}_c{q}"] for q in range(ncols)] if f"x{i}_c0" in z else None
+        out.append((name, text, nargs, skipped, cols, int(z[f"x{i}_rows"][0]),
+                    [int(v) for v in z[f"x{i}_checksum"]]))
+    return out

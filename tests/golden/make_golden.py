@@ -1,8 +1,9 @@
 """Generates the golden fixtures in this directory from the reference's own
 code (oracle/_ref, built from the reference sources by oracle/build_ref.sh).
 
-    python tests/golden/make_golden.py [--coverage]
-        (--coverage: coverage_cases.npz and test_runs.npz only)
+    python tests/golden/make_golden.py [--coverage | --text]
+        (--coverage: coverage_cases.npz and test_runs.npz only;
+         --text: text_cases.npz only)
 
 * eval_cases.npz   -- seeded evaluation cases (uniform and Zipf relations,
                       atoms, repeated variables, P = 0 / P = n, no join
@@ -25,6 +26,11 @@ code (oracle/_ref, built from the reference sources by oracle/build_ref.sh).
                       held-out test tables of the kinship and Bongard
                       knowledge bases (every rule-true example as a test
                       positive, fresh negatives).
+* text_cases.npz   -- '|'-delimited texts (comments, empty lines, white
+                      space, signs, trailing characters, CR LF endings,
+                      int32 limits, skipped arguments, no final newline, a
+                      200K-line random file) and the columns the reference's
+                      own LoadData (main/main.cpp:49-109) read from them.
 * coverage_cases.npz -- the reference's ComputeCoverageOnUncoveredData
                       (covered counts, covered flag per uncovered positive)
                       on seeded synthetic cases (repeated and unbound
@@ -54,7 +60,8 @@ sys.path.insert(0, ROOT)
 import oracle.ref as ref  # noqa: E402
 from quickfoil_gb300 import workloads  # noqa: E402
 from quickfoil_gb300.engine import Literal  # noqa: E402
-from tests.golden import coverage_case_checksum, coverage_synthetic, input_checksum  # noqa: E402
+from tests.golden import (column_checksums, coverage_case_checksum, coverage_synthetic,  # noqa: E402
+                          input_checksum, text_rejects, text_texts)
 
 
 def pack_relations(relations, prefix, out):
@@ -288,8 +295,56 @@ def test_runs():
     np.savez_compressed(os.path.join(HERE, "test_runs.npz"), **out)
 
 
+def text_cases():
+    import tempfile
+    out = {}
+    cases = text_texts()
+    for i, (name, text, nargs, skipped) in enumerate(cases):
+        with tempfile.NamedTemporaryFile(suffix=".txt", delete=False) as f:
+            f.write(text)
+            path = f.name
+        try:
+            cols = ref.load_text(path, nargs, skipped)
+        finally:
+            os.unlink(path)
+        out[f"x{i}_name"] = np.array([name])
+        out[f"x{i}_rows"] = np.array([len(cols[0]) if cols else 0])
+        out[f"x{i}_checksum"] = np.array(column_checksums(cols), dtype=np.uint64)
+        if len(text) < 100_000:  # small texts keep the reference's columns too
+            for q, c in enumerate(cols):
+                out[f"x{i}_c{q}"] = c
+        out[f"x{i}_ncols"] = np.array([len(cols)])
+        print(name, [len(c) for c in cols], [c[:4].tolist() for c in cols])
+    out["num_texts"] = np.array([len(cases)])
+    # Texts the reference rejects: its LoadData aborts the process (CHECK or
+    # LOG(FATAL)), so each runs in a child process; the fixture records
+    # whether the reference accepted it.
+    import subprocess
+    bad = text_rejects()
+    accepted = []
+    for j, (text, nargs) in enumerate(bad):
+        with tempfile.NamedTemporaryFile(suffix=".txt", delete=False) as f:
+            f.write(text)
+            path = f.name
+        try:
+            rc = subprocess.run([sys.executable, "-c",
+                                 "import sys; sys.path.insert(0, %r); import oracle.ref as r; "
+                                 "r.load_text(%r, %d)" % (ROOT, path, nargs)],
+                                capture_output=True).returncode
+        finally:
+            os.unlink(path)
+        accepted.append(rc == 0)
+    out["rejects_accepted"] = np.array(accepted)
+    print("reference accepted", sum(accepted), "of", len(bad), "rejected texts")
+    np.savez_compressed(os.path.join(HERE, "text_cases.npz"), **out)
+
+
 if __name__ == "__main__" and "--batched-step" not in sys.argv:
+    if "--text" in sys.argv:
+        text_cases()
+        sys.exit(0)
     if "--coverage" not in sys.argv:
+        text_cases()
         eval_cases()
         kinship()
         bongard()
