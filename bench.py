@@ -59,7 +59,8 @@ def parse_args():
     ap.add_argument("--eval-bits", type=int, default=0,
                     help="binding partition bits of the batched engine (0 = autotuned)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop leg")
-    ap.add_argument("--no-coverage", action="store_true", help="skip the coverage leg")
+    ap.add_argument("--no-coverage", action="store_true",
+                    help="skip the coverage, test-runner and loader legs")
     return ap.parse_args()
 
 
@@ -400,9 +401,11 @@ def run_gb300(args):
     serving = None
     if not args.no_serving and args.workload == "batched_step":
         serving = run_serving(eng, w, dev, torch)
-    coverage = None
+    coverage = loader = testrun = None
     if args.workload == "batched_step" and not args.no_coverage and rank == 0:
         coverage = run_coverage(eng, w, b, dev, torch, measured_peak_hbm()[0], args.no_cpu)
+        testrun = run_test_runner(eng, w, dev, torch, args.no_cpu)
+        loader = run_loader(eng, dev, torch, measured_peak_hbm()[0], args.no_cpu)
 
     if rank == 0:
         peak, peak_kind = measured_peak_hbm()
@@ -454,6 +457,10 @@ def run_gb300(args):
             line["serving"] = serving
         if coverage is not None:
             line["coverage"] = coverage
+        if testrun is not None:
+            line["test_runner"] = testrun
+        if loader is not None:
+            line["loader"] = loader
         if per_lit is not None:
             line["per_literal"] = per_lit
             line["batched_over_per_literal"] = line["value"] / (per_lit["value"] * world)
@@ -640,6 +647,109 @@ def run_coverage(eng, w, b, dev, torch, peak, no_cpu: bool, n_lits: int = 16, re
                            "achieved_gbs": comp_bytes / comp_s / 1e9,
                            "frac": comp_bytes / comp_s / 1e9 / peak},
             "cpu_baseline": cpu, "counts_equal_oracle": ok}
+
+
+def run_loader(eng, dev, torch, peak, no_cpu: bool, lines: int = 10_000_000, reps: int = 5):
+    """The fact loader (qfg_parse_text, LoadData on the device): a text of
+    `lines` facts of two random int32 arguments (about 220 MB), parsed from
+    device memory (the `value`) and from host memory with the copy inside
+    the timed region (`e2e`); the oracle's parser on the same text is the
+    CPU baseline."""
+    import ctypes
+    import oracle
+    from quickfoil_gb300 import _capi as C
+    from quickfoil_gb300.workloads import facts_text
+    rng = np.random.default_rng(17)
+    cols = [rng.integers(-2 ** 31, 2 ** 31, lines).astype(np.int32) for _ in range(2)]
+    text = facts_text(cols)
+    dtext = torch.from_numpy(np.frombuffer(text, dtype=np.uint8).copy()).to(dev)
+    outs = [torch.empty(lines, dtype=torch.int32, device=dev) for _ in range(2)]
+    optr = C.ptr_array([o.data_ptr() for o in outs])
+    rows, err = ctypes.c_int64(), ctypes.c_int64()
+    dptr = ctypes.cast(ctypes.c_void_p(dtext.data_ptr()), ctypes.c_char_p)
+
+    def parse(src, flags):
+        C.check(eng.lib.qfg_parse_text(eng.ctx, src, len(text), flags, 2, None, optr, lines,
+                                       ctypes.byref(rows), ctypes.byref(err)),
+                eng.ctx, "qfg_parse_text")
+
+    for _ in range(2):
+        parse(dptr, C.QFG_DEVICE_BORROW)
+        parse(text, C.QFG_HOST)
+    torch.cuda.synchronize()
+    ok = rows.value == lines and all(torch.equal(o.cpu(), torch.from_numpy(c)) for o, c in zip(outs, cols))
+    timings = {}
+    for name, src, flags in (("device", dptr, C.QFG_DEVICE_BORROW), ("host", text, C.QFG_HOST)):
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            parse(src, flags)
+        torch.cuda.synchronize()
+        timings[name] = (time.perf_counter() - t0) / reps
+    alg = len(text) + 8 * lines  # the text read once, the columns written once
+    line = {"metric": "fact text parsed (GB/s of '|'-delimited text)",
+            "value": len(text) / timings["device"] / 1e9, "unit": "GB/s",
+            "facts_per_s": lines / timings["device"], "ms": timings["device"] * 1e3,
+            "e2e": {"value": len(text) / timings["host"] / 1e9, "unit": "GB/s",
+                    "ms": timings["host"] * 1e3, "h2d_bytes": len(text),
+                    "mode": "qfg_parse_text from pageable host memory, copy included"},
+            "text_bytes": len(text), "facts": lines, "arguments": 2,
+            "roofline": {"bound": "hbm", "algorithmic_bytes": alg,
+                         "achieved": alg / timings["device"] / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / timings["device"] / 1e9 / peak,
+                         "note": "wall time of the call: newline pass, line scan, parse, compaction"},
+            "columns_equal_input": bool(ok)}
+    if not no_cpu:
+        t0 = time.perf_counter()
+        got = oracle.parse_text(text, 2)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(text) / dt / 1e9, "unit": "GB/s", "cores": 1,
+                                "kind": "port", "sample": f"the whole text ({dt:.1f} s)",
+                                "columns_equal": bool(all(np.array_equal(g, c) for g, c in zip(got, cols)))}
+    return line
+
+
+def run_test_runner(eng, w, dev, torch, no_cpu: bool, test_rows: int = 4_000_000, reps: int = 3):
+    """The device test runner (qfg_run_test, QuickFoilTestRunner::RunTest):
+    a test table of `test_rows` two-column rows (binding rows of the step:
+    their values meet the step's relations), three clauses of two body
+    literals over the step's relations; the oracle's restatement on the same
+    inputs is the CPU baseline."""
+    import oracle
+    from quickfoil_gb300 import workloads
+    from quickfoil_gb300.engine import Literal
+    rng = np.random.default_rng(23)
+    rows = rng.choice(len(w.binding_columns[0]), test_rows, replace=False)
+    test = [w.binding_columns[q][rows] for q in range(2)]
+    lits = workloads.random_literals(64, w.relations, 2, rng)
+    clauses = []
+    for i in range(3):
+        first = next(l for l in lits[8 * i:] if any(v < 0 for v in l.vars))
+        # the second literal joins on the column the first one introduced
+        tmpl = lits[40 + i]
+        jb = next(j for j, v in enumerate(tmpl.vars) if v >= 0)
+        second = Literal(tmpl.relation, tuple(2 if j == jb else v for j, v in enumerate(tmpl.vars)))
+        clauses.append([first, second])
+    dtest = [torch.from_numpy(c).to(dev) for c in test]
+    left = eng.run_test(clauses, dtest)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        left = eng.run_test(clauses, dtest)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    line = {"metric": "test rows checked/s (learnt clauses on a test table)",
+            "value": test_rows / dt, "unit": "rows/s", "ms": dt * 1e3, "test_rows": test_rows,
+            "clauses": [[(l.relation, list(l.vars)) for l in c] for c in clauses],
+            "uncovered": left}
+    if not no_cpu:
+        t0 = time.perf_counter()
+        want = oracle.run_test(w.relations, [[(l.relation, l.vars) for l in c] for c in clauses],
+                               test)
+        cdt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": test_rows / cdt, "unit": "rows/s", "cores": 1,
+                                "kind": "port", "sample": f"the same test table ({cdt:.1f} s)"}
+        line["uncovered_equal_oracle"] = len(want[0]) == left
+    return line
 
 
 def main():

@@ -95,7 +95,9 @@ __global__ void inline_keyset_insert_kernel(KeyCols keys, int64_t n,
     }
     uint32_t slot = hash64(v) & mask;
     for (uint32_t p = 0; p <= mask; ++p) {
-      const unsigned long long o = atomicCAS(&table[slot], kEmpty64, v);
+      unsigned long long o = table[slot];  // an occupied slot never changes
+      if (o == v) break;
+      if (o == kEmpty64) o = atomicCAS(&table[slot], kEmpty64, v);
       if (o == kEmpty64) atomicAdd(&table[(size_t)mask + 2], 1ull);
       if (o == kEmpty64 || o == v) break;
       slot = (slot + 1) & mask;
@@ -212,7 +214,8 @@ __global__ void inline_example_insert_kernel(KeyCols keys, int64_t n,
     }
     uint32_t slot = hash64(v) & mask;
     for (uint32_t p = 0; p <= mask; ++p) {
-      const unsigned long long o = atomicCAS(&table[slot], kEmpty64, v);
+      unsigned long long o = table[slot];  // an occupied slot never changes
+      if (o == kEmpty64) o = atomicCAS(&table[slot], kEmpty64, v);
       if (o == kEmpty64 || o == v) break;
       slot = (slot + 1) & mask;
     }

@@ -83,24 +83,30 @@ struct ExtendArgs {
   int32_t* out;            // (nc + nu) columns of out_rows
 };
 
-__global__ void extend_write_kernel(ExtendArgs a, int64_t n_probe, const int32_t* __restrict__ prep,
+// One thread per output row (a probe row matching a key of many build rows
+// would otherwise write them all alone): output row o belongs to the last
+// probe row i with pos[i] <= o (pos is the exclusive scan of the match
+// counts, so that row has a match left), and is its (o - pos[i])-th match.
+__global__ void extend_write_kernel(ExtendArgs a, int64_t n_probe, int64_t produced,
+                                    const int32_t* __restrict__ prep,
                                     const uint32_t* __restrict__ pos,
-                                    const int32_t* __restrict__ seg_first,
                                     const int32_t* __restrict__ seg_last,
                                     const int32_t* __restrict__ sorted_rows) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_probe;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t r = prep[i];
-    if (r < 0) continue;
-    int64_t o = a.out_base + pos[i];
-    // The build segment in descending row order = the reference's chain order.
-    for (int32_t s = seg_last[r]; s >= seg_first[r]; --s, ++o) {
-      const int32_t brow = sorted_rows[s];
-      const int64_t b = a.label_lo + (a.relation_is_probe ? (int64_t)brow : i);
-      const int64_t rr = a.relation_is_probe ? i : (int64_t)brow;
-      for (int c = 0; c < a.nc; ++c) a.out[(int64_t)c * a.out_rows + o] = a.bind_cols[c][b];
-      for (int u = 0; u < a.nu; ++u) a.out[(int64_t)(a.nc + u) * a.out_rows + o] = a.unbound[u][rr];
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < produced;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = n_probe - 1;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) >> 1;
+      if ((int64_t)pos[mid] <= k) lo = mid; else hi = mid - 1;
     }
+    const int64_t i = lo;
+    // The build segment in descending row order = the reference's chain order.
+    const int32_t brow = sorted_rows[seg_last[prep[i]] - (int32_t)(k - (int64_t)pos[i])];
+    const int64_t b = a.label_lo + (a.relation_is_probe ? (int64_t)brow : i);
+    const int64_t rr = a.relation_is_probe ? i : (int64_t)brow;
+    const int64_t o = a.out_base + k;
+    for (int c = 0; c < a.nc; ++c) a.out[(int64_t)c * a.out_rows + o] = a.bind_cols[c][b];
+    for (int u = 0; u < a.nu; ++u) a.out[(int64_t)(a.nc + u) * a.out_rows + o] = a.unbound[u][rr];
   }
 }
 
@@ -195,8 +201,8 @@ int extend_label(Ctx* ctx, const KeyCols& build, int64_t n_build, const KeyCols&
     return set_error(ctx, QFG_ERR_MISMATCH,
                      "extension produced " + std::to_string(produced) + " rows for a label, " +
                          std::to_string(expected) + " announced");
-  extend_write_kernel<<<rows_grid(ctx, n_probe), 256, 0, ctx->stream>>>(
-      args, n_probe, prep, cnt, seg_first, seg_last, srow);
+  extend_write_kernel<<<rows_grid(ctx, (int64_t)produced), 256, 0, ctx->stream>>>(
+      args, n_probe, (int64_t)produced, prep, cnt, seg_last, srow);
   QFG_LAUNCHED(ctx);
   // The next label reuses (and may regrow) the same scratch.
   QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

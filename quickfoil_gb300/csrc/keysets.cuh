@@ -53,7 +53,10 @@ __device__ __forceinline__ int32_t keyset_insert(const KeyCols& build, int32_t* 
                                                  uint32_t mask, int64_t r) {
   uint32_t slot = keys_hash<NK>(build, r) & mask;
   for (uint32_t probe = 0; probe <= mask; ++probe) {
-    const int32_t o = atomicCAS(&owner[slot], -1, (int32_t)r);
+    // A slot only ever goes from free to owned: a plain read that sees an
+    // owner is final, and repeated keys then spare the slot's atomics.
+    int32_t o = owner[slot];
+    if (o == -1) o = atomicCAS(&owner[slot], -1, (int32_t)r);
     if (o == -1) return (int32_t)r;
     if (keys_eq<NK>(build, o, build, r)) return o;
     slot = (slot + 1) & mask;

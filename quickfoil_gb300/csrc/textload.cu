@@ -168,8 +168,12 @@ int parse_text_device(Ctx* ctx, qfg_ctx* c, const uint8_t* text, int64_t n, int 
     if (skipped != nullptr && skipped[i] != 0) skip_mask |= 1ull << i;
     else ++kept;
   }
+  // Working memory in the context's grow-only scratch (nothing is allocated
+  // once a text of this size has been parsed): tile counts, newline
+  // positions, line-indexed columns, line bits; a host text is staged in
+  // TmpB.  The row compaction uses TmpA and the scan its own slot.
   const int64_t ntiles = (n + kTextTileBytes - 1) / kTextTileBytes;
-  DevBuf tiles;
+  DevBuf& tiles = ctx->scratch[kScrSortA];
   QFG_TRY(tiles.reserve(ctx, sizeof(uint32_t) * (size_t)(2 * ntiles + 1)));
   uint32_t* tile_count = tiles.as<uint32_t>();
   uint32_t* tile_first = tile_count + ntiles;
@@ -187,14 +191,18 @@ int parse_text_device(Ctx* ctx, qfg_ctx* c, const uint8_t* text, int64_t n, int 
   const int64_t num_lines = (int64_t)num_nl + (last != '\n' ? 1 : 0);
   if (num_lines > INT32_MAX)
     return set_error(ctx, QFG_ERR_INVALID, "qfg_parse_text: more than 2^31 - 1 lines");
-  DevBuf pos, colbuf, keep, err;
+  DevBuf& pos = ctx->scratch[kScrSortB];
+  DevBuf& colbuf = ctx->scratch[kScrJoin];
+  DevBuf& keep = ctx->scratch[kScrJoin2];
   QFG_TRY(pos.reserve(ctx, sizeof(int64_t) * (size_t)std::max<uint32_t>(num_nl, 1)));
   QFG_TRY(colbuf.reserve(ctx, sizeof(int32_t) * (size_t)std::max(kept, 1) * (size_t)num_lines));
   const int64_t nwords = (num_lines + 31) / 32 + 2;  // 64-bit blocks for the compaction
-  QFG_TRY(keep.reserve(ctx, sizeof(uint32_t) * (size_t)(nwords + 1)));
-  QFG_TRY(err.reserve(ctx, sizeof(unsigned long long)));
+  // line bits, then the error word (8-byte aligned)
+  const size_t err_off = ((sizeof(uint32_t) * (size_t)(nwords + 1)) + 7) & ~(size_t)7;
+  QFG_TRY(keep.reserve(ctx, err_off + sizeof(unsigned long long)));
+  unsigned long long* err_word = reinterpret_cast<unsigned long long*>(keep.as<char>() + err_off);
   QFG_CUDA(ctx, cudaMemsetAsync(keep.ptr(), 0, sizeof(uint32_t) * (size_t)(nwords + 1), ctx->stream));
-  QFG_CUDA(ctx, cudaMemsetAsync(err.ptr(), 0xff, sizeof(unsigned long long), ctx->stream));
+  QFG_CUDA(ctx, cudaMemsetAsync(err_word, 0xff, sizeof(unsigned long long), ctx->stream));
   if (num_nl > 0) {
     text_newlines_kernel<1><<<grid, kTextThreads, 0, ctx->stream>>>(text, n, ntiles, nullptr,
                                                                     tile_first, pos.as<int64_t>());
@@ -210,13 +218,13 @@ int parse_text_device(Ctx* ctx, qfg_ctx* c, const uint8_t* text, int64_t n, int 
   pa.skipped = skip_mask;
   pa.cols = colbuf.as<int32_t>();
   pa.keep_words = keep.as<uint32_t>();
-  pa.error = err.as<unsigned long long>();
+  pa.error = err_word;
   const unsigned pgrid = (unsigned)std::max<int64_t>(
       1, std::min<int64_t>((num_lines + kTextThreads - 1) / kTextThreads, (int64_t)ctx->num_sms * 8));
   text_parse_kernel<<<pgrid, kTextThreads, 0, ctx->stream>>>(pa);
   QFG_LAUNCHED(ctx);
   unsigned long long e = 0;
-  QFG_CUDA(ctx, cudaMemcpyAsync(&e, err.ptr(), sizeof(e), cudaMemcpyDeviceToHost, ctx->stream));
+  QFG_CUDA(ctx, cudaMemcpyAsync(&e, err_word, sizeof(e), cudaMemcpyDeviceToHost, ctx->stream));
   QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (e != ~0ull) {
     const int64_t line = (int64_t)(e >> 2) + 1;
@@ -267,8 +275,8 @@ extern "C" int qfg_parse_text(qfg_ctx* c, const char* text, int64_t num_bytes, i
   if (kept > 0 && capacity > 0 && d_out_columns == nullptr)
     return set_error(ctx, QFG_ERR_INVALID, "qfg_parse_text: no output columns");
   const uint8_t* dtext = reinterpret_cast<const uint8_t*>(text);
-  DevBuf staged;
   if (flags == QFG_HOST && num_bytes > 0) {
+    DevBuf& staged = ctx->scratch[kScrTmpB];
     QFG_TRY(staged.reserve(ctx, (size_t)num_bytes));
     QFG_CUDA(ctx, cudaMemcpyAsync(staged.ptr(), text, (size_t)num_bytes, cudaMemcpyHostToDevice,
                                   ctx->stream));

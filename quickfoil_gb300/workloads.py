@@ -242,3 +242,42 @@ def bongard(seed: int = 1, pictures: int = 300, mean_objects: float = 10.0,
     target = np.array(positives + negatives, dtype=np.int32)
     return LearnTask("bongard", relations, ["element", "circle", "triangle", "square", "inside"],
                      [target], len(positives), max_clause_length)
+
+
+def facts_text(columns) -> bytes:
+    """int32 columns as '|'-delimited lines, one fact a line (the fact-file
+    format of the reference's loader), built with numpy: every value's
+    decimal digits are written at offsets from a prefix sum of the field
+    widths."""
+    cols = [np.asarray(c, dtype=np.int64) for c in columns]
+    n = len(cols[0]) if cols else 0
+    if n == 0:
+        return b""
+    widths = []
+    for c in cols:
+        mag = np.abs(c)
+        digits = np.ones(n, dtype=np.int64)
+        t = mag // 10
+        while t.any():
+            digits += t > 0
+            t //= 10
+        widths.append(digits + (c < 0))
+    line_len = sum(widths) + len(cols)  # separators and the newline
+    start = np.concatenate([[0], np.cumsum(line_len)[:-1]])
+    out = np.empty(int(line_len.sum()), dtype=np.uint8)
+    pos = start.copy()
+    for q, (c, w) in enumerate(zip(cols, widths)):
+        neg = c < 0
+        out[pos[neg]] = ord("-")
+        mag = np.abs(c)
+        end = pos + w  # one past the last digit
+        k = 0
+        while True:
+            live = w - neg > k
+            if not live.any():
+                break
+            out[end[live] - 1 - k] = (ord("0") + (mag[live] // 10 ** k) % 10).astype(np.uint8)
+            k += 1
+        out[end] = ord("|") if q + 1 < len(cols) else ord("\n")
+        pos = end + 1
+    return out.tobytes()
