@@ -42,6 +42,59 @@ enum : unsigned long long {
   kTextOutOfRange = 3,
 };
 
+// Newline bytes of a 32-bit word: bit 7 of each byte set where it is '\n'
+// (the classic zero-byte test on word ^ 0x0a0a0a0a, exact for every byte).
+__device__ __forceinline__ uint32_t newline_bytes(uint32_t w) {
+  const uint32_t x = w ^ 0x0a0a0a0au;
+  return ~(((x & 0x7f7f7f7fu) + 0x7f7f7f7fu) | x | 0x7f7f7f7fu);
+}
+
+// The same two passes with one 16-byte load a thread (the text's start
+// 16-byte aligned): thread t owns bytes [16 t, 16 t + 16) of the tile, a
+// block scan of the threads' newline counts orders the positions.
+template <int PASS>
+__global__ void __launch_bounds__(kTextThreads)
+text_newlines16_kernel(const uint8_t* __restrict__ text, int64_t n, int64_t ntiles,
+                       uint32_t* __restrict__ tile_count, const uint32_t* __restrict__ tile_first,
+                       int64_t* __restrict__ nl_pos) {
+  __shared__ uint32_t warp_nl[kTextThreads / 32];
+  const int lane = lane_id(), warp = threadIdx.x / 32;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t p0 = tile * kTextTileBytes + 16 * (int64_t)threadIdx.x;
+    uint32_t m[4] = {0u, 0u, 0u, 0u};
+    if (p0 + 16 <= n) {
+      const uint4 v = *reinterpret_cast<const uint4*>(text + p0);
+      m[0] = newline_bytes(v.x);
+      m[1] = newline_bytes(v.y);
+      m[2] = newline_bytes(v.z);
+      m[3] = newline_bytes(v.w);
+    } else {
+      for (int b = 0; b < 16 && p0 + b < n; ++b)
+        if (text[p0 + b] == '\n') m[b >> 2] |= 0x80u << (8 * (b & 3));
+    }
+    const uint32_t mine = __popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3]);
+    uint32_t incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(kFullMask, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_nl[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < kTextThreads / 32; ++w) {
+      if (w < warp) before += warp_nl[w];
+      total += warp_nl[w];
+    }
+    if (PASS == 1 && mine != 0) {
+      uint32_t idx = tile_first[tile] + before + incl - mine;
+      for (int q = 0; q < 4; ++q)
+        for (uint32_t b = m[q]; b != 0; b &= b - 1) nl_pos[idx++] = p0 + 4 * q + ((__ffs(b) - 1) >> 3);
+    }
+    if (PASS == 0 && threadIdx.x == 0) tile_count[tile] = total;
+    __syncthreads();
+  }
+}
+
 // pass 0: newlines per tile -> tile_count; pass 1: newline positions, the
 // tile's first newline index read from tile_first.
 template <int PASS>
@@ -79,20 +132,22 @@ __device__ __forceinline__ bool c_space(uint8_t c) {
 }
 
 // std::stoi on text[s, e): 0 and the value, or an error code.
-__device__ __forceinline__ unsigned long long parse_int(const uint8_t* __restrict__ text, int64_t s,
+__device__ __forceinline__ unsigned long long parse_int(const uint8_t* __restrict__ t, int64_t s,
                                                         int64_t e, int32_t* out) {
-  while (s < e && c_space(text[s])) ++s;
+  while (s < e && c_space(__ldg(t + s))) ++s;
   bool neg = false;
-  if (s < e && (text[s] == '+' || text[s] == '-')) {
-    neg = text[s] == '-';
+  if (s < e && (__ldg(t + s) == '+' || __ldg(t + s) == '-')) {
+    neg = __ldg(t + s) == '-';
     ++s;
   }
-  if (s >= e || text[s] < '0' || text[s] > '9') return kTextNoDigits;
+  if (s >= e || __ldg(t + s) < '0' || __ldg(t + s) > '9') return kTextNoDigits;
   unsigned long long v = 0;
   bool over = false;
-  for (; s < e && text[s] >= '0' && text[s] <= '9'; ++s) {
+  for (; s < e; ++s) {
+    const uint8_t c = __ldg(t + s);
+    if (c < '0' || c > '9') break;
     if (!over) {
-      v = v * 10 + (text[s] - '0');
+      v = v * 10 + (c - '0');
       over = v > 2147483648ull;
     }
   }
@@ -124,27 +179,28 @@ __global__ void __launch_bounds__(kTextThreads) text_parse_kernel(ParseArgs a) {
     if (i < a.num_lines) {
       const int64_t s = i == 0 ? 0 : a.nl_pos[i - 1] + 1;
       const int64_t e = i < a.num_nl ? a.nl_pos[i] : a.n;
-      if (e > s && a.text[s] != '#') {
+      const uint8_t* t = a.text;
+      if (e > s && __ldg(t + s) != '#') {
         keep = true;
         unsigned long long err = 0;
+        // the field count is checked before any field is converted
+        int nf = 1;
+        for (int64_t p = s; p < e; ++p) nf += __ldg(t + p) == '|';
+        if (nf != a.num_args) err = kTextBadFieldCount;
         int field = 0, col = 0;
         int64_t fs = s;
         for (int64_t p = s; p <= e && err == 0; ++p) {
-          if (p < e && a.text[p] != '|') continue;
+          if (p < e && __ldg(t + p) != '|') continue;
           // field [fs, p)
-          if (field < a.num_args && !((a.skipped >> field) & 1ull)) {
+          if (!((a.skipped >> field) & 1ull)) {
             int32_t v = 0;
-            err = parse_int(a.text, fs, p, &v);
+            err = parse_int(t, fs, p, &v);
             if (err == 0) a.cols[(int64_t)col * a.num_lines + i] = v;
             ++col;
           }
           ++field;
           fs = p + 1;
         }
-        // the field count is checked before any field is converted
-        int nf = 1;
-        for (int64_t p = s; p < e; ++p) nf += a.text[p] == '|';
-        if (nf != a.num_args) err = kTextBadFieldCount;
         if (err != 0) atomicMin(a.error, ((unsigned long long)i << 2) | err);
       }
     }
@@ -179,8 +235,13 @@ int parse_text_device(Ctx* ctx, qfg_ctx* c, const uint8_t* text, int64_t n, int 
   uint32_t* tile_first = tile_count + ntiles;
   uint32_t* total = tile_first + ntiles;
   const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->num_sms * 8));
-  text_newlines_kernel<0><<<grid, kTextThreads, 0, ctx->stream>>>(text, n, ntiles, tile_count,
-                                                                  nullptr, nullptr);
+  const bool aligned16 = ((uintptr_t)text & 15) == 0;
+  if (aligned16)
+    text_newlines16_kernel<0><<<grid, kTextThreads, 0, ctx->stream>>>(text, n, ntiles, tile_count,
+                                                                      nullptr, nullptr);
+  else
+    text_newlines_kernel<0><<<grid, kTextThreads, 0, ctx->stream>>>(text, n, ntiles, tile_count,
+                                                                    nullptr, nullptr);
   QFG_LAUNCHED(ctx);
   QFG_TRY(exclusive_scan_u32(ctx, tile_count, tile_first, ntiles, total));
   uint32_t num_nl = 0;
@@ -204,8 +265,12 @@ int parse_text_device(Ctx* ctx, qfg_ctx* c, const uint8_t* text, int64_t n, int 
   QFG_CUDA(ctx, cudaMemsetAsync(keep.ptr(), 0, sizeof(uint32_t) * (size_t)(nwords + 1), ctx->stream));
   QFG_CUDA(ctx, cudaMemsetAsync(err_word, 0xff, sizeof(unsigned long long), ctx->stream));
   if (num_nl > 0) {
-    text_newlines_kernel<1><<<grid, kTextThreads, 0, ctx->stream>>>(text, n, ntiles, nullptr,
-                                                                    tile_first, pos.as<int64_t>());
+    if (aligned16)
+      text_newlines16_kernel<1><<<grid, kTextThreads, 0, ctx->stream>>>(
+          text, n, ntiles, nullptr, tile_first, pos.as<int64_t>());
+    else
+      text_newlines_kernel<1><<<grid, kTextThreads, 0, ctx->stream>>>(
+          text, n, ntiles, nullptr, tile_first, pos.as<int64_t>());
     QFG_LAUNCHED(ctx);
   }
   ParseArgs pa;

@@ -72,3 +72,19 @@ def test_relation_from_text_evaluates_like_the_parsed_columns(engine):
                            [(l.relation - base, l.vars, l.join_pos) for l in lits], bits=5)
     np.testing.assert_array_equal(got, want)
     b.close()
+
+
+@pytest.mark.parametrize("offset", [1, 2, 3, 5])
+def test_loader_on_device_text_at_any_byte_offset(engine, offset):
+    """A device text that does not start on a 4- or 16-byte boundary (a view
+    into a larger buffer): the byte-wise passes and the cursor's partial
+    words give the same columns."""
+    rng = np.random.default_rng(offset)
+    vals = rng.integers(-2 ** 31, 2 ** 31, (50_001, 3))
+    text = b"\n".join(b"%d|%d|%d" % tuple(r) for r in vals) + b"\n#end"
+    buf = torch.from_numpy(np.frombuffer(b"\n" * offset + text, dtype=np.uint8).copy()).cuda()
+    view = buf[offset:]
+    assert view.data_ptr() % 4 != 0 or offset % 4 == 0
+    got = engine.parse_text(view, 3)
+    for g, w in zip(got, oracle.parse_text(text, 3)):
+        np.testing.assert_array_equal(g.cpu().numpy(), w)
