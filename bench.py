@@ -32,6 +32,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -97,8 +98,11 @@ class ClockSampler:
 
     def start(self):
         try:
-            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-            self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+            # The samples go to a temporary file; the JSON line carries their
+            # summary.  QF_CLOCKS_DIR keeps the raw samples elsewhere.
+            out_dir = os.environ.get("QF_CLOCKS_DIR") or tempfile.gettempdir()
+            os.makedirs(out_dir, exist_ok=True)
+            self.path = os.path.join(out_dir, f"clocks_{os.getpid()}.csv")
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
