@@ -288,3 +288,24 @@ def test_coverage_with_and_without_the_relation_filter(engine, arity, distinct):
         got = _gpu_coverage(engine, [rel], B, n // 3, lit, 2, U, U, prepared=prepared)
         assert got[0] == want[0]
         np.testing.assert_array_equal(got[1], bits_to_flags(want[1], len(U[0])))
+
+
+def test_coverage_on_a_split_binding_set(engine):
+    """Positives and negatives uploaded from separate arrays
+    (qfg_bindings_create_split) give the same coverage as one table."""
+    rng = np.random.default_rng(44)
+    rel = [rng.integers(0, 80, 3000).astype(np.int32) for _ in range(2)]
+    P, N = 7001, 12003
+    B = [rng.integers(0, 80, P + N).astype(np.int32) for _ in range(3)]
+    U = [rng.integers(0, 80, 2500).astype(np.int32) for _ in range(2)]
+    base = _register(engine, [rel])
+    lit = Literal(base, (2, -1))
+    whole = engine.bindings([dev(c) for c in B], P)
+    split = engine.bindings_split([dev(c[:P]) for c in B], [dev(c[P:]) for c in B])
+    a = engine.coverage(whole, lit, 2, [dev(c) for c in U], [dev(c) for c in U])
+    b = engine.coverage(split, lit, 2, [dev(c) for c in U], [dev(c) for c in U])
+    want = oracle.coverage(B, P, rel, lit.as_tuple(), 2, U, U)
+    assert a[0] == b[0] == want[0]
+    assert torch.equal(a[1], b[1])
+    whole.close()
+    split.close()

@@ -88,3 +88,16 @@ def test_loader_on_device_text_at_any_byte_offset(engine, offset):
     got = engine.parse_text(view, 3)
     for g, w in zip(got, oracle.parse_text(text, 3)):
         np.testing.assert_array_equal(g.cpu().numpy(), w)
+
+
+def test_relation_from_text_with_a_skipped_argument(engine):
+    text = b"# name|id|parent\nann|1|7\nbob|2|7\n\ncid|3|1\n"
+    rid = 1_600_000
+    assert engine.register_relation_text(rid, text, 3, [1, 0, 0]) == 3
+    b = engine.bindings([np.array([7, 1, 9, 2], np.int32), np.array([1, 3, 3, 2], np.int32)], 2)
+    got = engine.evaluate_step(b, [Literal(rid, (-1, 0)), Literal(rid, (1, 0))])
+    want = oracle.evaluate([[np.array([1, 2, 3], np.int32), np.array([7, 7, 1], np.int32)]],
+                           [np.array([7, 1, 9, 2], np.int32), np.array([1, 3, 3, 2], np.int32)], 2,
+                           [(0, (-1, 0), 1), (0, (1, 0), 0)], bits=5)
+    np.testing.assert_array_equal(got, want)
+    b.close()
