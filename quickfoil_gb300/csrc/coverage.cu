@@ -17,7 +17,10 @@
 // row-owner form of keysets.cuh.  A relation with at most 2^18 distinct key
 // tuples also gets a 2^20-bit filter (a bit per hashed tuple, 128 KiB) that
 // every block keeps in shared memory: most binding rows fail it and never
-// touch L2, so the pass streams the binding columns at HBM speed.
+// touch L2, so the pass streams the binding columns at HBM speed.  Larger
+// relations, and the example tables, get filters of about 8 bits a tuple in
+// global memory, small enough to stay in L2: a row then costs one random L2
+// read instead of a DRAM miss in a key set of tens of megabytes.
 //
 // The second semi-join is built on the smaller of its two sides:
 //  * examples (usually: a few million examples against tens of millions of
@@ -109,19 +112,26 @@ constexpr int kFilterBits = 20;                         // 2^20-bit filter, 128 
 constexpr int kFilterWords = (1 << kFilterBits) / 32;
 constexpr int64_t kFilterMaxKeys = int64_t(1) << 18;    // false positives below 23%
 
-// Filter bit of a key tuple: a multiplicative hash (two multiplies), cheap
-// enough for every binding row; independent of the key set's slot hash.
-__device__ __forceinline__ uint32_t filter_bit(unsigned long long v) {
-  return (((uint32_t)v * 0x9e3779b1u) ^ ((uint32_t)(v >> 32) * 0x85ebca77u)) >> (32 - kFilterBits);
+// Filter bit of a key tuple among 2^bits: a multiplicative hash (two
+// multiplies), cheap enough for every binding row; independent of the key
+// set's slot hash.
+__device__ __forceinline__ uint32_t filter_bit(unsigned long long v, int bits = kFilterBits) {
+  return (((uint32_t)v * 0x9e3779b1u) ^ ((uint32_t)(v >> 32) * 0x85ebca77u)) >> (32 - bits);
 }
 
+// A relation with more distinct tuples than the shared-memory filter takes
+// gets a filter of about 8 bits per tuple in global memory (at most 2^28
+// bits): small enough to stay in L2, so most binding rows whose key is not
+// in the relation skip the key set's (larger, DRAM-resident) slots.
+constexpr int kMaxGlobalFilterBits = 28;
+
 __global__ void filter_build_kernel(const unsigned long long* __restrict__ table, uint32_t mask,
-                                    uint32_t* __restrict__ filter) {
+                                    uint32_t* __restrict__ filter, int bits) {
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s <= (int64_t)mask;
        s += (int64_t)gridDim.x * blockDim.x) {
     const unsigned long long t = table[s];
     if (t == kEmpty64) continue;
-    const uint32_t b = filter_bit(t);
+    const uint32_t b = filter_bit(t, bits);
     atomicOr(&filter[b >> 5], 1u << (b & 31));
   }
 }
@@ -146,8 +156,17 @@ struct RelSet {
   const int32_t* owner;             // owner form
   uint32_t mask;
   KeyCols keys;                     // the relation's bound-argument columns
-  const uint32_t* filter;           // hashed-bit filter (inline form), or null
+  const uint32_t* filter;           // hashed-bit filter for shared memory (inline form), or null
+  const uint32_t* gfilter;          // larger filter read from global memory, or null
+  int gbits;
 };
+
+// The global filter's verdict on a key tuple (true when there is none).
+__device__ __forceinline__ bool gfilter_pass(const RelSet& rs, unsigned long long v) {
+  if (rs.gfilter == nullptr) return true;
+  const uint32_t b = filter_bit(v, rs.gbits);
+  return (__ldg(rs.gfilter + (b >> 5)) >> (b & 31)) & 1u;
+}
 
 // NB: bound-argument count, 1-3 fixed, 0 = 4 or more (run time).
 template <int NB>
@@ -186,6 +205,11 @@ struct ExSet {
   uint32_t mask;
   const int32_t* rep;
   uint8_t* flag;
+  // Inline form: a filter of the example tuples (about 8 bits each, in
+  // global memory small enough for L2), so most passing binding rows whose
+  // tuple is no example skip the table's slots.
+  const uint32_t* efilter;
+  int ebits;
 };
 
 // Marks the example tuple of binding row r (target columns) as covered.
@@ -193,11 +217,29 @@ template <int K>
 __device__ __forceinline__ void ex_mark(const ExSet& e, const KeyCols& target, int64_t r) {
   if constexpr (K == 1 || K == 2) {
     const unsigned long long v = inline_key<K>(target, r);
+    if (v != kEmpty64) {
+      const uint32_t b = filter_bit(v, e.ebits);
+      if (!((__ldg(e.efilter + (b >> 5)) >> (b & 31)) & 1u)) return;
+    }
     const int64_t s = v == kEmpty64 ? (int64_t)e.mask + 1 : inline_keyset_slot(e.table, e.mask, v);
     if (s >= 0 && e.flag[s] == 0) e.flag[s] = 1;
   } else {
     const int32_t o = keyset_find<K>(e.keys, e.owner, e.mask, target, r);
     if (o >= 0 && e.flag[o] == 0) e.flag[o] = 1;
+  }
+}
+
+// The example tuples' filter bits (the (-1, -1) tuple has its own flag and
+// is never filtered).
+template <int K>
+__global__ void example_filter_kernel(KeyCols keys, int64_t n, uint32_t* __restrict__ filter,
+                                      int bits) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long v = inline_key<K>(keys, i);
+    if (v == kEmpty64) continue;
+    const uint32_t b = filter_bit(v, bits);
+    atomicOr(&filter[b >> 5], 1u << (b & 31));
   }
 }
 
@@ -280,6 +322,8 @@ coverage_scan_kernel(RelSet rs, KeyCols bound, KeyCols target, int64_t n, ExSet 
           const uint32_t b = filter_bit(v[u]);
           maybe[u] = (sfilter[b >> 5] >> (b & 31)) & 1u;
         }
+      } else {
+        if (maybe[u] && v[u] != kEmpty64) maybe[u] = gfilter_pass(rs, v[u]);
       }
       t[u] = maybe[u] && v[u] != kEmpty64 ? rs.table[hash64(v[u]) & rs.mask] : kEmpty64;
     }
@@ -310,6 +354,8 @@ __device__ __forceinline__ bool scan1_test(const RelSet& rs, const uint32_t* sfi
   if constexpr (FILTERED) {
     const uint32_t b = filter_bit(v);
     if (!((sfilter[b >> 5] >> (b & 31)) & 1u)) return false;
+  } else {
+    if (!gfilter_pass(rs, v)) return false;
   }
   return inline_keyset_probe(rs.table, rs.mask, v, hash64(v) & rs.mask);
 }
@@ -622,8 +668,19 @@ int relation_key_set(Ctx* ctx, Relation* rel, const std::vector<int>& args, cons
         QFG_CUDA(ctx, cudaMemsetAsync(fresh->filter.ptr(), 0, sizeof(uint32_t) * kFilterWords,
                                       ctx->stream));
         filter_build_kernel<<<rows_grid(ctx, (int64_t)slots), 256, 0, ctx->stream>>>(
-            t, fresh->mask, fresh->filter.as<uint32_t>());
+            t, fresh->mask, fresh->filter.as<uint32_t>(), kFilterBits);
         QFG_LAUNCHED(ctx);
+      } else {
+        int gb = kFilterBits + 1;
+        while (gb < kMaxGlobalFilterBits && ((int64_t)1 << gb) < 8 * fresh->distinct) ++gb;
+        const size_t words = ((size_t)1 << gb) / 32;
+        QFG_TRY(fresh->gfilter.reserve(ctx, sizeof(uint32_t) * words));
+        QFG_CUDA(ctx, cudaMemsetAsync(fresh->gfilter.ptr(), 0, sizeof(uint32_t) * words,
+                                      ctx->stream));
+        filter_build_kernel<<<rows_grid(ctx, (int64_t)slots), 256, 0, ctx->stream>>>(
+            t, fresh->mask, fresh->gfilter.as<uint32_t>(), gb);
+        QFG_LAUNCHED(ctx);
+        fresh->gbits = gb;
       }
     } else {
       QFG_TRY(fresh->owner.reserve(ctx, sizeof(int32_t) * slots));
@@ -638,6 +695,8 @@ int relation_key_set(Ctx* ctx, Relation* rel, const std::vector<int>& args, cons
   out->mask = ks->mask;
   out->keys = keys;
   out->filter = ks->filter.bytes() > 0 ? ks->filter.as<uint32_t>() : nullptr;
+  out->gfilter = ks->gbits > 0 ? ks->gfilter.as<uint32_t>() : nullptr;
+  out->gbits = ks->gbits;
   out->table = inline_form ? ks->owner.as<unsigned long long>() : nullptr;
   out->owner = inline_form ? nullptr : ks->owner.as<int32_t>();
   return QFG_OK;
@@ -658,10 +717,24 @@ size_t example_flag_bytes(int k, int64_t n, uint32_t mask) {
   return inline_examples(k) ? (size_t)mask + 2 : (size_t)n;
 }
 
-size_t example_set_bytes(int k, int64_t n, uint32_t mask) {
+// Bits (log2) of an inline example table's filter: about 8 a tuple.
+int example_filter_bits(int64_t n) {
+  int b = kFilterBits;
+  while (b < kMaxGlobalFilterBits && ((int64_t)1 << b) < 8 * n) ++b;
+  return b;
+}
+
+// Layout at `mem`: slots, representative per example, flags, then (inline
+// form) the filter at the next 16-byte boundary.
+size_t example_filter_offset(int k, int64_t n, uint32_t mask) {
   const size_t slot = inline_examples(k) ? sizeof(unsigned long long) : sizeof(int32_t);
-  return (slot * ((size_t)mask + 1) + sizeof(int32_t) * (size_t)n +
-          example_flag_bytes(k, n, mask) + 255) & ~(size_t)255;
+  return (slot * ((size_t)mask + 1) + sizeof(int32_t) * (size_t)n + example_flag_bytes(k, n, mask) +
+          15) & ~(size_t)15;
+}
+
+size_t example_set_bytes(int k, int64_t n, uint32_t mask) {
+  const size_t filter = inline_examples(k) ? ((size_t)1 << example_filter_bits(n)) / 8 : 0;
+  return (example_filter_offset(k, n, mask) + filter + 255) & ~(size_t)255;
 }
 
 ExSet example_view(const Examples& e) {
@@ -675,6 +748,10 @@ ExSet example_view(const Examples& e) {
       e.mem + (in ? sizeof(unsigned long long) : sizeof(int32_t)) * ((size_t)e.mask + 1));
   v.rep = rep;
   v.flag = reinterpret_cast<uint8_t*>(rep + e.n);
+  v.efilter = in ? reinterpret_cast<const uint32_t*>(
+                       e.mem + example_filter_offset(e.keys.nk, e.n, e.mask))
+                 : nullptr;
+  v.ebits = in ? example_filter_bits(e.n) : 0;
   return v;
 }
 
@@ -687,12 +764,17 @@ int build_example_set(Ctx* ctx, Examples* e) {
     unsigned long long* table = const_cast<unsigned long long*>(v.table);
     QFG_CUDA(ctx, cudaMemsetAsync(table, 0xff, sizeof(unsigned long long) * ((size_t)e->mask + 1),
                                   ctx->stream));
-    if (e->keys.nk == 1)
+    uint32_t* filter = const_cast<uint32_t*>(v.efilter);
+    QFG_CUDA(ctx, cudaMemsetAsync(filter, 0, ((size_t)1 << v.ebits) / 8, ctx->stream));
+    if (e->keys.nk == 1) {
       inline_example_insert_kernel<1><<<grid, 256, 0, ctx->stream>>>(e->keys, e->n, table,
                                                                       e->mask, rep);
-    else
+      example_filter_kernel<1><<<grid, 256, 0, ctx->stream>>>(e->keys, e->n, filter, v.ebits);
+    } else {
       inline_example_insert_kernel<2><<<grid, 256, 0, ctx->stream>>>(e->keys, e->n, table,
                                                                       e->mask, rep);
+      example_filter_kernel<2><<<grid, 256, 0, ctx->stream>>>(e->keys, e->n, filter, v.ebits);
+    }
   } else {
     int32_t* owner = const_cast<int32_t*>(v.owner);
     QFG_CUDA(ctx, cudaMemsetAsync(owner, 0xff, sizeof(int32_t) * ((size_t)e->mask + 1),

@@ -130,6 +130,8 @@ struct KeySet {
   DevBuf owner;
   int64_t distinct = 0;  // distinct key tuples (inline form)
   DevBuf filter;         // hashed-bit filter of the key tuples, or empty
+  int gbits = 0;         // bits (log2) of the larger filter kept in global memory, or 0
+  DevBuf gfilter;
 };
 
 struct Relation {
