@@ -14,9 +14,10 @@
 // newlines of every tile (256 threads read the tile's bytes coalesced, one
 // ballot per 256 bytes), an exclusive scan of the tile counts gives each
 // tile its first line, a second pass writes the position of every newline.
-// Then one thread per line parses its fields into line-indexed columns and
-// a ballot per 32 lines marks the data lines; the row compaction of
-// coverage.cu keeps those, in order.
+// Then one thread per line parses its fields into line-indexed columns in
+// one pass (32-bit offsets; the kernel is issue-bound, so the pass count and
+// the index width are what cost) and a ballot per 32 lines marks the data
+// lines; the row compaction of coverage.cu keeps those, in order.
 #include <cstring>
 #include <vector>
 
@@ -131,31 +132,6 @@ __device__ __forceinline__ bool c_space(uint8_t c) {
   return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r';
 }
 
-// std::stoi on text[s, e): 0 and the value, or an error code.
-__device__ __forceinline__ unsigned long long parse_int(const uint8_t* __restrict__ t, int64_t s,
-                                                        int64_t e, int32_t* out) {
-  while (s < e && c_space(__ldg(t + s))) ++s;
-  bool neg = false;
-  if (s < e && (__ldg(t + s) == '+' || __ldg(t + s) == '-')) {
-    neg = __ldg(t + s) == '-';
-    ++s;
-  }
-  if (s >= e || __ldg(t + s) < '0' || __ldg(t + s) > '9') return kTextNoDigits;
-  unsigned long long v = 0;
-  bool over = false;
-  for (; s < e; ++s) {
-    const uint8_t c = __ldg(t + s);
-    if (c < '0' || c > '9') break;
-    if (!over) {
-      v = v * 10 + (c - '0');
-      over = v > 2147483648ull;
-    }
-  }
-  if (over || (!neg && v > 2147483647ull)) return kTextOutOfRange;
-  *out = neg ? (int32_t)(-(long long)v) : (int32_t)v;
-  return 0;
-}
-
 struct ParseArgs {
   const uint8_t* text;
   int64_t n;
@@ -169,43 +145,67 @@ struct ParseArgs {
   unsigned long long* error;   // (line << 2 | code), atomicMin
 };
 
-// One thread per line (whole warps per 32 lines, for the ballot).
+// One thread per line (whole warps per 32 lines, for the ballot), one pass
+// over the line with 32-bit offsets: each kept field is converted where it
+// starts, every separator is counted, and a field count that differs wins
+// over a conversion error (the reference checks the count first).
 __global__ void __launch_bounds__(kTextThreads) text_parse_kernel(ParseArgs a) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int lane = lane_id();
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i - lane < a.num_lines;
-       i += stride) {
+  for (int64_t li = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; li - lane < a.num_lines;
+       li += stride) {
     bool keep = false;
-    if (i < a.num_lines) {
-      const int64_t s = i == 0 ? 0 : a.nl_pos[i - 1] + 1;
-      const int64_t e = i < a.num_nl ? a.nl_pos[i] : a.n;
-      const uint8_t* t = a.text;
-      if (e > s && __ldg(t + s) != '#') {
+    if (li < a.num_lines) {
+      const int64_t s = li == 0 ? 0 : a.nl_pos[li - 1] + 1;
+      const int64_t e = li < a.num_nl ? a.nl_pos[li] : a.n;
+      const uint8_t* __restrict__ lp = a.text + s;
+      const int len = (int)(e - s);
+      if (len > 0 && __ldg(lp) != '#') {
         keep = true;
         unsigned long long err = 0;
-        // the field count is checked before any field is converted
-        int nf = 1;
-        for (int64_t p = s; p < e; ++p) nf += __ldg(t + p) == '|';
-        if (nf != a.num_args) err = kTextBadFieldCount;
-        int field = 0, col = 0;
-        int64_t fs = s;
-        for (int64_t p = s; p <= e && err == 0; ++p) {
-          if (p < e && __ldg(t + p) != '|') continue;
-          // field [fs, p)
-          if (!((a.skipped >> field) & 1ull)) {
-            int32_t v = 0;
-            err = parse_int(t, fs, p, &v);
-            if (err == 0) a.cols[(int64_t)col * a.num_lines + i] = v;
+        int field = 0, col = 0, i = 0;
+        for (;;) {
+          if (field < a.num_args && !((a.skipped >> field) & 1ull)) {
+            if (err == 0) {
+              // std::stoi on the field starting at i
+              int j = i;
+              uint8_t c = j < len ? __ldg(lp + j) : 0;
+              while (j < len && c_space(c)) c = ++j < len ? __ldg(lp + j) : 0;
+              bool neg = false;
+              if (j < len && (c == '+' || c == '-')) {
+                neg = c == '-';
+                c = ++j < len ? __ldg(lp + j) : 0;
+              }
+              if (j >= len || c < '0' || c > '9') {
+                err = kTextNoDigits;
+              } else {
+                unsigned long long v = 0;
+                bool over = false;
+                while (j < len && c >= '0' && c <= '9') {
+                  if (!over) {
+                    v = v * 10 + (c - '0');
+                    over = v > 2147483648ull;
+                  }
+                  c = ++j < len ? __ldg(lp + j) : 0;
+                }
+                if (over || (!neg && v > 2147483647ull)) err = kTextOutOfRange;
+                else a.cols[(int64_t)col * a.num_lines + li] = neg ? (int32_t)(-(long long)v) : (int32_t)v;
+              }
+              i = j;
+            }
             ++col;
           }
+          while (i < len && __ldg(lp + i) != '|') ++i;
           ++field;
-          fs = p + 1;
+          if (i >= len) break;
+          ++i;
         }
-        if (err != 0) atomicMin(a.error, ((unsigned long long)i << 2) | err);
+        if (field != a.num_args) err = kTextBadFieldCount;
+        if (err != 0) atomicMin(a.error, ((unsigned long long)li << 2) | err);
       }
     }
     const unsigned ball = __ballot_sync(kFullMask, keep);
-    if (lane == 0 && i < a.num_lines + 32) a.keep_words[i >> 5] = ball;
+    if (lane == 0 && li < a.num_lines + 32) a.keep_words[li >> 5] = ball;
   }
 }
 
