@@ -22,6 +22,9 @@
 // matches walking its build segment from the end.  The side that is built on
 // follows the reference: the binding set when both label sides are smaller
 // than the relation (CollaborateJoin, :172-207), else the relation (:208-250).
+// The relation's build side (key set, sorted rows, segments) depends only on
+// the relation and the bound argument positions, so it is kept on the
+// relation for later extensions; a binding-set build side is built per call.
 #include <cstring>
 
 #include "keysets.cuh"
@@ -149,25 +152,26 @@ int semijoin(Ctx* ctx, const KeyCols& set_side, int64_t n_set, const KeyCols& bi
   return QFG_OK;
 }
 
-// One label of the extension: joins `probe` rows against `build` rows and
-// writes the matches in the reference's order at output rows
-// [out_base, out_base + expected).
-int extend_label(Ctx* ctx, const KeyCols& build, int64_t n_build, const KeyCols& probe,
-                 int64_t n_probe, int64_t expected, ExtendArgs args) {
-  if (n_build == 0 || n_probe == 0) {
-    return expected == 0 ? QFG_OK
-                         : set_error(ctx, QFG_ERR_MISMATCH, "extension produced 0 rows for a label");
-  }
-  const uint32_t mask = table_mask(n_build);
+// The build side of an extension: the key set of `build`, its rows sorted
+// stably by representative, each representative's segment.
+struct BuildView {
+  const int32_t* owner;
+  uint32_t mask;
+  const int32_t* sorted;
+  const int32_t* seg_first;
+  const int32_t* seg_last;
+};
+
+// Builds the view for `build` (n_build > 0) into `owner_mem` (mask + 1) and
+// `rows_mem` (3 * n_build: sorted rows, segment firsts, segment lasts).
+int build_side(Ctx* ctx, const KeyCols& build, int64_t n_build, uint32_t mask, int32_t* owner,
+               int32_t* rows_mem, BuildView* v) {
   const size_t cap = (size_t)mask + 1;
-  QFG_TRY(ctx->scratch[kScrJoin].reserve(ctx, sizeof(int32_t) * (cap + 3 * (size_t)n_build)));
-  int32_t* owner = ctx->scratch[kScrJoin].as<int32_t>();
-  int32_t* rep = owner + cap;
-  int32_t* seg_first = rep + n_build;
-  int32_t* seg_last = seg_first + n_build;
+  QFG_TRY(ctx->scratch[kScrJoin].reserve(ctx, sizeof(int32_t) * (size_t)n_build));
+  int32_t* rep = ctx->scratch[kScrJoin].as<int32_t>();
   QFG_CUDA(ctx, cudaMemsetAsync(owner, 0xff, sizeof(int32_t) * cap, ctx->stream));
   keyset_insert_kernel<0><<<rows_grid(ctx, n_build), 256, 0, ctx->stream>>>(build, n_build, owner,
-                                                                         mask, rep);
+                                                                            mask, rep);
   QFG_LAUNCHED(ctx);
   QFG_TRY(ctx->scratch[kScrSortA].reserve(ctx, 2 * sizeof(uint32_t) * (size_t)n_build));
   QFG_TRY(ctx->scratch[kScrSortB].reserve(ctx, 2 * sizeof(uint32_t) * (size_t)n_build));
@@ -182,15 +186,52 @@ int extend_label(Ctx* ctx, const KeyCols& build, int64_t n_build, const KeyCols&
   uint32_t* skey;
   int32_t* srow;
   QFG_TRY(sort_pairs_u32(ctx, k0, p0, k1, p1, n_build, bits, &skey, &srow));
+  int32_t* sorted = rows_mem;
+  int32_t* seg_first = rows_mem + n_build;
+  int32_t* seg_last = seg_first + n_build;
+  QFG_CUDA(ctx, cudaMemcpyAsync(sorted, srow, sizeof(int32_t) * (size_t)n_build,
+                                cudaMemcpyDeviceToDevice, ctx->stream));
   segments_kernel<<<rows_grid(ctx, n_build), 256, 0, ctx->stream>>>(skey, n_build, seg_first,
                                                                     seg_last);
   QFG_LAUNCHED(ctx);
+  *v = BuildView{owner, mask, sorted, seg_first, seg_last};
+  return QFG_OK;
+}
+
+// The relation's build side over the literal's bound argument positions,
+// built on first use and kept on the relation (its rows never change while
+// it is registered).
+int relation_build_side(Ctx* ctx, Relation* rel, const std::vector<int>& args,
+                        const KeyCols& keys, BuildView* v) {
+  auto it = rel->ext_builds.find(args);
+  if (it == rel->ext_builds.end()) {
+    auto eb = std::make_unique<ExtensionBuild>();
+    eb->mask = table_mask(rel->num_tuples);
+    QFG_TRY(eb->owner.reserve(ctx, sizeof(int32_t) * ((size_t)eb->mask + 1)));
+    QFG_TRY(eb->sorted.reserve(ctx, sizeof(int32_t) * 3 * (size_t)rel->num_tuples));
+    BuildView tmp;
+    QFG_TRY(build_side(ctx, keys, rel->num_tuples, eb->mask, eb->owner.as<int32_t>(),
+                       eb->sorted.as<int32_t>(), &tmp));
+    it = rel->ext_builds.emplace(args, std::move(eb)).first;
+  }
+  const ExtensionBuild& eb = *it->second;
+  const int32_t* base = eb.sorted.as<int32_t>();
+  *v = BuildView{eb.owner.as<int32_t>(), eb.mask, base, base + rel->num_tuples,
+                 base + 2 * rel->num_tuples};
+  return QFG_OK;
+}
+
+// One label of the extension: joins `probe` rows against the build side and
+// writes the matches in the reference's order at output rows
+// [out_base, out_base + expected).
+int probe_side(Ctx* ctx, const KeyCols& build, const BuildView& v, const KeyCols& probe,
+               int64_t n_probe, int64_t expected, ExtendArgs args) {
   QFG_TRY(ctx->scratch[kScrJoin2].reserve(ctx, sizeof(int32_t) * (2 * (size_t)n_probe + 2)));
   int32_t* prep = ctx->scratch[kScrJoin2].as<int32_t>();
   uint32_t* cnt = reinterpret_cast<uint32_t*>(prep + n_probe);
   uint32_t* total = cnt + n_probe;
   match_count_kernel<<<rows_grid(ctx, n_probe), 256, 0, ctx->stream>>>(
-      build, owner, mask, probe, n_probe, seg_first, seg_last, prep, cnt);
+      build, v.owner, v.mask, probe, n_probe, v.seg_first, v.seg_last, prep, cnt);
   QFG_LAUNCHED(ctx);
   QFG_TRY(exclusive_scan_u32(ctx, cnt, cnt, n_probe, total));
   uint32_t produced = 0;
@@ -202,11 +243,31 @@ int extend_label(Ctx* ctx, const KeyCols& build, int64_t n_build, const KeyCols&
                      "extension produced " + std::to_string(produced) + " rows for a label, " +
                          std::to_string(expected) + " announced");
   extend_write_kernel<<<rows_grid(ctx, (int64_t)produced), 256, 0, ctx->stream>>>(
-      args, n_probe, (int64_t)produced, prep, cnt, seg_last, srow);
+      args, n_probe, (int64_t)produced, prep, cnt, v.seg_last, v.sorted);
   QFG_LAUNCHED(ctx);
   // The next label reuses (and may regrow) the same scratch.
   QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return QFG_OK;
+}
+
+// One label of the extension with the binding rows as the build side (built
+// for this call only).
+int extend_label_binding_build(Ctx* ctx, const KeyCols& build, int64_t n_build,
+                               const KeyCols& probe, int64_t n_probe, int64_t expected,
+                               ExtendArgs args) {
+  if (n_build == 0 || n_probe == 0) {
+    return expected == 0 ? QFG_OK
+                         : set_error(ctx, QFG_ERR_MISMATCH, "extension produced 0 rows for a label");
+  }
+  const uint32_t mask = table_mask(n_build);
+  // Context scratch that nothing else of an extension uses (grow-only).
+  DevBuf& owner = ctx->scratch[kScrDedup];
+  DevBuf& rows = ctx->scratch[kScrMisc];
+  QFG_TRY(owner.reserve(ctx, sizeof(int32_t) * ((size_t)mask + 1)));
+  QFG_TRY(rows.reserve(ctx, sizeof(int32_t) * 3 * (size_t)n_build));
+  BuildView v;
+  QFG_TRY(build_side(ctx, build, n_build, mask, owner.as<int32_t>(), rows.as<int32_t>(), &v));
+  return probe_side(ctx, build, v, probe, n_probe, expected, args);
 }
 
 }  // namespace
@@ -228,6 +289,7 @@ extern "C" int qfg_extend_bindings(qfg_ctx* c, const qfg_bindings* b, const qfg_
     return set_error(ctx, QFG_ERR_INVALID, "qfg_extend_bindings: invalid literal or counts");
   KeyCols rel_keys, pos_keys, neg_keys;
   rel_keys.nk = pos_keys.nk = neg_keys.nk = 0;
+  std::vector<int> bound_args;
   ExtendArgs args;
   memset(&args, 0, sizeof(args));
   const int64_t P = b->num_positive, N = b->num_negative, R = rel->num_tuples;
@@ -236,6 +298,7 @@ extern "C" int qfg_extend_bindings(qfg_ctx* c, const qfg_bindings* b, const qfg_
     if (v >= b->num_columns || v < -1)
       return set_error(ctx, QFG_ERR_INVALID, "qfg_extend_bindings: variable out of range");
     if (v >= 0) {
+      bound_args.push_back(k);
       rel_keys.c[rel_keys.nk++] = rel->columns[k];
       pos_keys.c[pos_keys.nk++] = b->columns[v];
       neg_keys.c[neg_keys.nk++] = b->columns[v] + P;
@@ -270,10 +333,16 @@ extern "C" int qfg_extend_bindings(qfg_ctx* c, const qfg_bindings* b, const qfg_
     args.label_lo = label == 0 ? 0 : P;
     args.out_base = label == 0 ? 0 : num_out_positive;
     const int64_t expected = label == 0 ? num_out_positive : num_out_negative;
-    if (args.relation_is_probe)
-      QFG_TRY(extend_label(ctx, bind_keys, n_label, rel_keys, R, expected, args));
-    else
-      QFG_TRY(extend_label(ctx, rel_keys, R, bind_keys, n_label, expected, args));
+    if (args.relation_is_probe) {
+      QFG_TRY(extend_label_binding_build(ctx, bind_keys, n_label, rel_keys, R, expected, args));
+    } else if (R == 0 || n_label == 0) {
+      if (expected != 0)
+        return set_error(ctx, QFG_ERR_MISMATCH, "extension produced 0 rows for a label");
+    } else {
+      BuildView v;
+      QFG_TRY(relation_build_side(ctx, rel, bound_args, rel_keys, &v));
+      QFG_TRY(probe_side(ctx, rel_keys, v, bind_keys, n_label, expected, args));
+    }
   }
   QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   *out = nb.release();

@@ -134,6 +134,18 @@ struct KeySet {
   DevBuf gfilter;
 };
 
+// The relation as the build side of a binding-set extension, over a list of
+// argument positions: its key set (slot -> representative row), the rows
+// sorted stably by representative, and each representative's segment in
+// that order.
+struct ExtensionBuild {
+  uint32_t mask = 0;
+  DevBuf owner;      // mask + 1 int32
+  DevBuf sorted;     // n int32: relation rows by representative
+  DevBuf seg_first;  // n int32, indexed by representative row
+  DevBuf seg_last;   // n int32
+};
+
 struct Relation {
   int32_t id = 0;
   int32_t num_columns = 0;
@@ -144,6 +156,7 @@ struct Relation {
   std::map<std::vector<int>, std::unique_ptr<KeyTable>> key_tables;
   std::map<std::pair<int, int>, std::unique_ptr<PartitionedColumn>> partitions;  // (col, bits)
   std::map<std::vector<int>, std::unique_ptr<KeySet>> key_sets;  // by argument positions
+  std::map<std::vector<int>, std::unique_ptr<ExtensionBuild>> ext_builds;  // by argument positions
 };
 
 struct Ctx {
