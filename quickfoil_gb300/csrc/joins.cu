@@ -225,7 +225,8 @@ int relation_build_side(Ctx* ctx, Relation* rel, const std::vector<int>& args,
 // writes the matches in the reference's order at output rows
 // [out_base, out_base + expected).
 int probe_side(Ctx* ctx, const KeyCols& build, const BuildView& v, const KeyCols& probe,
-               int64_t n_probe, int64_t expected, ExtendArgs args) {
+               int64_t n_probe, int64_t expected, ExtendArgs args,
+               int64_t* produced_only = nullptr) {
   QFG_TRY(ctx->scratch[kScrJoin2].reserve(ctx, sizeof(int32_t) * (2 * (size_t)n_probe + 2)));
   int32_t* prep = ctx->scratch[kScrJoin2].as<int32_t>();
   uint32_t* cnt = reinterpret_cast<uint32_t*>(prep + n_probe);
@@ -238,6 +239,10 @@ int probe_side(Ctx* ctx, const KeyCols& build, const BuildView& v, const KeyCols
   QFG_CUDA(ctx, cudaMemcpyAsync(&produced, total, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                 ctx->stream));
   QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (produced_only != nullptr) {  // counting only: the row count, nothing written
+    *produced_only = produced;
+    return QFG_OK;
+  }
   if ((int64_t)produced != expected)
     return set_error(ctx, QFG_ERR_MISMATCH,
                      "extension produced " + std::to_string(produced) + " rows for a label, " +
@@ -254,8 +259,12 @@ int probe_side(Ctx* ctx, const KeyCols& build, const BuildView& v, const KeyCols
 // for this call only).
 int extend_label_binding_build(Ctx* ctx, const KeyCols& build, int64_t n_build,
                                const KeyCols& probe, int64_t n_probe, int64_t expected,
-                               ExtendArgs args) {
+                               ExtendArgs args, int64_t* produced_only = nullptr) {
   if (n_build == 0 || n_probe == 0) {
+    if (produced_only != nullptr) {
+      *produced_only = 0;
+      return QFG_OK;
+    }
     return expected == 0 ? QFG_OK
                          : set_error(ctx, QFG_ERR_MISMATCH, "extension produced 0 rows for a label");
   }
@@ -267,10 +276,55 @@ int extend_label_binding_build(Ctx* ctx, const KeyCols& build, int64_t n_build,
   QFG_TRY(rows.reserve(ctx, sizeof(int32_t) * 3 * (size_t)n_build));
   BuildView v;
   QFG_TRY(build_side(ctx, build, n_build, mask, owner.as<int32_t>(), rows.as<int32_t>(), &v));
-  return probe_side(ctx, build, v, probe, n_probe, expected, args);
+  return probe_side(ctx, build, v, probe, n_probe, expected, args, produced_only);
 }
 
 }  // namespace
+
+// The rows an extension by `lit` produces per label (the binding counts of
+// the literal), from the extension's own match counts.
+int extension_counts(Ctx* ctx, const qfg_bindings* b, const qfg_literal* lit, int64_t* num_pos,
+                     int64_t* num_neg) {
+  Relation* rel = nullptr;
+  QFG_TRY(find_relation(ctx, lit->relation_id, &rel));
+  if (lit->num_args != rel->num_columns)
+    return set_error(ctx, QFG_ERR_INVALID, "extension: literal arity differs from the relation");
+  KeyCols rel_keys, pos_keys, neg_keys;
+  rel_keys.nk = pos_keys.nk = neg_keys.nk = 0;
+  std::vector<int> bound_args;
+  const int64_t P = b->num_positive, N = b->num_negative, R = rel->num_tuples;
+  for (int k = 0; k < lit->num_args; ++k) {
+    const int v = lit->vars[k];
+    if (v >= b->num_columns || v < -1)
+      return set_error(ctx, QFG_ERR_INVALID, "extension: variable out of range");
+    if (v < 0) continue;
+    bound_args.push_back(k);
+    rel_keys.c[rel_keys.nk++] = rel->columns[k];
+    pos_keys.c[pos_keys.nk++] = b->columns[v];
+    neg_keys.c[neg_keys.nk++] = b->columns[v] + P;
+  }
+  if (rel_keys.nk == 0)
+    return set_error(ctx, QFG_ERR_INVALID, "extension: literal has no bound argument");
+  ExtendArgs args;
+  memset(&args, 0, sizeof(args));
+  const bool relation_is_probe = P < R && N < R;
+  int64_t got[2] = {0, 0};
+  for (int label = 0; label < 2; ++label) {
+    const KeyCols& bind_keys = label == 0 ? pos_keys : neg_keys;
+    const int64_t n_label = label == 0 ? P : N;
+    if (relation_is_probe) {
+      QFG_TRY(extend_label_binding_build(ctx, bind_keys, n_label, rel_keys, R, 0, args,
+                                         &got[label]));
+    } else if (R > 0 && n_label > 0) {
+      BuildView v;
+      QFG_TRY(relation_build_side(ctx, rel, bound_args, rel_keys, &v));
+      QFG_TRY(probe_side(ctx, rel_keys, v, bind_keys, n_label, 0, args, &got[label]));
+    }
+  }
+  *num_pos = got[0];
+  *num_neg = got[1];
+  return QFG_OK;
+}
 
 }  // namespace qfg
 

@@ -292,6 +292,9 @@ int cuda_error(Ctx* ctx, cudaError_t e, const char* what);
 // the total through *total_dev (device, may be null).
 int exclusive_scan_u32(Ctx* ctx, const uint32_t* in, uint32_t* out, int64_t n,
                        uint32_t* total_dev);
+// Rows per label that qfg_extend_bindings(bindings, lit) produces (joins.cu).
+int extension_counts(Ctx* ctx, const qfg_bindings* b, const qfg_literal* lit, int64_t* num_pos,
+                     int64_t* num_neg);
 
 // Stable radix partition into the reference layout (see qfg_radix_partition).
 int radix_partition_ref(Ctx* ctx, const int32_t* values, int64_t n, int bits,

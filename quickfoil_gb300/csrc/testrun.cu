@@ -6,8 +6,8 @@
 // (CreateBindingTable, operations/MultiColumnHashJoin.cpp:26-115), and the
 // last literal's coverage removes the test rows it covers from the ones
 // still uncovered (ComputeUnCoveredData, QuickFoilTestRunner.cpp:40-126).
-// Here the same chain runs on device-resident tables: qfg_evaluate_step
-// gives the size of each extension, qfg_extend_bindings builds it,
+// Here the same chain runs on device-resident tables: the extension's own
+// match counts give its size, qfg_extend_bindings builds it,
 // qfg_coverage and qfg_compact_rows take the covered rows out.  Nothing but
 // the counts crosses to the host between clauses.
 #include <cstring>
@@ -79,14 +79,14 @@ extern "C" int qfg_run_test(qfg_ctx* c, int32_t num_clauses, const int32_t* clau
     bind.reset(b0);
     bool empty = false;
     for (int32_t li = 0; li + 1 < clause_lengths[ci] && !empty; ++li) {
-      int64_t counts[4] = {0, 0, 0, 0};
-      QFG_TRY(qfg_evaluate_step(c, bind.b, 1, &lit[li], counts, QFG_COUNTS_HOST));
-      if (counts[2] == 0) {
+      int64_t np = 0, nn = 0;
+      QFG_TRY(extension_counts(ctx, bind.b, &lit[li], &np, &nn));
+      if (np == 0) {
         empty = true;
         break;
       }
       qfg_bindings* nb = nullptr;
-      QFG_TRY(qfg_extend_bindings(c, bind.b, &lit[li], counts[2], 0, &nb));
+      QFG_TRY(qfg_extend_bindings(c, bind.b, &lit[li], np, 0, &nb));
       bind.reset(nb);
     }
     if (empty) continue;  // the clause covers no test row
