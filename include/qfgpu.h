@@ -120,8 +120,12 @@ int qfg_ctx_stage_times(qfg_ctx* ctx, double* ms, int64_t* calls, int reset_afte
 /* ---- background relations --------------------------------------------- */
 /* Replaces FoilPredicate's fact table (schema/FoilPredicate.hpp:21-68):
  * num_columns int32 columns of num_tuples rows, registered once per run.
- * Derived per-column partitions and key tables are cached on the device,
- * as TableView caches partitions (storage/TableView.hpp:62-80). */
+ * Everything derived from the tuples is cached on the device until the
+ * relation is registered again under its id or released, as TableView
+ * caches partitions (storage/TableView.hpp:62-80): per-column partitions,
+ * key tables, coverage key sets and filters, extension build sides.  A
+ * relation registered with QFG_DEVICE_BORROW must therefore not change in
+ * place; register it again after changing it. */
 int qfg_relation_register(qfg_ctx* ctx, int32_t relation_id, int32_t num_columns,
                           const int32_t* const* columns, int64_t num_tuples, int flags);
 int qfg_relation_release(qfg_ctx* ctx, int32_t relation_id);
