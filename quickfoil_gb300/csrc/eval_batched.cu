@@ -241,47 +241,52 @@ __global__ void __launch_bounds__(kPartThreads, 1) bpart_hist_kernel(BPartArgs a
   }
 }
 
-// Round processing, templated on the number of carried columns NC so that
-// every per-column loop unrolls without predicated-off lanes.  Each thread
-// owns four consecutive rows of a round; rounds arrive by cp.async (16-byte
-// copies where the source is aligned) into one of two shared-memory buffers
-// while the previous round is sorted and written.  A round is
-// counting-sorted by bin in shared memory: ranks come from shared atomics on
-// the bin counters and stay in registers, one block scan gives the bins'
-// starts (and advances their output cursors), the permutation records (row,
-// bin) at each sorted position, and the threads then write sorted positions
-// in order, so the threads writing one bin's run write consecutive
-// addresses.
-template <int NC>
-struct PassShape {
-  static constexpr int kThreads = NC <= 6 ? 1024 : 512;
-  static constexpr int kRows = 4 * kThreads;  // rows per round
-};
+// Round processing.  A round is up to kPassRows consecutive rows of one
+// label.  Its join column is counting-sorted by destination bin in shared
+// memory: each thread ranks 16 rows with shared atomics on the bin counters
+// (ranks kept in registers), one block scan gives the bins' starts and their
+// output positions, and the permutation records (row, bin) at each sorted
+// position; every thread then keeps the output position and the source row
+// of its 16 sorted positions in registers.  The carried columns stream
+// through two shared-memory buffers one at a time: while column q of the
+// round is written in sorted order (consecutive threads on consecutive
+// addresses of a bin's run), column q + 1, or the next round's join column,
+// arrives by cp.async (16-byte copies where the source is aligned).  Sorting
+// once per round and holding one column at a time lets a round span 16K
+// rows in 200 KB of shared memory whatever the column count, so each bin's
+// run of a column averages 512 bytes at 128 bins.
+constexpr int kPassThreads = 1024;
+constexpr int kPassRows = 16384;                              // rows per round
+constexpr int kPassRowsPerThread = kPassRows / kPassThreads;  // 16
+constexpr int kPassPieces = kPassRows / (4 * kPassThreads);   // 4-row copy pieces per thread
+static_assert(kPassRows <= 65536, "a round's row index packs into 16 bits");
+static_assert((2 << kMaxCoarseBits) <= kPassThreads && (1 << kMaxSubBits) <= kPassThreads,
+              "one thread per bin in the round scan");
 
-struct RoundSmem {
-  int32_t* rows[2];   // NC * kRows each
-  uint32_t* perm;     // kRows: row | bin << 16 at each sorted position
+struct PassSmem {
+  int32_t* buf0;      // kPassRows: one column of a round
+  int32_t* buf1;      // kPassRows: the column after it
+  uint32_t* perm;     // kPassRows: row | bin << 16 at each sorted position
   uint32_t* lcount;   // nbins
   uint32_t* lstart;   // nbins
   uint32_t* gpos;     // nbins: output position of sorted position 0 of bin b
-  uint32_t* cursor;   // nbins: output cursor of each bin
+  uint32_t* cursor;   // nbins: output cursor of each bin (pass 1)
 };
 
-__device__ __forceinline__ RoundSmem carve_round(unsigned char* smem, int ncols, int nbins, int rows) {
-  RoundSmem S;
-  S.rows[0] = reinterpret_cast<int32_t*>(smem);
-  S.rows[1] = S.rows[0] + ncols * rows;
-  S.perm = reinterpret_cast<uint32_t*>(S.rows[1] + ncols * rows);
-  S.lcount = S.perm + rows;
+__device__ __forceinline__ PassSmem carve_pass(unsigned char* smem, int nbins) {
+  PassSmem S;
+  S.buf0 = reinterpret_cast<int32_t*>(smem);
+  S.buf1 = S.buf0 + kPassRows;
+  S.perm = reinterpret_cast<uint32_t*>(S.buf1 + kPassRows);
+  S.lcount = S.perm + kPassRows;
   S.lstart = S.lcount + nbins;
   S.gpos = S.lstart + nbins;
   S.cursor = S.gpos + nbins;
   return S;
 }
 
-size_t round_smem_bytes(int ncols, int nbins) {
-  const size_t rows = ncols <= 6 ? 4096 : 2048;
-  return sizeof(int32_t) * (2 * (size_t)ncols * rows + rows + 4 * (size_t)nbins);
+size_t pass_smem_bytes(int nbins) {
+  return sizeof(uint32_t) * (3 * (size_t)kPassRows + 4 * (size_t)nbins);
 }
 
 __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
@@ -295,32 +300,23 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// Starts the copies of rows [rr, rr + nt) of NC columns into `dst` (column
-// stride R): thread c copies rows 4c .. 4c + 3, with one 16-byte copy per
-// column when the source is 16-byte aligned and the chunk is whole.
-template <int NC>
-struct ColPtrs {
-  const int32_t* p[NC];
-};
-template <int NC>
-struct OutPtrs {
-  int32_t* p[NC];
-};
-
-template <int NC, int R>
-__device__ __forceinline__ void issue_round(const ColPtrs<NC> src, uint32_t rr, int nt, int32_t* dst,
-                                            bool vec) {
-  const int i0 = 4 * threadIdx.x;
+// Starts the copies of rows [rr, rr + nt) of one column into dst: the
+// thread copies the 4-row pieces t, t + T, t + 2T and t + 3T, each with one
+// 16-byte copy when `vec` (the source piece is 16-byte aligned) and the
+// piece is whole.
+__device__ __forceinline__ void issue_column(const int32_t* __restrict__ src, uint32_t rr, int nt,
+                                             int32_t* dst, bool vec) {
 #pragma unroll
-  for (int q = 0; q < NC; ++q) {
-    int32_t* d = dst + q * R + i0;
-    const int32_t* s = src.p[q] + rr + i0;
-    if (vec && i0 + 4 <= nt) {
-      cp_async16(d, s);
-    } else {
+  for (int m = 0; m < kPassPieces; ++m) {
+    const int i0 = 4 * ((int)threadIdx.x + m * kPassThreads);
+    if (i0 < nt) {
+      if (vec && i0 + 4 <= nt) {
+        cp_async16(dst + i0, src + rr + i0);
+      } else {
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
-        if (i0 + j < nt) cp_async4(d + j, s + j);
+        for (int j = 0; j < 4; ++j)
+          if (i0 + j < nt) cp_async4(dst + i0 + j, src + rr + i0 + j);
+      }
     }
   }
   cp_async_commit();
@@ -334,123 +330,168 @@ __device__ __forceinline__ uint32_t round_end(uint32_t r0, uint32_t rr, uint32_t
   return (rr < split && split < e) ? split : e;
 }
 
-// Rows [r0, r1) in rounds anchored at r0 (which is a multiple of 4); rounds
-// never straddle `split` (the first negative row in pass 1), so a round's
-// rows share one label and fan out to half the bins.  `aligned` says the
-// source columns are 16-byte aligned.
-template <int NC, typename BinFn>
-__device__ __forceinline__ void stream_rounds(const RoundSmem& S, const ColPtrs<NC> src, uint32_t r0,
-                                              uint32_t r1, uint32_t split, int nbins,
-                                              const OutPtrs<NC> out, bool aligned,
-                                              uint32_t* s_warp, uint32_t* s_total, BinFn bin_of) {
-  constexpr int T = PassShape<NC>::kThreads;
-  constexpr int R = PassShape<NC>::kRows;
-  if (r0 >= r1) return;
-  uint32_t rr = r0, re = round_end(r0, r0, r1, split, R);
-  issue_round<NC, R>(src, rr, (int)(re - rr), S.rows[0], aligned && (rr & 3u) == 0u);
-  int buf = 0;
-  while (rr < r1) {
-    const int nt = (int)(re - rr);
-    cp_async_wait_all();
-    __syncthreads();
-    const uint32_t nrr = re;
-    uint32_t nre = nrr;
-    if (nrr < r1) {
-      nre = round_end(r0, nrr, r1, split, R);
-      issue_round<NC, R>(src, nrr, (int)(nre - nrr), S.rows[buf ^ 1], aligned && (nrr & 3u) == 0u);
-    }
-    const int32_t* rows = S.rows[buf];
-    const int i0 = 4 * threadIdx.x;
-    uint32_t b0, b1, b2, b3, k0 = 0, k1 = 0, k2 = 0, k3 = 0;
-    {
-      const int4 kv = *reinterpret_cast<const int4*>(rows + i0);
-      b0 = bin_of(kv.x, rr + i0);
-      b1 = bin_of(kv.y, rr + i0 + 1);
-      b2 = bin_of(kv.z, rr + i0 + 2);
-      b3 = bin_of(kv.w, rr + i0 + 3);
-      if (i0 < nt) k0 = atomicAdd(&S.lcount[b0], 1u);
-      if (i0 + 1 < nt) k1 = atomicAdd(&S.lcount[b1], 1u);
-      if (i0 + 2 < nt) k2 = atomicAdd(&S.lcount[b2], 1u);
-      if (i0 + 3 < nt) k3 = atomicAdd(&S.lcount[b3], 1u);
-    }
-    __syncthreads();
-    {
-      const uint32_t c = (int)threadIdx.x < nbins ? S.lcount[threadIdx.x] : 0u;
-      const uint32_t ex = block_scan_excl(c, s_warp, s_total);
-      if ((int)threadIdx.x < nbins) {
-        S.lstart[threadIdx.x] = ex;
-        S.gpos[threadIdx.x] = S.cursor[threadIdx.x] - ex;
-        S.cursor[threadIdx.x] += c;
-        S.lcount[threadIdx.x] = 0u;
-      }
-    }
-    __syncthreads();
-    if (i0 < nt) S.perm[S.lstart[b0] + k0] = (uint32_t)i0 | (b0 << 16);
-    if (i0 + 1 < nt) S.perm[S.lstart[b1] + k1] = (uint32_t)(i0 + 1) | (b1 << 16);
-    if (i0 + 2 < nt) S.perm[S.lstart[b2] + k2] = (uint32_t)(i0 + 2) | (b2 << 16);
-    if (i0 + 3 < nt) S.perm[S.lstart[b3] + k3] = (uint32_t)(i0 + 3) | (b3 << 16);
-    __syncthreads();
+// Rows [rr, re) of a round; `chunk` is its pass-2 chunk.
+struct PassRound {
+  uint32_t rr, re, chunk;
+  bool valid;
+};
+
+// Streams the CTA's rounds, starting at `cur`.  next_of(round) gives the
+// round after it (invalid at the end); it runs at the start of a round, so
+// its global reads overlap the sort.  bin_of(key, row) gives a row's bin.
+// A bin's output position in a round comes from the CTA's cursors (pass 1:
+// h2 == nullptr) or from h2[chunk * nbins + bin] (pass 2, one round per
+// chunk).  src and dst are the columns (shared-memory arrays of pointers).
+template <typename NextFn, typename BinFn>
+__device__ __forceinline__ void stream_pass(const PassSmem& S, const int32_t* const* src,
+                                            int32_t* const* dst, int ncols, int nbins, bool aligned,
+                                            PassRound cur, const uint32_t* __restrict__ h2,
+                                            uint32_t* s_warp, uint32_t* s_total, NextFn next_of,
+                                            BinFn bin_of) {
+  constexpr int T = kPassThreads;
+  constexpr int J = kPassRowsPerThread;
+  const int t = threadIdx.x;
+  if (!cur.valid) return;
+  issue_column(src[0], cur.rr, (int)(cur.re - cur.rr), S.buf0, aligned && (cur.rr & 3u) == 0u);
+  bool slot = false;
+  uint32_t oidx[J];       // output position of sorted positions t + j T
+  uint32_t rowp[J / 2];   // their rows in the round, two 16-bit rows a word
+  while (true) {
+    const PassRound nxt = next_of(cur);
+    const int nt = (int)(cur.re - cur.rr);
+    const bool vec = aligned && (cur.rr & 3u) == 0u;
+    for (int q = 0; q < ncols; ++q) {
+      cp_async_wait_all();
+      __syncthreads();
+      const int32_t* const cbuf = slot ? S.buf1 : S.buf0;
+      int32_t* const obuf = slot ? S.buf0 : S.buf1;
+      if (q + 1 < ncols)
+        issue_column(src[q + 1], cur.rr, nt, obuf, vec);
+      else if (nxt.valid)
+        issue_column(src[0], nxt.rr, (int)(nxt.re - nxt.rr), obuf, aligned && (nxt.rr & 3u) == 0u);
+      if (q == 0) {
+        uint32_t hb = 0;
+        if (h2 != nullptr && t < nbins) hb = __ldg(h2 + (size_t)cur.chunk * (size_t)nbins + t);
+        uint32_t pk[J];   // rank | bin << 16
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int kk = threadIdx.x + k * T;
-      if (kk < nt) {
-        const uint32_t w = S.perm[kk];
-        const int i = (int)(w & 0xffffu);
-        const uint32_t g = S.gpos[w >> 16] + (uint32_t)kk;
+        for (int j = 0; j < J; ++j) {
+          const int i = t + j * T;
+          pk[j] = 0xffffffffu;
+          if (i < nt) {
+            const uint32_t b = bin_of(cbuf[i], cur.rr + (uint32_t)i);
+            pk[j] = atomicAdd(&S.lcount[b], 1u) | (b << 16);
+          }
+        }
+        __syncthreads();
+        const uint32_t c = t < nbins ? S.lcount[t] : 0u;
+        const uint32_t ex = block_scan_excl(c, s_warp, s_total);
+        if (t < nbins) {
+          S.lstart[t] = ex;
+          if (h2 != nullptr) {
+            S.gpos[t] = hb - ex;
+          } else {
+            S.gpos[t] = S.cursor[t] - ex;
+            S.cursor[t] += c;
+          }
+          S.lcount[t] = 0u;
+        }
+        __syncthreads();
 #pragma unroll
-        for (int q = 0; q < NC; ++q) out.p[q][g] = rows[q * R + i];
+        for (int j = 0; j < J; ++j) {
+          if (pk[j] != 0xffffffffu) {
+            const uint32_t b = pk[j] >> 16;
+            S.perm[S.lstart[b] + (pk[j] & 0xffffu)] = (uint32_t)(t + j * T) | (b << 16);
+          }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+          const int kk = t + j * T;
+          uint32_t w = 0;
+          if (kk < nt) w = S.perm[kk];
+          oidx[j] = S.gpos[w >> 16] + (uint32_t)kk;
+          if (j & 1)
+            rowp[j >> 1] |= (w & 0xffffu) << 16;
+          else
+            rowp[j >> 1] = w & 0xffffu;
+        }
       }
+      int32_t* __restrict__ out = dst[q];
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        const int kk = t + j * T;
+        if (kk < nt) out[oidx[j]] = cbuf[(rowp[j >> 1] >> (16 * (j & 1))) & 0xffffu];
+      }
+      slot = !slot;
     }
-    rr = nrr;
-    re = nre;
-    buf ^= 1;
+    if (!nxt.valid) break;
+    cur = nxt;
   }
 }
 
 // Pass 1: the CTA's chunk of the original columns into pass-1 bins at
 // p1_start[bin] + this CTA's base (out: column stride out_stride).
-template <int NC>
-__global__ void __launch_bounds__(PassShape<NC>::kThreads, 1)
+__global__ void __launch_bounds__(kPassThreads, 1)
 bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* __restrict__ out,
                    int64_t out_stride, int aligned) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
+  __shared__ const int32_t* s_src[kGroupCols];
+  __shared__ int32_t* s_dst[kGroupCols];
   const int np1 = 2 << a.cbits;
-  const RoundSmem S = carve_round(smem, NC, np1, PassShape<NC>::kRows);
+  const PassSmem S = carve_pass(smem, np1);
   for (int i = threadIdx.x; i < np1; i += blockDim.x) {
     S.cursor[i] = p1_start[i] + a.p1_base[(int64_t)blockIdx.x * np1 + i];
     S.lcount[i] = 0u;
   }
-  __syncthreads();
-  int64_t r0, r1;
-  cta_range4(a.n, &r0, &r1);
-  ColPtrs<NC> src;
-  OutPtrs<NC> dst;
+  if (threadIdx.x == 0) {
 #pragma unroll
-  for (int q = 0; q < NC; ++q) {
-    src.p[q] = a.cols[q];
-    dst.p[q] = out + (int64_t)q * out_stride;
+    for (int q = 0; q < kGroupCols; ++q) {
+      if (q < a.ncols) {
+        s_src[q] = a.cols[q];
+        s_dst[q] = out + (int64_t)q * out_stride;
+      }
+    }
   }
+  __syncthreads();
+  int64_t r0l, r1l;
+  cta_range4(a.n, &r0l, &r1l);
+  const uint32_t r0 = (uint32_t)r0l, r1 = (uint32_t)r1l;
   const int cbits = a.cbits;
   const uint32_t npos = (uint32_t)a.npos;
-  stream_rounds<NC>(S, src, (uint32_t)r0, (uint32_t)r1, npos, np1, dst, aligned != 0, s_warp,
-                    &s_total, [=](int32_t key, uint32_t r) {
-                      return (top_bits(key, cbits) << 1) | (r >= npos ? 1u : 0u);
-                    });
+  PassRound first;
+  first.rr = r0;
+  first.re = r0 < r1 ? round_end(r0, r0, r1, npos, kPassRows) : r0;
+  first.chunk = 0;
+  first.valid = r0 < r1;
+  stream_pass(
+      S, s_src, s_dst, a.ncols, np1, aligned != 0, first, nullptr, s_warp, &s_total,
+      [=](const PassRound& r) {
+        PassRound n;
+        n.rr = r.re;
+        n.valid = r.re < r1;
+        n.re = n.valid ? round_end(r0, r.re, r1, npos, kPassRows) : r.re;
+        n.chunk = 0;
+        return n;
+      },
+      [=](int32_t key, uint32_t r) { return (top_bits(key, cbits) << 1) | (r >= npos ? 1u : 0u); });
 }
 
 // Rows of a pass-2 work chunk: coarse bins (up to 9x apart in size, since
 // negatives outnumber positives) are cut into chunks so the persistent pass
 // 2 stays balanced.
 constexpr uint32_t kP2Chunk = 16384;
+static_assert(kP2Chunk <= (uint32_t)kPassRows, "a pass-2 chunk is one round");
 
 // Bin starts of pass 1, twice: padded to multiples of 4 rows (where pass 1
 // writes and pass 2 reads, so that pass 2's copies are 16-byte aligned) and
-// unpadded (where pass 2 writes); and the first pass-2 chunk of every bin
-// (chunk_start[nbins] = number of chunks).  One block, nbins <= blockDim.x.
+// unpadded (where pass 2 writes); the first pass-2 chunk of every bin
+// (chunk_start[nbins] = number of chunks) and the bin of every chunk.  One
+// block, nbins <= blockDim.x.
 __global__ void pad_scan_kernel(const uint32_t* __restrict__ tot, int nbins, uint32_t* __restrict__ pad,
-                                uint32_t* __restrict__ unp, uint32_t* __restrict__ chunk_start) {
+                                uint32_t* __restrict__ unp, uint32_t* __restrict__ chunk_start,
+                                uint32_t* __restrict__ chunk_bin) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   const uint32_t c = (int)threadIdx.x < nbins ? tot[threadIdx.x] : 0u;
@@ -463,6 +504,8 @@ __global__ void pad_scan_kernel(const uint32_t* __restrict__ tot, int nbins, uin
     unp[threadIdx.x] = ex;
     pad[threadIdx.x] = exp;
     chunk_start[threadIdx.x] = exc;
+    const uint32_t nch = (c + kP2Chunk - 1u) / kP2Chunk;
+    for (uint32_t j = 0; j < nch; ++j) chunk_bin[exc + j] = threadIdx.x;
   }
   if (threadIdx.x == 0) {
     unp[nbins] = total;
@@ -471,26 +514,23 @@ __global__ void pad_scan_kernel(const uint32_t* __restrict__ tot, int nbins, uin
   }
 }
 
-// Pass-2 chunk c: its coarse bin (the last bin whose first chunk is <= c;
-// bins without rows own no chunk) and row range in the padded layout.
+// Pass-2 chunk c: its coarse bin (from the chunk -> bin table) and row
+// range in the padded layout.
 struct P2Chunk {
   int bin;
   uint32_t r0, r1;
 };
-__device__ __forceinline__ P2Chunk p2_chunk(const uint32_t* __restrict__ chunk_start, int nbins,
+__device__ __forceinline__ P2Chunk p2_chunk(const uint32_t* __restrict__ chunk_bin,
+                                            const uint32_t* __restrict__ chunk_start,
                                             const uint32_t* __restrict__ pad,
                                             const uint32_t* __restrict__ unp, uint32_t c) {
-  int lo = 0, hi = nbins - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (chunk_start[mid] <= c) lo = mid; else hi = mid - 1;
-  }
-  const uint32_t k = c - chunk_start[lo];
-  const uint32_t cnt = unp[lo + 1] - unp[lo];
+  const int b = (int)chunk_bin[c];
+  const uint32_t k = c - chunk_start[b];
+  const uint32_t cnt = unp[b + 1] - unp[b];
   P2Chunk r;
-  r.bin = lo;
-  r.r0 = pad[lo] + k * kP2Chunk;
-  r.r1 = pad[lo] + umin(cnt, (k + 1) * kP2Chunk);
+  r.bin = b;
+  r.r0 = pad[b] + k * kP2Chunk;
+  r.r1 = pad[b] + umin(cnt, (k + 1) * kP2Chunk);
   return r;
 }
 
@@ -498,6 +538,7 @@ __device__ __forceinline__ P2Chunk p2_chunk(const uint32_t* __restrict__ chunk_s
 __global__ void __launch_bounds__(512) bpart_p2hist_kernel(BPartArgs a, const uint32_t* __restrict__ pad,
                                                            const uint32_t* __restrict__ unp,
                                                            const uint32_t* __restrict__ chunk_start,
+                                                           const uint32_t* __restrict__ chunk_bin,
                                                            const int32_t* __restrict__ keys,
                                                            uint32_t* __restrict__ h2) {
   __shared__ uint32_t cntr[1 << kMaxSubBits];
@@ -507,7 +548,7 @@ __global__ void __launch_bounds__(512) bpart_p2hist_kernel(BPartArgs a, const ui
   const uint32_t mask = (uint32_t)(nsub - 1);
   const uint32_t nch = chunk_start[np1];
   for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
-    const P2Chunk ch = p2_chunk(chunk_start, np1, pad, unp, c);
+    const P2Chunk ch = p2_chunk(chunk_bin, chunk_start, pad, unp, c);
     for (int i = threadIdx.x; i < nsub; i += blockDim.x) cntr[i] = 0u;
     __syncthreads();
     uint32_t r = ch.r0 + threadIdx.x;
@@ -560,74 +601,48 @@ __global__ void __launch_bounds__(512) bpart_p2scan_kernel(BPartArgs a, const ui
 
 // Pass 2, persistent over chunks: each chunk of a coarse bin, read from the
 // padded layout, is split into sub-bins 0 .. 2^sbits - 1 at its cursors.
-template <int NC>
-__global__ void __launch_bounds__(PassShape<NC>::kThreads, 1)
+__global__ void __launch_bounds__(kPassThreads, 1)
 bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ pad, const uint32_t* __restrict__ unp,
-                   const uint32_t* __restrict__ chunk_start, const uint32_t* __restrict__ h2,
-                   const int32_t* __restrict__ in, int64_t in_stride, int32_t* __restrict__ out,
-                   int64_t out_stride) {
+                   const uint32_t* __restrict__ chunk_start, const uint32_t* __restrict__ chunk_bin,
+                   const uint32_t* __restrict__ h2, const int32_t* __restrict__ in, int64_t in_stride,
+                   int32_t* __restrict__ out, int64_t out_stride) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
+  __shared__ const int32_t* s_src[kGroupCols];
+  __shared__ int32_t* s_dst[kGroupCols];
   const int np1 = 2 << a.cbits;
   const int nsub = 1 << (a.bits - a.cbits);
-  const RoundSmem S = carve_round(smem, NC, nsub, PassShape<NC>::kRows);
+  const PassSmem S = carve_pass(smem, nsub);
   const uint32_t mask = (uint32_t)(nsub - 1);
   const int bits = a.bits;
-  ColPtrs<NC> src;
-  OutPtrs<NC> dst;
-#pragma unroll
-  for (int q = 0; q < NC; ++q) {
-    src.p[q] = in + (int64_t)q * in_stride;
-    dst.p[q] = out + (int64_t)q * out_stride;
-  }
   for (int i = threadIdx.x; i < nsub; i += blockDim.x) S.lcount[i] = 0u;
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < a.ncols; ++q) {
+      s_src[q] = in + (int64_t)q * in_stride;
+      s_dst[q] = out + (int64_t)q * out_stride;
+    }
+  }
+  __syncthreads();
   const uint32_t nch = chunk_start[np1];
-  for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
-    const P2Chunk ch = p2_chunk(chunk_start, np1, pad, unp, c);
-    for (int i = threadIdx.x; i < nsub; i += blockDim.x) S.cursor[i] = h2[(int64_t)c * nsub + i];
-    __syncthreads();
-    stream_rounds<NC>(S, src, ch.r0, ch.r1, ch.r1, nsub, dst, true, s_warp, &s_total,
-                      [=](int32_t key, uint32_t) { return top_bits(key, bits) & mask; });
-    __syncthreads();
-  }
+  auto round_of = [=](uint32_t c) {
+    PassRound r;
+    r.chunk = c;
+    r.valid = c < nch;
+    r.rr = r.re = 0;
+    if (r.valid) {
+      const P2Chunk ch = p2_chunk(chunk_bin, chunk_start, pad, unp, c);
+      r.rr = ch.r0;
+      r.re = ch.r1;
+    }
+    return r;
+  };
+  const uint32_t stride = gridDim.x;
+  stream_pass(
+      S, s_src, s_dst, a.ncols, nsub, true, round_of(blockIdx.x), h2, s_warp, &s_total,
+      [=](const PassRound& r) { return round_of(r.chunk + stride); },
+      [=](int32_t key, uint32_t) { return top_bits(key, bits) & mask; });
 }
-
-// Launches of the templated passes for a group's column count.
-template <int NC>
-void launch_pass1(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t st,
-                  const uint32_t* p1_start, int32_t* out, int64_t out_stride, bool aligned) {
-  bpart_pass1_kernel<NC><<<grid, PassShape<NC>::kThreads, smem, st>>>(pa, p1_start, out, out_stride,
-                                                                      aligned ? 1 : 0);
-}
-template <int NC>
-void launch_pass2(const BPartArgs& pa, unsigned grid, size_t smem, cudaStream_t st, const uint32_t* pad,
-                  const uint32_t* unp, const uint32_t* chunk_start, const uint32_t* h2,
-                  const int32_t* in, int64_t in_stride, int32_t* out, int64_t out_stride) {
-  bpart_pass2_kernel<NC><<<grid, PassShape<NC>::kThreads, smem, st>>>(pa, pad, unp, chunk_start, h2, in,
-                                                                      in_stride, out, out_stride);
-}
-template <int NC>
-cudaError_t set_pass_smem(size_t smem1, size_t smem2) {
-  cudaError_t e = cudaFuncSetAttribute(bpart_pass1_kernel<NC>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(bpart_pass2_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)smem2);
-}
-
-#define QFG_NC_SWITCH(nc, CALL) \
-  switch (nc) {                 \
-    case 1: CALL(1); break;     \
-    case 2: CALL(2); break;     \
-    case 3: CALL(3); break;     \
-    case 4: CALL(4); break;     \
-    case 5: CALL(5); break;     \
-    case 6: CALL(6); break;     \
-    case 7: CALL(7); break;     \
-    default: CALL(8); break;    \
-  }
-static_assert(kGroupCols == 8, "column-count dispatch covers 1..8");
 
 // ----------------------------------------------------------------------------
 // Persistent evaluation kernel.
@@ -1411,6 +1426,7 @@ struct PreparedStep {
   uint32_t* p1_start = nullptr;   // padded bin starts (two passes)
   uint32_t* p1_unp = nullptr;     // unpadded bin starts (two passes)
   uint32_t* chunk_start = nullptr;  // first pass-2 chunk of every bin
+  uint32_t* chunk_bin = nullptr;    // coarse bin of every pass-2 chunk
   uint32_t* h2 = nullptr;         // pass-2 chunk sub-bin counts, then cursors
   int32_t* tmp_cols = nullptr;
   int64_t tmp_stride = 0;
@@ -1468,8 +1484,9 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   const size_t fs_words = (size_t)nfine + 1;
   const size_t h2_words =
       ps->two_pass ? ((size_t)nb / kP2Chunk + (size_t)ps->np1 + 1) * ((size_t)1 << ps->sbits) : 0;
+  const size_t chunk_words = ps->two_pass ? (size_t)nb / kP2Chunk + (size_t)ps->np1 + 1 : 0;
   const size_t bins_words = (size_t)ps->np1 + 1 + (size_t)ps->pgrid * ps->np1 +
-                            3 * ((size_t)ps->np1 + 1) + h2_words;
+                            3 * ((size_t)ps->np1 + 1) + h2_words + chunk_words;
   QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * (tmp_off + tmp_words)));
   QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(
       ctx, sizeof(uint32_t) * (groups.size() * fs_words + bins_words)));
@@ -1482,13 +1499,13 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   ps->p1_unp = ps->p1_start + ps->np1 + 1;
   ps->chunk_start = ps->p1_unp + ps->np1 + 1;
   ps->h2 = ps->chunk_start + ps->np1 + 1;
-  for (auto& g : groups) {
-    const int nc = (int)g.cols.size();
-    const size_t s1 = round_smem_bytes(nc, ps->np1), s2 = round_smem_bytes(nc, 1 << ps->sbits);
-#define QFG_SET_SMEM(N) QFG_CUDA(ctx, set_pass_smem<N>(s1, s2))
-    QFG_NC_SWITCH(nc, QFG_SET_SMEM)
-#undef QFG_SET_SMEM
-  }
+  ps->chunk_bin = ps->h2 + h2_words;
+  ps->p1_smem = pass_smem_bytes(ps->np1);
+  ps->p2_smem = pass_smem_bytes(1 << ps->sbits);
+  QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)ps->p1_smem));
+  QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)ps->p2_smem));
 
   std::vector<GroupDesc> gdesc(groups.size());
   std::vector<LitDesc> ldesc;
@@ -1659,35 +1676,27 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
     else
       bpart_hist_kernel<false><<<ps.pgrid, kPartThreads, 0, ctx->stream>>>(job.pa);
     QFG_LAUNCHED(ctx);
-    const int nc = job.pa.ncols;
-    const size_t s1 = round_smem_bytes(nc, ps.np1), s2 = round_smem_bytes(nc, 1 << ps.sbits);
     if (ps.two_pass) {
       pad_scan_kernel<<<1, 512, 0, ctx->stream>>>(ps.p1_tot, ps.np1, ps.p1_start, ps.p1_unp,
-                                                  ps.chunk_start);
+                                                  ps.chunk_start, ps.chunk_bin);
       QFG_LAUNCHED(ctx);
-#define QFG_P1(N) \
-  launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, ps.p1_start, ps.tmp_cols, ps.tmp_stride, job.vec)
-      QFG_NC_SWITCH(nc, QFG_P1)
-#undef QFG_P1
+      bpart_pass1_kernel<<<ps.pgrid, kPassThreads, ps.p1_smem, ctx->stream>>>(
+          job.pa, ps.p1_start, ps.tmp_cols, ps.tmp_stride, job.vec ? 1 : 0);
       QFG_LAUNCHED(ctx);
-      bpart_p2hist_kernel<<<ps.pgrid * 2, 512, 0, ctx->stream>>>(job.pa, ps.p1_start, ps.p1_unp,
-                                                                 ps.chunk_start, ps.tmp_cols, ps.h2);
+      bpart_p2hist_kernel<<<ps.pgrid * 2, 512, 0, ctx->stream>>>(
+          job.pa, ps.p1_start, ps.p1_unp, ps.chunk_start, ps.chunk_bin, ps.tmp_cols, ps.h2);
       QFG_LAUNCHED(ctx);
       bpart_p2scan_kernel<<<ps.np1, 512, 0, ctx->stream>>>(job.pa, ps.p1_unp, ps.chunk_start, ps.h2,
                                                            job.fstart);
       QFG_LAUNCHED(ctx);
-#define QFG_P2(N)                                                                                  \
-  launch_pass2<N>(job.pa, ps.pgrid, s2, ctx->stream, ps.p1_start, ps.p1_unp, ps.chunk_start, ps.h2, \
-                  ps.tmp_cols, ps.tmp_stride, job.final_out, ps.col_stride)
-      QFG_NC_SWITCH(nc, QFG_P2)
-#undef QFG_P2
+      bpart_pass2_kernel<<<ps.pgrid, kPassThreads, ps.p2_smem, ctx->stream>>>(
+          job.pa, ps.p1_start, ps.p1_unp, ps.chunk_start, ps.chunk_bin, ps.h2, ps.tmp_cols,
+          ps.tmp_stride, job.final_out, ps.col_stride);
       QFG_LAUNCHED(ctx);
     } else {
       QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, job.fstart, ps.np1, job.fstart + ps.np1));
-#define QFG_P1(N) \
-  launch_pass1<N>(job.pa, ps.pgrid, s1, ctx->stream, job.fstart, job.final_out, ps.col_stride, job.vec)
-      QFG_NC_SWITCH(nc, QFG_P1)
-#undef QFG_P1
+      bpart_pass1_kernel<<<ps.pgrid, kPassThreads, ps.p1_smem, ctx->stream>>>(
+          job.pa, job.fstart, job.final_out, ps.col_stride, job.vec ? 1 : 0);
       QFG_LAUNCHED(ctx);
     }
   }
@@ -1738,7 +1747,7 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
   }
   if (two_pass) words += (int64_t)max_ncols * (nb + 4 + 4 * np1) + 64;
   words += (int64_t)np1 * (ctx->num_sms * 2 + 5);
-  if (two_pass) words += (nb / kP2Chunk + np1 + 1) << (bits - cb);
+  if (two_pass) words += (nb / kP2Chunk + np1 + 1) * ((1 << (bits - cb)) + 1);
   int64_t units = (int64_t)plan.groups.size() << bits;
   int64_t entries = 0;
   for (KeyTable* kt : plan.tables) {
