@@ -228,3 +228,50 @@ def test_evaluate_pass_split_does_not_change_counts(engine, bits, pass1):
     finally:
         engine.set_option(C.QFG_OPT_EVAL_BITS, 0)
         engine.set_option(C.QFG_OPT_PASS1_BITS, 0)
+
+
+@pytest.mark.parametrize("offset", [0, 1, 3])
+def test_partition_rounds_wide_and_unaligned(engine, offset):
+    """5M binding rows: every partition CTA streams several 16K-row rounds.
+    One literal group carries all eight columns (a literal binding every
+    argument of an 8-ary relation), the label boundary is not a multiple of
+    4 rows, and the binding columns are borrowed from device memory at an
+    element offset (1 and 3: not 16-byte aligned, so every round is copied
+    4 bytes at a time).  Counts equal the oracle's at the automatic, a
+    small single-pass-adjacent and the widest partition settings."""
+    from quickfoil_gb300 import _capi as C
+    rng = np.random.default_rng(31 + offset)
+    n, P, dom = 5_000_003, 1_234_567, 48
+    B = [rng.integers(0, dom, n, dtype=np.int32) for _ in range(8)]
+    B[0] = rng.integers(0, 300_000, n, dtype=np.int32)
+    pick = rng.choice(n, 600_000, replace=False)
+    noise = 80_000
+    R8 = [np.concatenate([c[pick], rng.integers(0, dom, noise, dtype=np.int32)]) for c in B]
+    R8[0][-noise:] = rng.integers(0, 300_000, noise, dtype=np.int32)
+    R3 = [rng.integers(0, 300_000, 400_000, dtype=np.int32),
+          rng.integers(0, dom, 400_000, dtype=np.int32),
+          rng.integers(0, dom, 400_000, dtype=np.int32)]
+    rels = [R8, R3]
+    spec = [(0, list(range(8)), 0), (0, [0, 1, 2, -1, -1, -1, -1, 7], 0),
+            (1, [0, 3, -1], 0), (1, [0, -1, 5], 0), (1, [0, -1, -1], 0)]
+    want = oracle.evaluate(rels, B, P, spec, bits=8, nthreads=8)
+    assert want[0, 0] > 0 and want[0, 1] > 0  # the 8-column literal covers rows of both labels
+    base = fresh_ids(len(rels))
+    for i, r in enumerate(rels):
+        engine.register_relation(base + i, r)
+    lits = [Literal(base + r, tuple(v), j) for r, v, j in spec]
+    cols = []
+    for c in B:
+        t = torch.zeros(n + offset, dtype=torch.int32, device="cuda")
+        t[offset:] = torch.from_numpy(c).cuda()
+        cols.append(t[offset:])
+    assert all((c.data_ptr() % 16 == 0) == (offset == 0) for c in cols)
+    b = engine.bindings(cols, P)
+    try:
+        for bits, pass1 in ((0, 0), (9, 0), (16, 7)):
+            engine.set_option(C.QFG_OPT_EVAL_BITS, bits)
+            engine.set_option(C.QFG_OPT_PASS1_BITS, pass1)
+            np.testing.assert_array_equal(engine.evaluate_step(b, lits), want)
+    finally:
+        engine.set_option(C.QFG_OPT_EVAL_BITS, 0)
+        engine.set_option(C.QFG_OPT_PASS1_BITS, 0)
