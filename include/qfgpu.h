@@ -264,8 +264,10 @@ int qfg_server_destroy(qfg_server* server);
 /* RadixPartition (operations/RadixPartition.hpp:13-14, .cpp:56-186):
  * stable partition of n int32 values by ((uint32)v) & (2^bits - 1) into
  * PartitionTuple{int32 value, int32 tuple_id} (storage/PartitionTuple.hpp:
- * 20-42).  d_out_tuples holds 2*n int32; d_offsets 2^bits + 1 int64
- * (partition p = tuples [offsets[p], offsets[p+1])).  1 <= bits <= 15. */
+ * 20-42).  d_out_tuples holds 2*n int32 and is 8-byte aligned (a tuple is
+ * stored as one 8-byte word; cudaMalloc memory qualifies), else the call
+ * returns QFG_ERR_INVALID; d_offsets 2^bits + 1 int64 (partition p = tuples
+ * [offsets[p], offsets[p+1])).  1 <= bits <= 15. */
 int qfg_radix_partition(qfg_ctx* ctx, const int32_t* d_values, int64_t n, int bits,
                         int32_t* d_out_tuples, int64_t* d_offsets);
 
@@ -291,7 +293,8 @@ int qfg_radix_partition_static(void* stream, const int32_t* d_values, int64_t n,
  * FoilHashTable layout (storage/FoilHashTable.cpp:34-49): for each non-empty
  * partition p, buckets[next_pow2(n_p)] of 1-based chain heads and next[n_p]
  * links, chains in descending position order, byte-identical to the
- * reference's.  Input is qfg_radix_partition's output.  d_bucket_offsets
+ * reference's.  Input is qfg_radix_partition's output (8-byte aligned,
+ * else QFG_ERR_INVALID).  d_bucket_offsets
  * (2^bits + 1 int64) receives where partition p's buckets start inside
  * d_buckets, which must hold at least 2*n + 2^bits int32; d_masks (2^bits
  * uint32) receives FoilHashTable::mask(); d_next holds n int32. */

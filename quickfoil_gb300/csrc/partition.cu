@@ -335,6 +335,8 @@ extern "C" int qfg_radix_partition(qfg_ctx* c, const int32_t* d_values, int64_t 
   if (bits < 1 || bits > QFG_MAX_RADIX_BITS || n < 0 || n > INT32_MAX || d_offsets == nullptr ||
       (n > 0 && (d_values == nullptr || d_out_tuples == nullptr)))
     return set_error(ctx, QFG_ERR_INVALID, "qfg_radix_partition: invalid arguments");
+  if (reinterpret_cast<uintptr_t>(d_out_tuples) % 8 != 0)
+    return set_error(ctx, QFG_ERR_INVALID, "qfg_radix_partition: d_out_tuples must be 8-byte aligned");
   return radix_partition_ref(ctx, d_values, n, bits, d_out_tuples, d_offsets);
 }
 
@@ -348,6 +350,9 @@ extern "C" int qfg_build_hash_table_on_partitions(qfg_ctx* c, const int32_t* d_t
       d_offsets == nullptr || d_bucket_offsets == nullptr || d_masks == nullptr ||
       (n > 0 && (d_tuples == nullptr || d_buckets == nullptr || d_next == nullptr)))
     return set_error(ctx, QFG_ERR_INVALID, "qfg_build_hash_table_on_partitions: invalid arguments");
+  if (reinterpret_cast<uintptr_t>(d_tuples) % 8 != 0)
+    return set_error(ctx, QFG_ERR_INVALID,
+                     "qfg_build_hash_table_on_partitions: d_tuples must be 8-byte aligned");
   const int P = 1 << bits;
   QFG_TRY(ctx->scratch[kScrTmpA].reserve(ctx, sizeof(uint32_t) * (size_t)(2 * P + 2)));
   uint32_t* nb = ctx->scratch[kScrTmpA].as<uint32_t>();
@@ -549,6 +554,8 @@ extern "C" int qfg_radix_partition_static(void* stream, const int32_t* d_values,
   if (bits < 1 || bits > QFG_MAX_RADIX_BITS || n < 0 || n > INT32_MAX || d_offsets == nullptr ||
       (n > 0 && (d_values == nullptr || d_out_tuples == nullptr)))
     return fail(QFG_ERR_INVALID, "qfg_radix_partition_static: invalid arguments");
+  if (reinterpret_cast<uintptr_t>(d_out_tuples) % 8 != 0)
+    return fail(QFG_ERR_INVALID, "qfg_radix_partition_static: d_out_tuples must be 8-byte aligned");
   const PassShape s = pass_shape(std::max<int64_t>(n, 1), bits);
   const int64_t entries = s.num_chunks * (int64_t(1) << bits);
   const int64_t tiles = (entries + kStaticScanTile - 1) / kStaticScanTile;

@@ -62,3 +62,18 @@ def test_context_creation_fails_cleanly_without_gpu():
     h = ctypes.c_void_p()
     assert lib.qfg_ctx_create(0, 0, ctypes.byref(h)) == C.QFG_ERR_CUDA
     assert not h.value
+
+
+def test_misaligned_partition_tuples_are_rejected_without_a_device():
+    """A PartitionTuple is stored as one 8-byte word, so an output array that
+    is only 4-byte aligned is refused with a status before any device work.
+    Run only where no GPU is present: the addresses are never dereferenced,
+    because the arguments are checked first."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = C.load()
+    err = ctypes.create_string_buffer(128)
+    rc = lib.qfg_radix_partition_static(None, 0x10000, 10, 5, 0x20004, 0x30000, err, len(err))
+    assert rc == C.QFG_ERR_INVALID
+    assert b"8-byte aligned" in err.value
