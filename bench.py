@@ -388,8 +388,12 @@ def run_gb300(args):
 
     # End to end, pipelined through the serving API: step i+1's binding set
     # uploads on the context stream while step i evaluates on a server slot.
+    # One slot: the steps take the GPU one after another while the uploads
+    # overlap them; with two slots consecutive steps evaluate concurrently
+    # and contend for SMs and L2 (10.80 against 10.61 ms a step on the
+    # batched step).
     def pipelined(steps):
-        srv = eng.server(slots=2)
+        srv = eng.server(slots=1)
         prev, got = None, None
         for _ in range(steps):
             be = eng.bindings(pinned, w.num_positive)
@@ -450,9 +454,9 @@ def run_gb300(args):
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": pipe_s * 1e3,
                     "ms_per_step_repeats": [round(x * 1e3, 3) for x in pipe_runs],
-                    "mode": "pipelined through qfg_server: each step uploads its binding set "
-                            "from pinned host memory (qfg_bindings_create) while the previous "
-                            "step evaluates, counts read back to the host every step",
+                    "mode": "pipelined through qfg_server (one slot): each step uploads its "
+                            "binding set from pinned host memory (qfg_bindings_create) while the "
+                            "previous step evaluates, counts read back to the host every step",
                     "counts_equal_device_path": bool(np.array_equal(pipe_counts, batched_counts))},
             "e2e_serial": {"value": n * world / e2e_s, "unit": "literals/s",
                            "ms_per_step": e2e_s * 1e3,
