@@ -391,9 +391,10 @@ def run_gb300(args):
     # One slot: the steps take the GPU one after another while the uploads
     # overlap them; with two slots consecutive steps evaluate concurrently
     # and contend for SMs and L2 (10.80 against 10.61 ms a step on the
-    # batched step).
+    # batched step).  Depth 2: the next step is queued on the slot's stream
+    # behind the running one, so no host turnaround separates them.
     def pipelined(steps):
-        srv = eng.server(slots=1)
+        srv = eng.server(slots=1, depth=2)
         prev, got = None, None
         for _ in range(steps):
             be = eng.bindings(pinned, w.num_positive)
@@ -454,7 +455,7 @@ def run_gb300(args):
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": pipe_s * 1e3,
                     "ms_per_step_repeats": [round(x * 1e3, 3) for x in pipe_runs],
-                    "mode": "pipelined through qfg_server (one slot): each step uploads its "
+                    "mode": "pipelined through qfg_server (one slot, depth 2): each step uploads its "
                             "binding set from pinned host memory (qfg_bindings_create) while the "
                             "previous step evaluates, counts read back to the host every step",
                     "counts_equal_device_path": bool(np.array_equal(pipe_counts, batched_counts))},

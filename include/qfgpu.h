@@ -63,7 +63,9 @@ enum {
   QFG_OPT_SHARD_INDEX = 6,      /* this context's shard of the partition space (default 0) */
   QFG_OPT_SHARD_COUNT = 7,      /* number of shards (default 1); see qfg_evaluate_step */
   QFG_OPT_AUTOTUNE = 8,         /* 1 = use the partition bits qfg_autotune_step chose per size class */
-  QFG_OPT_PASS1_BITS = 9        /* pass-1 bits of a two-pass partition (0 = automatic, else 1..8) */
+  QFG_OPT_PASS1_BITS = 9,       /* pass-1 bits of a two-pass partition (0 = automatic, else 1..8) */
+  QFG_OPT_SERVER_DEPTH = 10     /* requests a server slot holds at once, 1..8 (default 1); read by
+                                   qfg_server_create (see the serving loop below) */
 };
 
 /* Evaluation stages timed under QFG_OPT_STAGE_TIMING (the GPU counterpart of
@@ -248,7 +250,12 @@ int qfg_step_graph_destroy(qfg_ctx* ctx, qfg_step_graph* graph);
  * after the work queued on the context's stream when it was submitted, so a
  * binding set uploaded with qfg_bindings_create just before its submission
  * is complete when the request starts (and the next upload can overlap the
- * request).  While a server is alive the context runs no other evaluation. */
+ * request).  With QFG_OPT_SERVER_DEPTH = d > 1 at creation a slot holds up
+ * to d requests: the ones after the first are queued on the slot's stream
+ * behind it (no host turnaround between them on the GPU) and the slot's
+ * requests run one after another; qfg_server_wait then waits for its
+ * request alone.  While a server is alive the context runs no other
+ * evaluation. */
 typedef struct qfg_server qfg_server;
 int qfg_server_create(qfg_ctx* ctx, int32_t slots, int64_t hbm_budget_bytes, qfg_server** out);
 int qfg_server_submit(qfg_server* server, const qfg_bindings* bindings, int32_t num_literals,

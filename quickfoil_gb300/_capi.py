@@ -39,6 +39,7 @@ QFG_OPT_SHARD_INDEX = 6
 QFG_OPT_SHARD_COUNT = 7
 QFG_OPT_AUTOTUNE = 8
 QFG_OPT_PASS1_BITS = 9
+QFG_OPT_SERVER_DEPTH = 10
 
 STAGES = ("key_tables", "bind_partition", "evaluate", "per_literal", "unit_plan",
           "coverage_scan", "coverage_examples")

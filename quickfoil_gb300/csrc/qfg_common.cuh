@@ -178,6 +178,7 @@ struct Ctx {
   bool autotune = false;
   std::map<int, std::pair<int, int>> tuned_bits;
   int eval_cbits = 0;
+  int server_depth = 1;  // QFG_OPT_SERVER_DEPTH: requests a server slot holds
   int shard_index = 0;
   int shard_count = 1;
   int64_t launches = 0;

@@ -436,6 +436,11 @@ extern "C" int qfg_ctx_set_option(qfg_ctx* c, int option, int64_t value) {
         return set_error(ctx, QFG_ERR_INVALID, "pass-1 bits out of range [0, 8]");
       ctx->eval_cbits = (int)value;
       return QFG_OK;
+    case QFG_OPT_SERVER_DEPTH:
+      if (value < 1 || value > 8)
+        return set_error(ctx, QFG_ERR_INVALID, "server depth out of range [1, 8]");
+      ctx->server_depth = (int)value;
+      return QFG_OK;
     default:
       return set_error(ctx, QFG_ERR_INVALID, "unknown option " + std::to_string(option));
   }

@@ -10,13 +10,17 @@
 // evaluated by a replay.
 //
 // Serving.  A server owns `slots` workspaces, each with its own stream and
-// pinned count buffer.  Requests (a device-resident binding set plus a batch
-// of candidate literals) are admitted in arrival order when a slot is free
+// pinned count buffers.  Requests (a device-resident binding set plus a batch
+// of candidate literals) are admitted in arrival order when a slot has room
 // and the scratch they need fits the server's HBM budget next to the
 // requests in flight; admitted requests run concurrently on their slots'
 // streams, and requests that arrive meanwhile are admitted as slots and
-// memory free up (continuous batching).  Completion is stamped on the host by
-// a stream callback; latency = completion - submission.
+// memory free up (continuous batching).  A slot holds up to `depth`
+// requests (QFG_OPT_SERVER_DEPTH): the ones after the first are queued on
+// its stream behind it, so consecutive requests of a slot follow each other
+// on the GPU without a host turnaround between them, sharing the slot's
+// workspace in stream order.  Completion is stamped on the host by a stream
+// callback; latency = completion - submission.
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -217,17 +221,31 @@ struct Request {
   // Recorded on the context stream at submission: work queued there before
   // (e.g. the upload of this request's binding set) precedes the request.
   cudaEvent_t ready = nullptr;
+  // Recorded on the slot stream after the completion callback: a wait for
+  // this request alone (the slot's stream may hold requests queued behind).
+  cudaEvent_t complete = nullptr;
+  int buf = -1;           // the slot's pinned count buffer it uses
+  bool retired = false;   // counts copied out, slot room given back
   ~Request() {
     if (ready != nullptr) cudaEventDestroy(ready);
+    if (complete != nullptr) cudaEventDestroy(complete);
   }
+};
+
+struct PinnedCounts {
+  int64_t* p = nullptr;
+  size_t cap = 0;  // int64 values
 };
 
 struct Slot {
   Workspace ws;
   cudaStream_t stream = nullptr;
-  int64_t* pinned_counts = nullptr;
-  size_t pinned_cap = 0;
-  Request* running = nullptr;
+  // One pinned count buffer per request the slot can hold, used in turn:
+  // requests of a slot retire in admission order, so a buffer comes round
+  // again only after its previous request retired.
+  std::vector<PinnedCounts> counts;
+  int next_buf = 0;
+  std::deque<Request*> running;  // admitted, in stream order
 };
 
 void CUDART_CB mark_done(void* user) {
@@ -241,6 +259,7 @@ void CUDART_CB mark_done(void* user) {
 struct qfg_server {
   Ctx* ctx = nullptr;
   int64_t budget = 0;
+  int depth = 1;  // requests a slot holds at once
   std::vector<Slot> slots;
   std::deque<Request*> queue;
   std::vector<Request*> all;
@@ -257,13 +276,16 @@ int server_admit(qfg_server* s) {
   Ctx* ctx = s->ctx;
   while (!s->queue.empty()) {
     Request* r = s->queue.front();
+    // The slot holding the fewest requests, if it has room.
     int free_slot = -1;
+    size_t fewest = (size_t)s->depth;
     int running = 0;
     for (size_t i = 0; i < s->slots.size(); ++i) {
-      if (s->slots[i].running == nullptr) {
-        if (free_slot < 0) free_slot = (int)i;
-      } else {
-        ++running;
+      const size_t k = s->slots[i].running.size();
+      running += (int)k;
+      if (k < fewest) {
+        fewest = k;
+        free_slot = (int)i;
       }
     }
     if (free_slot < 0) return QFG_OK;
@@ -275,12 +297,15 @@ int server_admit(qfg_server* s) {
                             "request needs more scratch than the server's HBM budget");
       r->finished = Clock::now();
       r->done.store(1, std::memory_order_release);
+      r->retired = true;
       s->finished.push_back(r->id);
       continue;
     }
     Slot& slot = s->slots[free_slot];
     r->slot = free_slot;
-    slot.running = r;
+    r->buf = slot.next_buf;
+    slot.next_buf = (slot.next_buf + 1) % s->depth;
+    slot.running.push_back(r);
     s->in_flight_bytes += r->scratch_bytes;
     s->peak_in_flight = std::max<int64_t>(s->peak_in_flight, running + 1);
     // Idle slots give their cached scratch back when it would not fit.
@@ -288,18 +313,19 @@ int server_admit(qfg_server* s) {
     for (const Slot& o : s->slots) held += o.ws.bytes();
     if (held - slot.ws.bytes() + r->scratch_bytes > s->budget) {
       for (Slot& o : s->slots)
-        if (o.running == nullptr && &o != &slot) o.ws.release();
+        if (o.running.empty() && &o != &slot) o.ws.release();
     }
     const int n = (int)r->literals.size();
     int st = QFG_OK;
-    if ((size_t)std::max(n, 1) * 4 > slot.pinned_cap) {
-      if (slot.pinned_counts != nullptr) cudaFreeHost(slot.pinned_counts);
-      slot.pinned_counts = nullptr;
-      slot.pinned_cap = 0;
-      cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&slot.pinned_counts),
+    PinnedCounts& pc = slot.counts[r->buf];
+    if ((size_t)std::max(n, 1) * 4 > pc.cap) {
+      if (pc.p != nullptr) cudaFreeHost(pc.p);
+      pc.p = nullptr;
+      pc.cap = 0;
+      cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&pc.p),
                                     sizeof(int64_t) * 4 * (size_t)std::max(n, 1), cudaHostAllocDefault);
       if (e != cudaSuccess) st = cuda_error(ctx, e, "cudaHostAlloc");
-      else slot.pinned_cap = (size_t)std::max(n, 1) * 4;
+      else pc.cap = (size_t)std::max(n, 1) * 4;
     }
     if (st == QFG_OK && r->ready != nullptr) {
       const cudaError_t e = cudaStreamWaitEvent(slot.stream, r->ready, 0);
@@ -322,7 +348,7 @@ int server_admit(qfg_server* s) {
         if (st == QFG_OK) st = enqueue_step(ctx, ps);
         prepared_step_free(ps);
         if (st == QFG_OK) {
-          cudaError_t e = cudaMemcpyAsync(slot.pinned_counts, dev, sizeof(int64_t) * 4 * (size_t)n,
+          cudaError_t e = cudaMemcpyAsync(pc.p, dev, sizeof(int64_t) * 4 * (size_t)n,
                                           cudaMemcpyDeviceToHost, ctx->stream);
           if (e != cudaSuccess) st = cuda_error(ctx, e, "count download");
         }
@@ -330,6 +356,12 @@ int server_admit(qfg_server* s) {
       if (st == QFG_OK) {
         cudaError_t e = cudaLaunchHostFunc(ctx->stream, mark_done, r);
         if (e != cudaSuccess) st = cuda_error(ctx, e, "cudaLaunchHostFunc");
+      }
+      if (st == QFG_OK) {
+        // After the callback in stream order: complete means done is set.
+        cudaError_t e = cudaEventCreateWithFlags(&r->complete, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(r->complete, ctx->stream);
+        if (e != cudaSuccess) st = cuda_error(ctx, e, "cudaEventRecord");
       }
     }
     if (st != QFG_OK) {
@@ -341,18 +373,22 @@ int server_admit(qfg_server* s) {
   return QFG_OK;
 }
 
-// Retires finished requests: copies their counts out and frees their slots.
+// Retires finished requests, each slot's in admission order: copies their
+// counts out and gives their room in the slot back.
 int server_reap(qfg_server* s) {
   for (Slot& slot : s->slots) {
-    Request* r = slot.running;
-    if (r == nullptr || !r->done.load(std::memory_order_acquire)) continue;
-    if (r->status == QFG_OK && !r->literals.empty())
-      memcpy(r->host_counts, slot.pinned_counts, sizeof(int64_t) * 4 * r->literals.size());
-    s->in_flight_bytes -= r->scratch_bytes;
-    slot.running = nullptr;
-    s->latencies_ms.push_back(
-        std::chrono::duration<double, std::milli>(r->finished - r->submitted).count());
-    s->finished.push_back(r->id);
+    while (!slot.running.empty()) {
+      Request* r = slot.running.front();
+      if (!r->done.load(std::memory_order_acquire)) break;
+      if (r->status == QFG_OK && !r->literals.empty())
+        memcpy(r->host_counts, slot.counts[r->buf].p, sizeof(int64_t) * 4 * r->literals.size());
+      s->in_flight_bytes -= r->scratch_bytes;
+      slot.running.pop_front();
+      r->retired = true;
+      s->latencies_ms.push_back(
+          std::chrono::duration<double, std::milli>(r->finished - r->submitted).count());
+      s->finished.push_back(r->id);
+    }
   }
   return QFG_OK;
 }
@@ -366,8 +402,10 @@ extern "C" int qfg_server_create(qfg_ctx* c, int32_t slots, int64_t hbm_budget_b
   auto s = new qfg_server();
   s->ctx = ctx;
   s->budget = hbm_budget_bytes > 0 ? hbm_budget_bytes : ctx->budget / 2;
+  s->depth = std::max(1, ctx->server_depth);
   s->slots.resize(slots);
   for (Slot& slot : s->slots) {
+    slot.counts.resize((size_t)s->depth);
     if (cudaStreamCreateWithFlags(&slot.stream, cudaStreamNonBlocking) != cudaSuccess) {
       cudaGetLastError();
       for (Slot& o : s->slots)
@@ -431,22 +469,22 @@ extern "C" int qfg_server_wait(qfg_server* s, int64_t request_id) {
   for (;;) {
     QFG_TRY(server_reap(s));
     QFG_TRY(server_admit(s));
-    if (target->done.load() && target->slot >= 0 && s->slots[target->slot].running != target) break;
-    if (target->done.load() && target->slot < 0) break;
-    if (target->slot < 0 && !target->done.load()) {
-      bool any = false;
-      for (Slot& slot : s->slots) any = any || slot.running != nullptr;
-      if (!any) return set_error(s->ctx, QFG_ERR_INVALID, "request cannot be admitted");
-    }
-    // Block on the stream of the slot the request runs on, or on any busy one.
-    cudaStream_t wait_on = nullptr;
-    if (target->slot >= 0 && s->slots[target->slot].running == target)
-      wait_on = s->slots[target->slot].stream;
-    else
+    if (target->retired) break;
+    // Block on the request itself once it is admitted, else on the oldest
+    // request of a busy slot (its retirement makes room).  A request whose
+    // admission failed has no event: it is done and retires once the
+    // requests ahead of it in its slot do.
+    Request* w = nullptr;
+    if (target->slot >= 0) {
+      const Slot& sl = s->slots[target->slot];
+      w = target->complete != nullptr ? target : (sl.running.empty() ? nullptr : sl.running.front());
+    } else {
       for (Slot& slot : s->slots)
-        if (slot.running != nullptr) wait_on = slot.stream;
-    if (wait_on == nullptr) break;
-    QFG_CUDA(s->ctx, cudaStreamSynchronize(wait_on));
+        if (w == nullptr && !slot.running.empty()) w = slot.running.front();
+      if (w == nullptr) return set_error(s->ctx, QFG_ERR_INVALID, "request cannot be admitted");
+    }
+    if (w == nullptr) break;
+    if (w->complete != nullptr) QFG_CUDA(s->ctx, cudaEventSynchronize(w->complete));
   }
   return target->status;
 }
@@ -458,7 +496,7 @@ extern "C" int qfg_server_drain(qfg_server* s) {
     QFG_TRY(server_admit(s));
     bool busy = false;
     for (Slot& slot : s->slots)
-      if (slot.running != nullptr) {
+      if (!slot.running.empty()) {
         busy = true;
         QFG_CUDA(s->ctx, cudaStreamSynchronize(slot.stream));
       }
@@ -489,7 +527,8 @@ extern "C" int qfg_server_destroy(qfg_server* s) {
   qfg_server_drain(s);
   for (Slot& slot : s->slots) {
     slot.ws.release();
-    if (slot.pinned_counts != nullptr) cudaFreeHost(slot.pinned_counts);
+    for (PinnedCounts& pc : slot.counts)
+      if (pc.p != nullptr) cudaFreeHost(pc.p);
     if (slot.stream != nullptr) cudaStreamDestroy(slot.stream);
   }
   for (Request* r : s->all) delete r;

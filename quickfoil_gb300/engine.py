@@ -328,8 +328,10 @@ class Engine:
         (device, 4*n int64)."""
         return StepGraph(self, bindings, literals, counts_dev_ptr)
 
-    def server(self, slots: int = 4, hbm_budget: int = 0) -> "StepServer":
-        """A serving loop over concurrent requests of many rule searches."""
+    def server(self, slots: int = 4, hbm_budget: int = 0, depth: int = 1) -> "StepServer":
+        """A serving loop over concurrent requests of many rule searches;
+        ``depth`` requests a slot holds at once (queued on its stream)."""
+        self.set_option(C.QFG_OPT_SERVER_DEPTH, depth)
         return StepServer(self, slots, hbm_budget)
 
     # -- API-kept operators (torch CUDA tensors) ------------------------------

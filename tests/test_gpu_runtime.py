@@ -77,8 +77,8 @@ def _requests(engine, seeds, sizes):
     return reqs
 
 
-@pytest.mark.parametrize("slots", [1, 3, 8])
-def test_served_requests_equal_direct_steps(engine, slots):
+@pytest.mark.parametrize("slots,depth", [(1, 1), (3, 1), (8, 1), (1, 2), (2, 3)])
+def test_served_requests_equal_direct_steps(engine, slots, depth):
     reqs = _requests(engine, range(10, 22), [500, 200000, 3000, 70000, 1, 40000, 9000, 120000,
                                              2500, 60000, 800, 30000])
     # the oracle pins the direct counts of two of them
@@ -87,7 +87,7 @@ def test_served_requests_equal_direct_steps(engine, slots):
         got = oracle.evaluate(w.relations, w.binding_columns, w.num_positive,
                               [(l.relation - base, l.vars, l.join_pos) for l in lits], bits=5)
         np.testing.assert_array_equal(want, got)
-    srv = engine.server(slots=slots)
+    srv = engine.server(slots=slots, depth=depth)
     ids = [srv.submit(b, lits) for _, b, lits, _ in reqs]
     seen = srv.poll()
     srv.result(ids[len(ids) // 2])
@@ -100,8 +100,8 @@ def test_served_requests_equal_direct_steps(engine, slots):
     st = srv.stats()
     assert st["completed"] == len(ids)
     assert 0 < st["p50_ms"] <= st["p99_ms"]
-    assert 1 <= st["peak_in_flight"] <= slots
-    if slots > 1:
+    assert 1 <= st["peak_in_flight"] <= slots * depth
+    if slots * depth > 1:
         assert st["peak_in_flight"] > 1
     srv.close()
     for _, b, _, _ in reqs:
@@ -187,9 +187,12 @@ def test_autotuner_picks_bits_and_keeps_counts(engine):
     b.close()
 
 
-def test_served_request_waits_for_its_binding_upload(engine):
+@pytest.mark.parametrize("slots,depth", [(2, 1), (1, 2)])
+def test_served_request_waits_for_its_binding_upload(engine, slots, depth):
     """Binding sets uploaded from host memory right before submission: the
-    request starts after the upload, and the next upload overlaps it."""
+    request starts after the upload, and the next upload overlaps it.  With
+    one slot of depth 2 the next request is queued behind the running one
+    and each result is waited for before the one after it is submitted."""
     reqs = []
     for seed in (50, 51, 52):
         w = workloads.small_random(seed, n_bindings=300_000, max_tuples=8000, num_literals=30)
@@ -197,12 +200,14 @@ def test_served_request_waits_for_its_binding_upload(engine):
         b = engine.bindings(w.binding_columns, w.num_positive)
         reqs.append((w, lits, engine.evaluate_step(b, lits)))
         b.close()
-    srv = engine.server(slots=2)
+    srv = engine.server(slots=slots, depth=depth)
     ids, keep = [], []
-    for w, lits, _ in reqs * 2:
+    for i, (w, lits, want) in enumerate(reqs * 2):
         b = engine.bindings(w.binding_columns, w.num_positive)  # host upload on the context stream
         ids.append(srv.submit(b, lits))
         keep.append(b)
+        if depth > 1 and i > 0:  # the pipelined pattern: result of the previous request
+            np.testing.assert_array_equal(srv.result(ids[i - 1]), (reqs * 2)[i - 1][2])
     for rid, (_, _, want) in zip(ids, reqs * 2):
         np.testing.assert_array_equal(srv.result(rid), want)
     srv.close()
