@@ -1657,7 +1657,12 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_batched_kernel,
                                                                kEvalThreads, L.smem));
     L.grid = ctx->num_sms * std::max(per_sm, 1);
-    L.gather_grid = ctx->num_sms * 8;
+    // One wave of resident gather blocks: each block strides over the units,
+    // so blocks beyond what the SMs hold at once would run as a second wave.
+    int gather_per_sm = 0;
+    QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gather_per_sm, gather_entries_kernel,
+                                                                32 * kGatherWarps, 0));
+    L.gather_grid = ctx->num_sms * std::max(gather_per_sm, 1);
     L.plan_grid = (int)std::max<int64_t>(
         1, std::min<int64_t>((ea.total_items + 255) / 256, (int64_t)ctx->num_sms * 8));
     ps->launches.push_back(L);
