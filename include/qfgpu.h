@@ -180,7 +180,7 @@ int qfg_evaluate_step(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_li
 
 /* The plain per-literal GPU path: one RadixPartition -> BuildHashTable ->
  * HashJoin -> Filter -> CountAggregator chain per literal, as the
- * reference runs it (operations/*), with the binding side re-partitioned
+ * reference runs it (the operations/ sources), with the binding side re-partitioned
  * for every literal. */
 int qfg_evaluate_per_literal(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
                              const qfg_literal* literals, int64_t* counts, int flags);

@@ -77,3 +77,20 @@ def test_misaligned_partition_tuples_are_rejected_without_a_device():
     rc = lib.qfg_radix_partition_static(None, 0x10000, 10, 5, 0x20004, 0x30000, err, len(err))
     assert rc == C.QFG_ERR_INVALID
     assert b"8-byte aligned" in err.value
+
+
+@pytest.mark.parametrize("lang,std", [("c", "c99"), ("c++", "c++17")])
+def test_header_compiles_cleanly_for_c_and_cpp_callers(tmp_path, lang, std):
+    """include/qfgpu.h is the boundary a C (cgo, ctypes, JNI glue) or C++
+    caller includes: it must compile on its own without warnings."""
+    import shutil
+    import subprocess
+    cc = "gcc" if lang == "c" else "g++"
+    if shutil.which(cc) is None:
+        pytest.skip(f"{cc} not installed")
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "qfgpu.h"\nint main(void) { return qfg_version() > 0 ? 0 : 1; }\n')
+    r = subprocess.run([cc, "-x", lang, f"-std={std}", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                        "-I", os.path.join(ROOT, "include"), "-c", str(src), "-o",
+                        str(tmp_path / "use_header.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
