@@ -746,7 +746,7 @@ constexpr int kTileStride = kTile + 8;
 size_t eval_smem_bytes(int num_lits, int max_cols) {
   return sizeof(unsigned long long) * 4 * (size_t)num_lits +
          sizeof(int32_t) * (size_t)max_cols * kTileStride + sizeof(uint32_t) * 3 * kSlots +
-         sizeof(uint16_t) * 3 * kTile;
+         sizeof(uint16_t) * 4 * kTile;
 }
 
 // One segment of a tile column: global rows [g0, g0 + c) to shared index
@@ -945,9 +945,11 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
   uint16_t* rslot = reinterpret_cast<uint16_t*>(sstart + kSlots);     // kTile
   uint16_t* rrank = rslot + kTile;                                    // kTile
   uint16_t* rows = rrank + kTile;                                     // kTile: shared positions
+  uint16_t* klist = rows + kTile;  // kTile: the slots of the tile's distinct keys, in claim order
   __shared__ __align__(8) uint64_t s_bar;
   __shared__ WorkUnit s_unit;
   __shared__ uint32_t s_idx, s_count;
+  __shared__ uint32_t s_nkeys;  // distinct keys of the current tile (entries of klist)
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
 
@@ -957,6 +959,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     cnt[i] = 0u;
   }
   if (threadIdx.x == 0) {
+    s_nkeys = 0u;
     s_count = umin(a.unit_count[0], a.unit_cap);
     s_idx = atomicAdd(a.work_counter, 1u);
     if (s_idx < s_count) s_unit = a.units[s_idx];
@@ -1081,7 +1084,11 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         uint32_t slot = mix32((uint32_t)key) & (kSlots - 1);
         for (int probe = 0; probe < kSlots; ++probe) {
           const uint32_t o = atomicCAS(&owner[slot], 0u, pos + 1u);
-          if (o == 0u || raw[o - 1u] == key) break;
+          if (o == 0u) {
+            klist[atomicAdd(&s_nkeys, 1u)] = (uint16_t)slot;
+            break;
+          }
+          if (raw[o - 1u] == key) break;
           slot = (slot + 1) & (kSlots - 1);
         }
         const uint32_t old = atomicAdd(&cnt[slot], posr ? 1u : 0x10000u);
@@ -1093,30 +1100,29 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
       {
         // Owners become keys (probes compare keys directly); with atom
         // literals, slot starts for per-key row lists, positives first.
-        constexpr int kPer = kSlots / kEvalThreads;
-        uint32_t v[kPer], key[kPer];
-        uint32_t sum = 0;
-#pragma unroll
-        for (int k = 0; k < kPer; ++k) {
-          const int sl = threadIdx.x * kPer + k;
-          const uint32_t w = cnt[sl];
-          v[k] = (w & 0xffffu) + (w >> 16);
-          key[k] = w != 0u ? (uint32_t)raw[owner[sl] - 1u] : 0u;
-          sum += v[k];
-        }
+        // Only the claimed slots are visited: each thread takes a run of
+        // consecutive entries of the key list.
+        const uint32_t nk = s_nkeys;
+        const uint32_t per = (nk + kEvalThreads - 1u) / kEvalThreads;
+        const uint32_t d0 = umin(nk, threadIdx.x * per), d1 = umin(nk, d0 + per);
         if (has_atoms) {
-          uint32_t run = block_scan_excl(sum, s_warp, &s_total);
-#pragma unroll
-          for (int k = 0; k < kPer; ++k) {
-            sstart[threadIdx.x * kPer + k] = run;
-            run += v[k];
+          uint32_t sum = 0;
+          for (uint32_t d = d0; d < d1; ++d) {
+            const uint32_t w = cnt[klist[d]];
+            sum += (w & 0xffffu) + (w >> 16);
           }
-        } else {
-          __syncthreads();  // every owner read before any is overwritten
+          uint32_t run = block_scan_excl(sum, s_warp, &s_total);
+          for (uint32_t d = d0; d < d1; ++d) {
+            const uint32_t sl = klist[d];
+            const uint32_t w = cnt[sl];
+            sstart[sl] = run;
+            run += (w & 0xffffu) + (w >> 16);
+          }
         }
-#pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          if (v[k] != 0u) owner[threadIdx.x * kPer + k] = key[k];
+        for (uint32_t d = d0; d < d1; ++d) {
+          const uint32_t sl = klist[d];
+          owner[sl] = (uint32_t)raw[owner[sl] - 1u];
+        }
       }
       __syncthreads();
       if (has_atoms) {
@@ -1202,11 +1208,16 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         cn += hn;
       }
       __syncthreads();
-      for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-        owner[rslot[i]] = 0u;
-        cnt[rslot[i]] = 0u;
+      {
+        const uint32_t nk = s_nkeys;
+        for (uint32_t d = threadIdx.x; d < nk; d += blockDim.x) {
+          const uint32_t sl = klist[d];
+          owner[sl] = 0u;
+          cnt[sl] = 0u;
+        }
       }
       __syncthreads();
+      if (threadIdx.x == 0) s_nkeys = 0u;  // read by every thread above; next read after a barrier
     }
     // Threads' entries are contiguous and increasing, so equal literals sit
     // on consecutive lanes; idle lanes (Lrun = -1) trail.
