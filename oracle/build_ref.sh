@@ -13,6 +13,13 @@ set -euo pipefail
 REF="${QF_REFERENCE:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
+# --where prints the reference checkout this script reads and exits (1 when
+# its sources are absent), so other checker scripts name no path of their own.
+if [ "${1:-}" = "--where" ]; then
+  echo "$REF"
+  [ -d "$REF/operations" ]
+  exit $?
+fi
 if [ ! -d "$REF/operations" ]; then
   echo "build_ref: no reference sources at $REF; skipped"
   exit 0
@@ -36,13 +43,18 @@ for p in "${pids[@]}"; do wait "$p"; done
 # the shim types, so they are read from the objects.
 EVAL=$(nm "$OUT/obj/learner_CandidateLiteralEvaluator.o" | awk '$2 == "T" && $3 ~ /CandidateLiteralEvaluator8Evaluate/ {print $3}')
 EXT=$(nm "$OUT/obj/operations_MultiColumnHashJoin.o" | awk '$2 == "T" && $3 ~ /CreateLabelAwareBindingTables/ {print $3}')
-printf '#define QFREF_EVALUATE "%s"\n#define QFREF_EXTEND "%s"\n' "$EVAL" "$EXT" > "$OUT/wrap_names.h"
+SELECT=$(nm "$OUT/obj/operations_SemiJoinFactory.o" | awk '$2 == "T" && $3 ~ /SelectAndCreateSemiJoin/ {print $3}')
+CREATE=$(nm "$OUT/obj/operations_SemiJoinFactory.o" | awk '$2 == "T" && $3 ~ /14CreateSemiJoin/ {print $3}')
+AFTER=$(nm "$OUT/obj/operations_BuildHashTable.o" | awk '$2 == "T" && $3 ~ /BuildHashTableAfterSemiJoin/ {print $3}')
+printf '#define QFREF_EVALUATE "%s"\n#define QFREF_EXTEND "%s"\n#define QFREF_SELECT "%s"\n#define QFREF_CREATE "%s"\n#define QFREF_AFTER "%s"\n' \
+  "$EVAL" "$EXT" "$SELECT" "$CREATE" "$AFTER" > "$OUT/wrap_names.h"
 g++ $FLAGS -I"$OUT" -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.o" &
 p1=$!
 g++ $FLAGS -c "$HERE/ref_loader.cpp" -o "$OUT/obj/ref_loader.o" &
 p2=$!
 wait "$p1"
 wait "$p2"
-g++ -shared -o "$OUT/libqfref.so.tmp" "$OUT"/obj/*.o "-Wl,--wrap=$EVAL" "-Wl,--wrap=$EXT"
+g++ -shared -o "$OUT/libqfref.so.tmp" "$OUT"/obj/*.o "-Wl,--wrap=$EVAL" "-Wl,--wrap=$EXT" \
+  "-Wl,--wrap=$SELECT" "-Wl,--wrap=$CREATE" "-Wl,--wrap=$AFTER"
 mv "$OUT/libqfref.so.tmp" "$OUT/libqfref.so"
 echo "build_ref: $OUT/libqfref.so"

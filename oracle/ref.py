@@ -19,8 +19,16 @@ LIB_PATH = os.path.join(_HERE, "_ref", "libqfref.so")
 _lib = None
 
 
+def reference_dir():
+    """The reference checkout oracle/build_ref.sh reads (QF_REFERENCE or the
+    script's default), or None when its sources are absent."""
+    res = subprocess.run(["bash", os.path.join(_HERE, "build_ref.sh"), "--where"],
+                         capture_output=True, text=True)
+    return res.stdout.strip() if res.returncode == 0 else None
+
+
 def available() -> bool:
-    return os.path.exists(LIB_PATH) or os.path.isdir("/root/reference/operations")
+    return os.path.exists(LIB_PATH) or reference_dir() is not None
 
 
 def lib():
@@ -57,6 +65,13 @@ def lib():
         L.qfref_load_text.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(i32p), ctypes.c_int64, i64p]
         L.qfref_load_text.restype = ctypes.c_int
+        L.qfref_learn_compact.argtypes = L.qfref_learn.argtypes + [ctypes.POINTER(ctypes.c_double)]
+        L.qfref_learn_compact.restype = ctypes.c_int
+        L.qfref_build_after_semijoin.argtypes = [ctypes.c_int, ctypes.POINTER(i32p), ctypes.c_int64,
+                                                 ctypes.POINTER(ctypes.c_uint64), ctypes.c_int64,
+                                                 ctypes.c_int32, i32p, i32p,
+                                                 ctypes.POINTER(ctypes.c_uint32)]
+        L.qfref_build_after_semijoin.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -111,6 +126,23 @@ def learn(relations, target_columns, num_positive: int, max_clause_length: int,
     if rc != 0:
         raise RuntimeError(f"reference learner failed ({rc})")
     return [l for l in out.value.decode().splitlines() if l]
+
+
+def learn_compact(relations, target_columns, num_positive: int, max_clause_length: int,
+                  trace_path: str):
+    """Runs the reference learner with the compact trace (column checksums,
+    coverage steps; see oracle/ref_driver.cpp); returns (learnt clauses,
+    seconds in Learn, inside Evaluate, inside extensions, inside coverage)."""
+    keep_r, rptr, rnc, rnt = _relations(relations)
+    keep_t, tptr = _cols(target_columns)
+    out = ctypes.create_string_buffer(1 << 16)
+    secs = (ctypes.c_double * 4)()
+    rc = lib().qfref_learn_compact(len(relations), rnc, rnt, rptr, len(keep_t), len(keep_t[0]),
+                                   num_positive, tptr, max_clause_length, trace_path.encode(), out,
+                                   len(out), secs)
+    if rc != 0:
+        raise RuntimeError(f"reference learner failed ({rc})")
+    return [l for l in out.value.decode().splitlines() if l], tuple(secs)
 
 
 def coverage(relations, target_columns, target_num_positive: int, binding_columns,
@@ -181,3 +213,27 @@ def load_text(path: str, num_args: int, skipped=None):
     if rc != 0:
         raise RuntimeError(f"reference loader: {rc}")
     return [o[:rows.value] for o in keep[:kept]]
+
+
+def build_after_semijoin(keys, bits, chunk_rows: int, num_build_tuples: int, num_rows=None):
+    """The reference's BuildHashTableAfterSemiJoin (operations/BuildHashTable.
+    cpp:212-236) over the first num_rows rows (default: all) of `keys`
+    (projected columns, which may run longer) cut into chunk_rows-row chunks
+    with their semi-join bits (uint64 blocks); returns (buckets, next, mask)
+    with next[] zero at positions no chain reaches."""
+    keep, ptrs = _cols(keys)
+    n = len(keep[0]) if num_rows is None else num_rows
+    bits = np.ascontiguousarray(bits, dtype=np.uint64)
+    nb = 1
+    while nb < num_build_tuples:
+        nb <<= 1
+    buckets = np.zeros(nb, dtype=np.int32)
+    nxt = np.zeros(num_build_tuples, dtype=np.int32)
+    mask = ctypes.c_uint32()
+    rc = lib().qfref_build_after_semijoin(
+        len(keep), ptrs, n, bits.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), chunk_rows,
+        num_build_tuples, buckets.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+        nxt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ctypes.byref(mask))
+    if rc != 0:
+        raise ValueError(f"reference driver rejected the input ({rc})")
+    return buckets, nxt, int(mask.value)

@@ -59,6 +59,36 @@ def test_static_partition_equals_allocating_entry_point_twice(own_engine, bits, 
         assert torch.equal(tuples, want_t), f"tuples differ on call {call}"
 
 
+def test_static_partition_of_no_values_zeroes_the_offsets(own_engine):
+    for call in range(2):
+        vals = torch.empty(0, dtype=torch.int32, device="cuda")
+        rc, err, _, offsets = _static_partition(vals, 7)
+        assert rc == C.QFG_OK, err
+        _, want_o = own_engine.radix_partition(vals, 7)
+        torch.cuda.synchronize()
+        assert torch.equal(offsets, torch.zeros_like(offsets))
+        assert torch.equal(offsets, want_o), f"offsets differ on call {call}"
+
+
+def test_static_partition_at_the_exact_scratch_limit(own_engine):
+    # At 8 radix bits a warp chunk is 2048 values with 256 digit counts, and
+    # the scan adds one word per 4096 counts: 4095 chunks fill the 2^20-word
+    # array exactly (1 048 320 counts + 256 tile sums); one more value needs a
+    # 4096th chunk and is refused.
+    bits, n = 8, 4095 * 2048
+    rng = np.random.default_rng(8)
+    for call in range(2):
+        vals = torch.from_numpy(rng.integers(-2**31, 2**31, n).astype(np.int32)).cuda()
+        rc, err, tuples, offsets = _static_partition(vals, bits)
+        assert rc == C.QFG_OK, err
+        want_t, want_o = own_engine.radix_partition(vals, bits)
+        torch.cuda.synchronize()
+        assert torch.equal(offsets, want_o), f"offsets differ on call {call}"
+        assert torch.equal(tuples, want_t), f"tuples differ on call {call}"
+    rc, err, _, _ = _static_partition(torch.zeros(n + 1, dtype=torch.int32, device="cuda"), bits)
+    assert rc == C.QFG_ERR_INVALID and "static scratch" in err
+
+
 def test_static_partition_rejects_inputs_beyond_its_scratch():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
