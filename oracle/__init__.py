@@ -71,6 +71,10 @@ def lib():
         L.qfo_build_table_hash_table.argtypes = [ctypes.POINTER(i32p), ctypes.c_int, ctypes.c_int64,
                                                  i32p, i32p]
         L.qfo_build_table_hash_table.restype = ctypes.c_uint32
+        L.qfo_build_hash_table_after_semijoin.argtypes = [
+            ctypes.POINTER(i32p), ctypes.c_int, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64),
+            ctypes.c_int64, ctypes.c_int32, i32p, i32p]
+        L.qfo_build_hash_table_after_semijoin.restype = ctypes.c_uint32
         L.qfo_relcache_create.argtypes = []
         L.qfo_relcache_create.restype = ctypes.c_void_p
         L.qfo_relcache_destroy.argtypes = [ctypes.c_void_p]
@@ -94,6 +98,8 @@ def lib():
                                    ctypes.POINTER(_Literal), ctypes.c_int, ctypes.POINTER(_Table),
                                    ctypes.POINTER(_Table), u64p, i64p]
         L.qfo_coverage.restype = ctypes.c_int
+        L.qfo_coverage_compat.argtypes = L.qfo_coverage.argtypes
+        L.qfo_coverage_compat.restype = L.qfo_coverage.restype
         L.qfo_compact_rows.argtypes = [ctypes.c_int, ctypes.POINTER(i32p), ctypes.c_int64, u64p,
                                        ctypes.c_int, ctypes.POINTER(i32p)]
         L.qfo_compact_rows.restype = ctypes.c_int64
@@ -257,10 +263,12 @@ def extend_bindings(binding_columns, num_positive, relation_columns, literal,
 
 
 def coverage(binding_columns, num_positive, relation_columns, literal, num_target_columns,
-             uncovered_positive, negative=None):
+             uncovered_positive, negative=None, compat=False):
     """Covered counts of a literal appended to the building clause and the
     uncovered positives' bits; returns ((covered positives, covered
-    negatives), uint64 bit blocks)."""
+    negatives), uint64 bit blocks).  compat: the reference's own procedure
+    with its chunk-relative projection tables (qfo_coverage_compat) instead
+    of set membership."""
     b = _TableHandle(binding_columns)
     r = _TableHandle(relation_columns)
     u = _TableHandle(uncovered_positive)
@@ -269,7 +277,8 @@ def coverage(binding_columns, num_positive, relation_columns, literal, num_targe
     bits = np.zeros(max(1, (nu + 63) // 64), dtype=np.uint64)
     counts = np.zeros(2, dtype=np.int64)
     lit = _literal_struct(literal)
-    rc = lib().qfo_coverage(ctypes.byref(b.struct), num_positive, ctypes.byref(r.struct),
+    fn = lib().qfo_coverage_compat if compat else lib().qfo_coverage
+    rc = fn(ctypes.byref(b.struct), num_positive, ctypes.byref(r.struct),
                             ctypes.byref(lit), num_target_columns, ctypes.byref(u.struct),
                             ctypes.byref(ng.struct) if ng is not None else None,
                             bits.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
@@ -348,3 +357,35 @@ def parse_text(text: bytes, num_args: int, skipped=None):
     if rc != 0:
         raise TextError(rc, err.value)
     return [o[:rows.value] for o in outs[:kept]]
+
+
+def build_hash_table_after_semijoin(keys, bits, chunk_rows: int, num_build_tuples: int):
+    """BuildHashTableAfterSemiJoin restated (qf_oracle.c): (buckets, next,
+    mask) for `keys` cut into chunk_rows-row chunks (<= 0: one chunk) with
+    semi-join bits (uint64 blocks); next is 0 at positions never inserted."""
+    keys = _as_cols(keys)
+    n = len(keys[0])
+    bits = np.ascontiguousarray(bits, dtype=np.uint64)
+    nb = int(lib().qfo_num_buckets(num_build_tuples))
+    buckets = np.zeros(nb, dtype=np.int32)
+    nxt = np.zeros(num_build_tuples, dtype=np.int32)
+    mask = lib().qfo_build_hash_table_after_semijoin(
+        _colptrs(keys), len(keys), n, bits.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+        chunk_rows, num_build_tuples, buckets.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+        nxt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    return buckets, nxt, int(mask)
+
+
+def reachable_next(buckets, nxt):
+    """next[] with the entries of positions that no chain reaches set to 0:
+    the part of a chained table a probe can observe (the reference leaves
+    next[] of never-inserted positions uninitialised)."""
+    out = np.zeros_like(nxt)
+    seen = np.zeros(len(nxt), dtype=bool)
+    for h in buckets:
+        pos = int(h) - 1
+        while pos >= 0 and not seen[pos]:
+            seen[pos] = True
+            out[pos] = nxt[pos]
+            pos = int(nxt[pos]) - 1
+    return out

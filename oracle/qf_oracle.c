@@ -24,6 +24,9 @@ static inline uint32_t hash_combine(uint32_t seed, int32_t v) {
   return seed ^ (hash_i32(v) + 0x9e3779b9u + (seed << 6) + (seed >> 2));
 }
 
+static int keys_equal(const int32_t* const* a, int64_t ta, const int32_t* const* b, int64_t tb,
+                      int num_keys);
+
 uint32_t qfo_hash_keys(const int32_t* const* keys, int num_keys, int64_t tid) {
   uint32_t seed = hash_i32(keys[0][tid]);
   for (int i = 1; i < num_keys; ++i) seed = hash_combine(seed, keys[i][tid]);
@@ -95,6 +98,59 @@ uint32_t qfo_build_table_hash_table(const int32_t* const* keys, int num_keys, in
     const uint32_t bucket = qfo_hash_keys(keys, num_keys, i) & mask;
     next[i] = buckets[bucket];
     buckets[bucket] = (int32_t)i + 1;
+  }
+  return mask;
+}
+
+/* operations/BuildHashTable.cpp:127-189 (InsertIfNotPresent,
+ * BuildHashTableAfterSemiJoinImpl) with the chunking of
+ * operations/LeftSemiJoin.hpp:55-83; see qf_oracle.h. */
+static uint32_t after_semijoin_readable(const int32_t* const* keys, int num_keys, int64_t num_rows,
+                                        int64_t readable, const uint64_t* bits, int64_t chunk_rows,
+                                        int32_t num_build_tuples, int32_t* buckets, int32_t* next);
+
+uint32_t qfo_build_hash_table_after_semijoin(const int32_t* const* keys, int num_keys,
+                                             int64_t num_rows, const uint64_t* bits,
+                                             int64_t chunk_rows, int32_t num_build_tuples,
+                                             int32_t* buckets, int32_t* next) {
+  return after_semijoin_readable(keys, num_keys, num_rows, num_rows, bits, chunk_rows,
+                                 num_build_tuples, buckets, next);
+}
+
+/* As above; the columns go on past the last row up to `readable` rows,
+ * where a chain position of a short last chunk is read (beyond: unequal). */
+static uint32_t after_semijoin_readable(const int32_t* const* keys, int num_keys, int64_t num_rows,
+                                        int64_t readable, const uint64_t* bits, int64_t chunk_rows,
+                                        int32_t num_build_tuples, int32_t* buckets, int32_t* next) {
+  const int32_t nb = qfo_num_buckets(num_build_tuples);
+  const uint32_t mask = (uint32_t)nb - 1u;
+  memset(buckets, 0, sizeof(int32_t) * (size_t)nb);
+  memset(next, 0, sizeof(int32_t) * (size_t)num_build_tuples);
+  if (chunk_rows <= 0 || chunk_rows > num_rows) chunk_rows = num_rows;
+  const int32_t* chunk_keys[QFO_MAX_ARITY];
+  for (int64_t c0 = 0; c0 < num_rows; c0 += chunk_rows) {
+    const int64_t len = num_rows - c0 < chunk_rows ? num_rows - c0 : chunk_rows;
+    for (int k = 0; k < num_keys; ++k) chunk_keys[k] = keys[k] + c0;
+    for (int64_t tid = 0; tid < len; ++tid) {
+      const int64_t row = c0 + tid;
+      if (!((bits[row >> 6] >> (row & 63)) & 1u)) continue;
+      const uint32_t bucket = qfo_hash_keys(chunk_keys, num_keys, tid) & mask;
+      int exist = 0;
+      for (int32_t pos = buckets[bucket] - 1; pos >= 0; pos = next[pos] - 1) {
+        /* A position an earlier, longer chunk inserted can lie past the end
+         * of a short last chunk: the reference then reads on past the end of
+         * the columns.  Here such a position is read while the columns go
+         * on (`readable`) and compares unequal beyond. */
+        if (c0 + pos < readable && keys_equal(chunk_keys, tid, chunk_keys, pos, num_keys)) {
+          exist = 1;
+          break;
+        }
+      }
+      if (!exist) {
+        next[tid] = buckets[bucket];
+        buckets[bucket] = (int32_t)tid + 1;
+      }
+    }
   }
   return mask;
 }
@@ -671,4 +727,73 @@ int qfo_parse_text(const char* text, int64_t n, int num_args, const int32_t* ski
   }
   *num_rows = rows;
   return rows > capacity ? 1 : 0;
+}
+
+
+/* QuickFoil::ComputeCoverageOnUncoveredData (learner/QuickFoil.cpp:471-573)
+ * step by step as the reference runs it; see qf_oracle.h. */
+int qfo_coverage_compat(const qfo_table* bindings, int64_t num_positive, const qfo_table* relation,
+                        const qfo_literal* literal, int num_target_columns,
+                        const qfo_table* uncovered_positive, const qfo_table* negative,
+                        uint64_t* positive_bits, int64_t* num_covered) {
+  const int64_t nb = bindings->num_tuples, P = num_positive;
+  const int k = num_target_columns;
+  const int32_t* rel_keys[QFO_MAX_ARITY];
+  const int32_t* bind_keys[QFO_MAX_ARITY];
+  int nk = 0;
+  for (int i = 0; i < literal->num_args; ++i) {
+    if (literal->vars[i] < 0) continue;
+    if (literal->vars[i] >= bindings->num_columns) return 1;
+    rel_keys[nk] = relation->columns[i];
+    bind_keys[nk] = bindings->columns[literal->vars[i]];
+    ++nk;
+  }
+  if (nk == 0 || k < 1 || k > bindings->num_columns) return 1;
+  num_covered[0] = num_covered[1] = 0;
+  const qfo_table* ex_tab[2] = {uncovered_positive, negative};
+  if (positive_bits != NULL && uncovered_positive != NULL)
+    memset(positive_bits, 0, sizeof(uint64_t) * (size_t)((uncovered_positive->num_tuples + 63) / 64));
+  const int64_t start[2] = {0, P}, rows_of[2] = {P, nb - P};
+  for (int s = 0; s < 2; ++s) {
+    const int64_t rows = rows_of[s];
+    const qfo_table* ex = ex_tab[s];
+    if (rows == 0 || ex == NULL || ex->num_tuples == 0 || relation->num_tuples == 0) continue;
+    /* First semi-join: the side's rows against the relation (membership). */
+    const int32_t* probe[QFO_MAX_ARITY];
+    const int32_t* target[QFO_MAX_ARITY];
+    for (int q = 0; q < nk; ++q) probe[q] = bind_keys[q] + start[s];
+    for (int q = 0; q < k; ++q) target[q] = bindings->columns[q] + start[s];
+    uint64_t* member = calloc((size_t)((rows + 63) / 64), sizeof(uint64_t));
+    qfo_left_semijoin(probe, rows, rel_keys, relation->num_tuples, nk, member);
+    /* SelectAndCreateSemiJoin (operations/SemiJoinFactory.cpp:45-82): one
+     * chunk (right semi-join) when the side is smaller than the relation,
+     * else 32768-row chunks (FLAGS_semijoin_chunck_size).  The positive side
+     * is a view of the consecutive binding columns: reads past its end land
+     * on the negative rows. */
+    const int64_t chunk = rows < relation->num_tuples ? 0 : 32768;
+    const int64_t readable = s == 0 ? nb : rows;
+    const int32_t nbt = (int32_t)rows;
+    const int32_t nbk = qfo_num_buckets(nbt);
+    int32_t* buckets = malloc(sizeof(int32_t) * (size_t)nbk);
+    int32_t* next = malloc(sizeof(int32_t) * (size_t)nbt);
+    const uint32_t mask = after_semijoin_readable(target, k, rows, readable, member, chunk, nbt,
+                                                  buckets, next);
+    /* Second semi-join: the examples probed through that table against the
+     * side's rows (LeftSemiJoin::DoSemiJoin, operations/LeftSemiJoin.hpp:
+     * 86-141). */
+    for (int64_t e = 0; e < ex->num_tuples; ++e) {
+      const uint32_t b = qfo_hash_keys(ex->columns, k, e) & mask;
+      for (int32_t pos = buckets[b] - 1; pos >= 0; pos = next[pos] - 1) {
+        if (keys_equal(ex->columns, e, target, pos, k)) {
+          ++num_covered[s];
+          if (s == 0 && positive_bits != NULL) positive_bits[e >> 6] |= (uint64_t)1 << (e & 63);
+          break;
+        }
+      }
+    }
+    free(buckets);
+    free(next);
+    free(member);
+  }
+  return 0;
 }

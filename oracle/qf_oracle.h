@@ -75,6 +75,32 @@ uint32_t qfo_hash_keys(const int32_t* const* keys, int num_keys, int64_t tid);
 uint32_t qfo_build_table_hash_table(const int32_t* const* keys, int num_keys, int64_t n,
                                     int32_t* buckets, int32_t* next);
 
+/* BuildHashTableAfterSemiJoin (operations/BuildHashTable.cpp:127-189,
+ * 212-236) over the chunks a semi-join yields.  keys are the semi-join's
+ * projected columns (num_rows rows); bits (64-bit little-endian blocks)
+ * marks the rows that passed.  Chunk c covers rows [c*chunk_rows,
+ * min((c+1)*chunk_rows, num_rows)) -- LeftSemiJoin::Next cuts its probe side
+ * into FLAGS_semijoin_chunck_size rows and offsets the output columns by
+ * the chunk start (operations/LeftSemiJoin.hpp:55-83); chunk_rows <= 0 or
+ * >= num_rows is one chunk (RightSemiJoin::Next, operations/
+ * RightSemiJoin.hpp:44-82).  Each chunk's set positions are visited in
+ * increasing order (BitVectorIterator) and are chunk-relative: the id
+ * inserted is the position within the chunk and keys are read at the
+ * chunk's rows, also for the positions already in a chain
+ * (InsertIfNotPresent, :127-148: inserted at the head of its bucket unless
+ * the chain reaches a position with equal keys).  A chain position that
+ * lies past the end of a short last chunk (inserted by an earlier chunk)
+ * compares unequal; the reference reads past the end of its columns there.
+ * The table is
+ * FoilHashTable(num_build_tuples, 0): buckets[next_pow2(num_build_tuples)],
+ * next[num_build_tuples]; next entries of positions never inserted are 0
+ * here (the reference leaves them uninitialised).  num_build_tuples must
+ * exceed every chunk-relative position.  Returns the mask. */
+uint32_t qfo_build_hash_table_after_semijoin(const int32_t* const* keys, int num_keys,
+                                             int64_t num_rows, const uint64_t* bits,
+                                             int64_t chunk_rows, int32_t num_build_tuples,
+                                             int32_t* buckets, int32_t* next);
+
 /* Relation-partition cache, the analogue of TableView::partitions_
  * (storage/TableView.hpp:62-80): a relation column is partitioned once and
  * reused by every later evaluation (learner/CandidateLiteralEvaluator.cpp:296-299). */
@@ -139,6 +165,21 @@ int qfo_coverage(const qfo_table* bindings, int64_t num_positive, const qfo_tabl
                  const qfo_literal* literal, int num_target_columns,
                  const qfo_table* uncovered_positive, const qfo_table* negative,
                  uint64_t* positive_bits, int64_t* num_covered);
+
+/* ComputeCoverageOnUncoveredData as the reference runs it (the engine's
+ * QFG_OPT_COVERAGE_COMPAT): per label side, the bit vector of the side's
+ * rows against the relation (its first semi-join), the table
+ * BuildHashTableAfterSemiJoin builds from it with chunk-relative positions
+ * (32768-row chunks when the side is not smaller than the relation,
+ * operations/SemiJoinFactory.cpp:45-82), and the examples probed through
+ * that table against the side's rows.  The positive side reads past its end
+ * into the negative rows (a view of the consecutive binding columns); past
+ * the negative side's end a position compares unequal (the reference reads
+ * past its columns).  Same arguments and results as qfo_coverage. */
+int qfo_coverage_compat(const qfo_table* bindings, int64_t num_positive, const qfo_table* relation,
+                        const qfo_literal* literal, int num_target_columns,
+                        const qfo_table* uncovered_positive, const qfo_table* negative,
+                        uint64_t* positive_bits, int64_t* num_covered);
 
 /* The compaction of learner/QuickFoil.cpp:655-679 (bit vector flipped, then
  * AttributeReference::EvaluateWithFilter per column): rows whose bit is clear

@@ -954,6 +954,11 @@ extern "C" int qfg_coverage(qfg_ctx* c, const qfg_bindings* b, const qfg_literal
   QFG_TRY(check_examples(ctx, k, d_uncovered_positive, num_uncovered_positive,
                          "uncovered positives"));
   QFG_TRY(check_examples(ctx, k, d_negative, num_negative, "negatives"));
+  if (ctx->coverage_compat) {
+    const int32_t* const* cols[2] = {d_uncovered_positive, d_negative};
+    const int64_t ns[2] = {num_uncovered_positive, d_negative != nullptr ? num_negative : 0};
+    return coverage_compat(ctx, b, lit, k, cols, ns, d_positive_bits, num_covered);
+  }
   Examples ex[2];
   const int64_t n_side[2] = {b->num_positive, b->num_negative};
   ex[0].n = num_uncovered_positive;
@@ -1043,6 +1048,12 @@ extern "C" int qfg_coverage_examples(qfg_ctx* c, const qfg_bindings* b, const qf
                      "qfg_coverage_examples: positive and negative column counts differ");
   CoverageArgs a;
   QFG_TRY(coverage_args(ctx, b, lit, k, &a));
+  if (ctx->coverage_compat) {
+    const int32_t* const* cols[2] = {uncovered_positive->columns.data(),
+                                     negative != nullptr ? negative->columns.data() : nullptr};
+    const int64_t ns[2] = {uncovered_positive->num_rows, negative != nullptr ? negative->num_rows : 0};
+    return coverage_compat(ctx, b, lit, k, cols, ns, d_positive_bits, num_covered);
+  }
   Examples ex[2];
   const qfg_examples* src[2] = {uncovered_positive, negative};
   for (int s = 0; s < 2; ++s) {

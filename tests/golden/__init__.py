@@ -242,3 +242,16 @@ def text_cases():
         out.append((name, text, nargs, skipped, cols, int(z[f"x{i}_rows"][0]),
                     [int(v) for v in z[f"x{i}_checksum"]]))
     return out
+
+
+def after_semijoin_cases():
+    """[(keys, bits (uint64 blocks), chunk_rows, num_build_tuples, reference
+    buckets, reference next (0 where no chain reaches), reference mask)] of
+    BuildHashTableAfterSemiJoin (after_semijoin_cases.npz)."""
+    z = np.load(os.path.join(HERE, "after_semijoin_cases.npz"))
+    out = []
+    for j in range(int(z["num_cases"][0])):
+        n, k, chunk, nbt, mask = (int(v) for v in z[f"c{j}_meta"])
+        out.append(([z[f"c{j}_k{q}"] for q in range(k)], z[f"c{j}_bits"], chunk, nbt,
+                    z[f"c{j}_buckets"], z[f"c{j}_next"], mask))
+    return out

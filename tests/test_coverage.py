@@ -149,3 +149,25 @@ def test_oracle_compaction_keeps_rows_in_order(n, keep_set):
     keep = flags if keep_set else ~flags
     for g, c in zip(got, cols):
         np.testing.assert_array_equal(g, c[keep])
+
+
+def test_compat_coverage_oracle_equals_the_reference_everywhere():
+    """The oracle's restatement of the reference's own coverage procedure
+    (chunk-relative projection tables, qfo_coverage_compat) equals the
+    reference on every synthetic case, the divergent one included, where
+    set membership does not."""
+    from tests import golden
+    seen_divergent = False
+    for case, want_counts, want_flags, _ in golden.coverage_cases()[0]:
+        rels, T, tP, B, bP, lit, rows, divergent = case
+        U = [t[rows] for t in T]
+        got, bits = oracle.coverage(B, bP, rels[0], lit.as_tuple(), len(T), U, [t[tP:] for t in T],
+                                    compat=True)
+        assert got == want_counts
+        np.testing.assert_array_equal(bits_to_flags(bits, len(rows)), want_flags)
+        if divergent:
+            seen_divergent = True
+            member, _ = oracle.coverage(B, bP, rels[0], lit.as_tuple(), len(T), U,
+                                        [t[tP:] for t in T])
+            assert member != want_counts
+    assert seen_divergent

@@ -106,3 +106,16 @@ def test_added_literals_have_the_best_reference_score(name):
         best = max(s for s, _, _ in scored)
         chosen = [s for s, l, c in scored if l == lit and c[2:] == (npos, nneg)]
         assert chosen and chosen[0] == pytest.approx(best, abs=1e-5)
+
+
+def test_oracle_after_semijoin_table_matches_the_reference():
+    """BuildHashTableAfterSemiJoin restated (qf_oracle.c) against the
+    reference's own tables: one chunk, 32768-row chunks with chunk-relative
+    positions, short chunks, no or all bits set, seven keys."""
+    cases = golden.after_semijoin_cases()
+    assert any(chunk and len(keys[0]) > chunk for keys, _, chunk, *_ in cases)
+    for keys, bits, chunk, nbt, want_b, want_n, want_m in cases:
+        b, nx, m = oracle.build_hash_table_after_semijoin(keys, bits, chunk, nbt)
+        assert m == want_m
+        np.testing.assert_array_equal(b, want_b)
+        np.testing.assert_array_equal(oracle.reachable_next(b, nx), want_n)

@@ -32,8 +32,19 @@ def _register(engine, rels):
     return base
 
 
-def _gpu_coverage(engine, rels, B, bP, lit, k, U, negatives, bits=True, prepared=False):
-    """Through qfg_coverage, or (prepared) through qfg_coverage_examples."""
+def _gpu_coverage(engine, rels, B, bP, lit, k, U, negatives, bits=True, prepared=False,
+                  compat=False):
+    """Through qfg_coverage, or (prepared) through qfg_coverage_examples;
+    compat: under QFG_OPT_COVERAGE_COMPAT."""
+    from quickfoil_gb300 import _capi as C
+    engine.set_option(C.QFG_OPT_COVERAGE_COMPAT, 1 if compat else 0)
+    try:
+        return _gpu_coverage_run(engine, rels, B, bP, lit, k, U, negatives, bits, prepared)
+    finally:
+        engine.set_option(C.QFG_OPT_COVERAGE_COMPAT, 0)
+
+
+def _gpu_coverage_run(engine, rels, B, bP, lit, k, U, negatives, bits, prepared):
     base = _register(engine, rels)
     b = engine.bindings([dev(c) for c in B], bP)
     dU = [dev(c) for c in U]
@@ -66,6 +77,40 @@ def test_coverage_matches_reference_on_synthetic_cases(engine):
             want_flags = bits_to_flags(wbits, len(rows))
         assert counts == want_counts
         np.testing.assert_array_equal(flags, want_flags)
+
+
+@pytest.mark.parametrize("prepared", [False, True])
+def test_compat_coverage_matches_reference_everywhere(engine, prepared):
+    """QFG_OPT_COVERAGE_COMPAT: the reference's own procedure, chunk-relative
+    projection tables included -- equal to the reference on every synthetic
+    case, the divergent one (a label side of more than 32768 rows, not
+    smaller than the relation) included."""
+    seen_divergent = False
+    for case, want_counts, want_flags, _ in golden.coverage_cases()[0]:
+        rels, T, tP, B, bP, lit, rows, divergent = case
+        U = [t[rows] for t in T]
+        counts, flags = _gpu_coverage(engine, rels, B, bP, lit, len(T), U, [t[tP:] for t in T],
+                                      prepared=prepared, compat=True)
+        assert counts == want_counts, divergent
+        np.testing.assert_array_equal(flags, want_flags)
+        seen_divergent |= bool(divergent)
+    assert seen_divergent
+
+
+@pytest.mark.parametrize("seed,nb,nrel,dom,k", [(0, 100_000, 5000, 300, 2), (1, 200_000, 900, 40, 1),
+                                                (2, 80_000, 80_001, 50, 2), (3, 150_000, 20_000, 9, 3)])
+def test_compat_coverage_matches_compat_oracle(engine, seed, nb, nrel, dom, k):
+    rng = np.random.default_rng(seed)
+    B = [rng.integers(0, dom, nb).astype(np.int32) for _ in range(4)]
+    bP = nb // 3
+    rel = [rng.integers(0, dom, nrel).astype(np.int32) for _ in range(2)]
+    lit = Literal(0, (k - 1 if k > 1 else 0, 3), 0)
+    U = [rng.integers(0, dom, 40_000).astype(np.int32) for _ in range(k)]
+    Ng = [rng.integers(0, dom, 60_000).astype(np.int32) for _ in range(k)]
+    counts, flags = _gpu_coverage(engine, [rel], B, bP, lit, k, U, Ng, compat=True)
+    want, wbits = oracle.coverage(B, bP, rel, lit.as_tuple(), k, U, Ng, compat=True)
+    assert counts == want
+    np.testing.assert_array_equal(flags, bits_to_flags(wbits, len(U[0])))
 
 
 @pytest.mark.parametrize("name", ["kinship", "bongard"])

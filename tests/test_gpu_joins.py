@@ -81,3 +81,40 @@ def test_extension_feeds_next_step(engine):
     lits = [Literal(rid, (2, 1)), Literal(rid, (2, -1)), Literal(rid, (-1, 0))]
     want = brute_counts({rid: R}, cols, nb.num_positive, lits)
     np.testing.assert_array_equal(engine.evaluate_step(nb, lits), want)
+
+
+def test_after_semijoin_table_matches_reference_and_oracle(engine):
+    """qfg_build_hash_table_after_semijoin against the reference's own tables
+    (golden fixture) and the oracle, byte for byte: buckets, mask, and every
+    next link (0 for positions never inserted, in both)."""
+    from tests import golden
+    for keys, bits, chunk, nbt, want_b, want_n, want_m in golden.after_semijoin_cases():
+        dk = [dev(k) for k in keys]
+        db = torch.from_numpy(bits.view(np.int64)).cuda()
+        b, nx, m = engine.build_hash_table_after_semijoin(dk, db, chunk, nbt)
+        b, nx = b.cpu().numpy(), nx.cpu().numpy()
+        assert m == want_m
+        np.testing.assert_array_equal(b, want_b)
+        np.testing.assert_array_equal(oracle.reachable_next(b, nx), want_n)
+        ob, onx, om = oracle.build_hash_table_after_semijoin(keys, bits, chunk, nbt)
+        np.testing.assert_array_equal(b, ob)
+        np.testing.assert_array_equal(nx, onx)
+
+
+@pytest.mark.parametrize("n,k,dom,chunk", [(1, 1, 5, 0), (40000, 2, 20, 32768), (9000, 4, 3, 2000),
+                                           (50000, 1, 1 << 30, 0)])
+def test_after_semijoin_table_random_against_oracle(engine, n, k, dom, chunk):
+    rng = np.random.default_rng(n + k)
+    keys = [rng.integers(0, dom, n).astype(np.int32) for _ in range(k)]
+    flags = rng.random(n) < 0.7
+    words = np.zeros((n + 63) // 64, dtype=np.uint64)
+    idx = np.nonzero(flags)[0]
+    np.bitwise_or.at(words, idx >> 6, np.left_shift(np.uint64(1), (idx & 63).astype(np.uint64)))
+    nbt = n if chunk <= 0 else max(chunk, 1)
+    b, nx, m = engine.build_hash_table_after_semijoin([dev(c) for c in keys],
+                                                      torch.from_numpy(words.view(np.int64)).cuda(),
+                                                      chunk, nbt)
+    ob, onx, om = oracle.build_hash_table_after_semijoin(keys, words, chunk, nbt)
+    assert m == om
+    np.testing.assert_array_equal(b.cpu().numpy(), ob)
+    np.testing.assert_array_equal(nx.cpu().numpy(), onx)
