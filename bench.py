@@ -22,7 +22,7 @@ so no flush is needed between steps.
 
 ``--impl reference`` times the CPU restatement of the reference's operator
 chain (the oracle; the reference itself cannot be built on the GPU host) on
-all host cores over a bounded sample of the same step.
+all host cores over the whole step (all literals), for at most 3 steps.
 """
 from __future__ import annotations
 
@@ -186,29 +186,46 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(w, nthreads: int, sample: int, budget_s: float = 12.0):
+def join_group_sample(w):
+    """The literals of the step that join on one binding column (the
+    smallest such group): one Evaluate call's worth, so the sample pays one
+    binding-set partition for its literals, about the full step's ratio (a
+    partition per join column, 6 for 256 literals)."""
+    groups = {}
+    for l in w.literals:
+        groups.setdefault(l.vars[l.join_pos], []).append(l.as_tuple())
+    col, lits = min(groups.items(), key=lambda kv: len(kv[1]))
+    return col, lits
+
+
+def cpu_baseline(w, nthreads: int, sample: int):
     """The oracle (CPU restatement of the reference chain) on a bounded
-    sample of the step's literals; returns (literals/s, sample description)."""
+    sample of the step: by default every literal of one join column
+    (join_group_sample), else the first `sample` literals; returns
+    (literals/s, seconds, literals, description)."""
     import oracle
     o = oracle.Oracle(w.relations)
-    lits = [l.as_tuple() for l in w.literals]
-    if sample <= 0:
-        # grow the sample until the run takes a few seconds, within the budget
-        sample = min(2, len(lits))
-        t0 = time.perf_counter()
-        o.evaluate(w.binding_columns, w.num_positive, lits[:sample], 5, nthreads)
-        dt = time.perf_counter() - t0
-        sample = int(max(1, min(len(lits), sample * budget_s / max(dt, 1e-3) / 2)))
-    sample = max(1, min(sample, len(lits)))
-    o.evaluate(w.binding_columns, w.num_positive, lits[:sample], 5, nthreads)  # warm relation cache
+    if sample > 0:
+        lits = [l.as_tuple() for l in w.literals][:sample]
+        what = f"first {len(lits)} of {len(w.literals)} literals of the step"
+    else:
+        col, lits = join_group_sample(w)
+        what = (f"the {len(lits)} literals of the step that join on binding column {col} "
+                f"(one Evaluate call: one binding partition for them)")
+    o.evaluate(w.binding_columns, w.num_positive, lits[:1], 5, nthreads)  # warm relation cache
     t0 = time.perf_counter()
-    o.evaluate(w.binding_columns, w.num_positive, lits[:sample], 5, nthreads)
+    o.evaluate(w.binding_columns, w.num_positive, lits, 5, nthreads)
     dt = time.perf_counter() - t0
     o.close()
-    return sample / dt, dt, sample
+    return len(lits) / dt, dt, len(lits), what
 
 
 def run_reference(args):
+    """The reference arm: the oracle port of the reference's operator chain
+    (the reference itself cannot be built on the GPU host) over the whole
+    step -- all of its literals, every binding partition -- on all host
+    threads.  A step takes seconds, so at most 3 timed steps after 1 warm-up
+    step are run (the JSON line gives the numbers run)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
@@ -217,25 +234,28 @@ def run_reference(args):
     import oracle
     o = oracle.Oracle(w.relations)
     lits = [l.as_tuple() for l in w.literals]
-    sample = args.cpu_sample if args.cpu_sample > 0 else min(len(lits), 16)
-    step_lits = lits[:sample]
-    for _ in range(args.warmup):
-        o.evaluate(w.binding_columns, w.num_positive, step_lits, 5, threads)
+    if args.cpu_sample > 0:
+        lits = lits[:args.cpu_sample]
+    warmup, steps = min(args.warmup, 1), max(1, min(args.steps, 3))
+    for _ in range(warmup):
+        o.evaluate(w.binding_columns, w.num_positive, lits, 5, threads)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        o.evaluate(w.binding_columns, w.num_positive, step_lits, 5, threads)
-    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    for _ in range(steps):
+        o.evaluate(w.binding_columns, w.num_positive, lits, 5, threads)
+    dt = (time.perf_counter() - t0) / steps
     o.close()
-    value = sample / dt
+    value = len(lits) / dt
     line = {"impl": "reference", "metric": HEADLINE_METRIC,
-            "value": value, "unit": "literals/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "value": value, "unit": "literals/s", "n_gpus": args.gpus, "steps": steps,
+            "warmup": warmup, "steps_requested": args.steps, "warmup_requested": args.warmup,
+            "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64",
             "data": "synthetic (seeded)", "config": workload_config(args, w),
             "cpu_baseline": {"value": value, "unit": "literals/s", "cores": threads,
                              "kind": "port", "host": host_cpu(),
-                             "sample": f"first {sample} of {len(lits)} literals of the step, "
-                                       "oracle (C restatement of the reference operator chain), "
+                             "sample": f"the whole step: all {len(lits)} of {len(w.literals)} "
+                                       "literals (every binding partition), oracle (C "
+                                       "restatement of the reference operator chain), "
                                        f"{threads} threads"},
             "e2e": {"value": value, "unit": "literals/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -359,6 +379,12 @@ def run_gb300(args):
                    "join_count_kernel_ms": pl_stage["per_literal"][0],
                    "counts_equal_batched": bool(np.array_equal(host_counts, batched_counts))}
 
+    # The API-kept RadixPartition (qfg_radix_partition, the reference layout)
+    # on one binding column at 15 radix bits, against 12 bytes a row.
+    radix = None
+    if args.workload == "batched_step" and rank == 0:
+        radix = run_radix_partition(eng, dev_cols[0], stream, torch, measured_peak_hbm()[0])
+
     # End to end through the C ABI from pinned host buffers.
     pinned = [torch.from_numpy(c).pin_memory() for c in w.binding_columns]
     h2d = sum(c.numel() * 4 for c in pinned)
@@ -481,6 +507,8 @@ def run_gb300(args):
         }
         if serving is not None:
             line["serving"] = serving
+        if radix is not None:
+            line["radix_partition"] = radix
         if coverage is not None:
             line["coverage"] = coverage
         if testrun is not None:
@@ -493,13 +521,11 @@ def run_gb300(args):
         if clk is not None:
             line["clocks"] = clk
         if not args.no_cpu:
-            sample = args.cpu_sample
-            v, dt, s = cpu_baseline(w, 1, sample)
+            v, dt, s, what = cpu_baseline(w, 1, args.cpu_sample)
             line["cpu_baseline"] = {"value": v, "unit": "literals/s", "cores": 1, "kind": "port",
                                     "host": host_cpu(),
-                                    "sample": f"first {s} of {n} literals of the step "
-                                              f"({dt:.1f} s), oracle = C restatement of the "
-                                              "reference operator chain, 1 thread like the "
+                                    "sample": f"{what} ({dt:.1f} s), oracle = C restatement of "
+                                              "the reference operator chain, 1 thread like the "
                                               "reference"}
         print(json.dumps(line), flush=True)
     b.close()
@@ -507,6 +533,36 @@ def run_gb300(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def run_radix_partition(eng, values, stream, torch, peak, bits: int = 15, reps: int = 5):
+    """qfg_radix_partition (RadixPartition, stable, PartitionTuple output) of
+    one 32M-row binding column at 15 radix bits, timed with CUDA events on
+    the context stream; checked for a stable partition; HBM fraction on the
+    12 bytes a row of the benchmark spec's partition figure (4 read, 8 written)."""
+    n = values.numel()
+    tuples, offsets = eng.radix_partition(values, bits)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(reps):
+        tuples, offsets = eng.radix_partition(values, bits)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / reps
+    # stable partition: values grouped by digit, tuple ids ascending within
+    # every partition, every row once
+    v, t = tuples[:, 0], tuples[:, 1].long()
+    digit = v & ((1 << bits) - 1)
+    ok = bool(torch.equal(values[t], v)) and bool((digit[1:] >= digit[:-1]).all())
+    same = digit[1:] == digit[:-1]
+    ok = ok and bool((t[1:][same] > t[:-1][same]).all())
+    ok = ok and int(offsets[-1]) == n and bool(torch.equal(
+        torch.bincount(digit.long(), minlength=1 << bits).cumsum(0), offsets[1:]))
+    alg = 12 * n
+    return {"kernel": "qfg_radix_partition (two stable 7/8-bit passes)", "rows": n, "bits": bits,
+            "ms": ms, "algorithmic_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9,
+            "frac": alg / (ms * 1e-3) / 1e9 / peak, "peak": peak, "stable_partition": ok}
 
 
 def run_serving(eng, w, dev, torch, n_requests: int = 64, lits_per_request: int = 64, slots: int = 8):

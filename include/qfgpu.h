@@ -64,8 +64,16 @@ enum {
   QFG_OPT_SHARD_COUNT = 7,      /* number of shards (default 1); see qfg_evaluate_step */
   QFG_OPT_AUTOTUNE = 8,         /* 1 = use the partition bits qfg_autotune_step chose per size class */
   QFG_OPT_PASS1_BITS = 9,       /* pass-1 bits of a two-pass partition (0 = automatic, else 1..8) */
-  QFG_OPT_SERVER_DEPTH = 10     /* requests a server slot holds at once, 1..8 (default 1); read by
+  QFG_OPT_SERVER_DEPTH = 10,    /* requests a server slot holds at once, 1..8 (default 1); read by
                                    qfg_server_create (see the serving loop below) */
+  QFG_OPT_TEST_WITHHOLD_COPIES = 11, /* tests of the bounded wait only: 1 = the batched evaluation
+                                   kernel arms its tile barrier without issuing the tile copies,
+                                   so its bounded wait runs out (QFG_OPT_WAIT_LIMIT polls) and
+                                   the call returns QFG_ERR_TIMEOUT; nothing is in flight when
+                                   the CTAs stop.  Default 0 */
+  QFG_OPT_COVERAGE_COMPAT = 12  /* 1 = qfg_coverage / qfg_coverage_examples compute coverage as
+                                   the reference does, through its chunk-relative projection
+                                   tables (see qfg_coverage); 0 (default) = set membership */
 };
 
 /* Evaluation stages timed under QFG_OPT_STAGE_TIMING (the GPU counterpart of
@@ -180,8 +188,11 @@ int qfg_evaluate_step(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_li
 
 /* The plain per-literal GPU path: one RadixPartition -> BuildHashTable ->
  * HashJoin -> Filter -> CountAggregator chain per literal, as the
- * reference runs it (the operations/ sources), with the binding side re-partitioned
- * for every literal. */
+ * reference runs it (the operations/ sources).  As in the reference, the
+ * binding side is partitioned once per join variable (once per Evaluate
+ * call, learner/CandidateLiteralEvaluator.cpp:316-323) and each literal then
+ * builds, probes and counts over that partition; relation partitions are
+ * cached per (relation, column). */
 int qfg_evaluate_per_literal(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
                              const qfg_literal* literals, int64_t* counts, int flags);
 
@@ -289,8 +300,11 @@ int qfg_radix_partition(qfg_ctx* ctx, const int32_t* d_values, int64_t n, int bi
  * radix bits, 8 Mi values at 12 or more bits; larger inputs return
  * QFG_ERR_INVALID with the reason in `error` (error_len bytes, may be NULL).
  * The first call on a device looks the array's device address up with that
- * device current; make that first call before any stream capture.  All calls
- * on a device share the array, so calls whose work overlaps on the GPU race.
+ * device current; make that first call before any stream capture.  The
+ * address is kept for the life of the process, so do not use this entry
+ * point across a cudaDeviceReset.  All calls on a device share the array,
+ * so calls whose work overlaps on the GPU race.  A CUDA error already
+ * pending when the call starts is reported (QFG_ERR_CUDA) and left pending.
  * Work is queued on `stream` (a cudaStream_t, NULL = legacy stream). */
 int qfg_radix_partition_static(void* stream, const int32_t* d_values, int64_t n, int bits,
                                int32_t* d_out_tuples, int64_t* d_offsets, char* error,
@@ -318,6 +332,34 @@ int qfg_build_hash_table_on_partitions(qfg_ctx* ctx, const int32_t* d_tuples,
 int qfg_build_hash_table_on_table(qfg_ctx* ctx, const int32_t* const* d_keys, int32_t num_keys,
                                   int64_t n, int32_t* d_buckets, int32_t* d_next,
                                   uint32_t* mask_out);
+
+/* BuildHashTableAfterSemiJoin (operations/BuildHashTable.cpp:127-189,
+ * 212-236): the chained table the reference builds from a semi-join's
+ * output, byte-identical.  d_keys are the semi-join's projected columns
+ * (num_keys device columns of num_rows rows), d_bits its bit vector
+ * (64-bit little-endian blocks, one bit per row).  The semi-join's chunks
+ * are rows [c*chunk_rows, (c+1)*chunk_rows): a LeftSemiJoin cuts its probe
+ * side into FLAGS_semijoin_chunck_size (32768) rows, a RightSemiJoin yields
+ * one chunk (chunk_rows <= 0).  Within a chunk the set positions are taken
+ * in order and, as in the reference, are chunk-relative: the id inserted is
+ * the position within the chunk and keys are read at the chunk's rows, also
+ * for positions already in a chain (operations/LeftSemiJoin.hpp:55-83).  A
+ * position is inserted at the head of its bucket (Hash<k>, utility/Hash.hpp:
+ * 35-55) unless its chain reaches a position with equal keys; a chain
+ * position past the end of a short last chunk compares unequal (there the
+ * reference reads past the end of its columns).  The table is
+ * FoilHashTable(num_build_tuples, 0): d_buckets holds next_pow2(
+ * num_build_tuples) 1-based heads, d_next num_build_tuples links (0 for
+ * positions never inserted; the reference leaves those uninitialised), and
+ * *mask_out the mask.  num_build_tuples must exceed every chunk-relative
+ * position.  The first chunk is built in parallel; later chunks change
+ * chains in an order-dependent way and are replayed in order by one GPU
+ * thread (slow for many chunks; the learner's projected sides are label
+ * sides of a binding set). */
+int qfg_build_hash_table_after_semijoin(qfg_ctx* ctx, const int32_t* const* d_keys,
+                                        int32_t num_keys, int64_t num_rows, const uint64_t* d_bits,
+                                        int64_t chunk_rows, int32_t num_build_tuples,
+                                        int32_t* d_buckets, int32_t* d_next, uint32_t* mask_out);
 
 /* LeftSemiJoin<k> (operations/LeftSemiJoin.hpp:55-141): bit i of d_bits
  * (64-bit little-endian blocks, the BitVector layout of utility/BitVector.hpp)
@@ -390,8 +432,18 @@ int qfg_relation_register_text(qfg_ctx* ctx, int32_t relation_id, const char* te
  * the relation, operations/BuildHashTable.cpp:152-189 with
  * operations/LeftSemiJoin.hpp:55-83); there its counts are not set
  * membership.  These are set membership for every size, which equals the
- * reference wherever its row ids are whole-table.  1 <= num_target_columns
- * <= 8; the literal needs at least one bound argument. */
+ * reference wherever its row ids are whole-table.  Under
+ * QFG_OPT_COVERAGE_COMPAT = 1 the reference's own procedure is followed
+ * instead, chunk-relative ids included: per label side the bit vector of the
+ * first semi-join, the table qfg_build_hash_table_after_semijoin builds from
+ * it (32768-row chunks when the side is not smaller than the relation, as
+ * SelectAndCreateSemiJoin chooses, operations/SemiJoinFactory.cpp:45-82),
+ * and the examples probed through that table against the side's rows.  The
+ * positive side reads past its end into the negative rows, as the
+ * reference's positive view of a consecutive binding set does; past the
+ * negative side's end a position compares unequal (the reference reads past
+ * its columns there).  1 <= num_target_columns <= 8; the literal needs at
+ * least one bound argument. */
 int qfg_coverage(qfg_ctx* ctx, const qfg_bindings* bindings, const qfg_literal* literal,
                  int32_t num_target_columns, const int32_t* const* d_uncovered_positive,
                  int64_t num_uncovered_positive, const int32_t* const* d_negative,

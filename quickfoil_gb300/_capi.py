@@ -40,6 +40,8 @@ QFG_OPT_SHARD_COUNT = 7
 QFG_OPT_AUTOTUNE = 8
 QFG_OPT_PASS1_BITS = 9
 QFG_OPT_SERVER_DEPTH = 10
+QFG_OPT_TEST_WITHHOLD_COPIES = 11
+QFG_OPT_COVERAGE_COMPAT = 12
 
 STAGES = ("key_tables", "bind_partition", "evaluate", "per_literal", "unit_plan",
           "coverage_scan", "coverage_examples")
@@ -125,6 +127,9 @@ SIGNATURES = [
      [c_vp, c_vp, c_vp, ctypes.c_int64, ctypes.c_int, c_vp, c_vp, c_vp, c_vp]),
     ("qfg_build_hash_table_on_table", ctypes.c_int,
      [c_vp, ctypes.POINTER(c_vp), ctypes.c_int32, ctypes.c_int64, c_vp, c_vp, c_u32p]),
+    ("qfg_build_hash_table_after_semijoin", ctypes.c_int,
+     [c_vp, ctypes.POINTER(c_vp), ctypes.c_int32, ctypes.c_int64, c_vp, ctypes.c_int64,
+      ctypes.c_int32, c_vp, c_vp, c_u32p]),
     ("qfg_left_semijoin", ctypes.c_int,
      [c_vp, ctypes.POINTER(c_vp), ctypes.c_int64, ctypes.POINTER(c_vp), ctypes.c_int64,
       ctypes.c_int32, c_vp, c_i64p]),

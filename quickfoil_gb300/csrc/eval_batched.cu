@@ -736,6 +736,7 @@ struct EvalArgs {
   unsigned long long* counts;
   int* error_flag;           // set when a bounded wait gave up
   int64_t wait_limit;        // iterations of a bounded wait
+  int withhold_copies;       // tests: arm the tile barrier, issue no copy
 };
 
 // Shared-memory stride of a tile column: room for the alignment shifts of
@@ -952,6 +953,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
   __shared__ uint32_t s_nkeys;  // distinct keys of the current tile (entries of klist)
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
+  __shared__ uint32_t s_abort;  // a bounded wait gave up: the CTA stops
 
   for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) acc[i] = 0ull;
   for (int i = threadIdx.x; i < kSlots; i += blockDim.x) {
@@ -960,6 +962,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
   }
   if (threadIdx.x == 0) {
     s_nkeys = 0u;
+    s_abort = 0u;
     s_count = umin(a.unit_count[0], a.unit_cap);
     s_idx = atomicAdd(a.work_counter, 1u);
     if (s_idx < s_count) s_unit = a.units[s_idx];
@@ -1036,12 +1039,18 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
       const uint32_t shP = seg[0].s0, baseN = seg[1].s0;
       if (threadIdx.x == 0) {
         fence_proxy_async_smem();  // this tile's copies come after all earlier reads of the buffer
-        mbar_arrive_expect_tx(&s_bar, (uint32_t)ncols * (seg[0].body_bytes() + seg[1].body_bytes()));
-        for (int q = 0; q < ncols; ++q)
-          for (int k = 0; k < 2; ++k)
-            if (seg[k].has_body())
-              bulk_g2s(raw + q * kTileStride + seg[k].s0 + (seg[k].body_lo() - seg[k].g0),
-                       gcols + (int64_t)q * gn + seg[k].body_lo(), seg[k].body_bytes(), &s_bar);
+        const uint32_t tx = (uint32_t)ncols * (seg[0].body_bytes() + seg[1].body_bytes());
+        if (a.withhold_copies) {
+          // Tests of the bounded wait: bytes announced that never arrive.
+          mbar_arrive_expect_tx(&s_bar, tx > 0u ? tx : 16u);
+        } else {
+          mbar_arrive_expect_tx(&s_bar, tx);
+          for (int q = 0; q < ncols; ++q)
+            for (int k = 0; k < 2; ++k)
+              if (seg[k].has_body())
+                bulk_g2s(raw + q * kTileStride + seg[k].s0 + (seg[k].body_lo() - seg[k].g0),
+                         gcols + (int64_t)q * gn + seg[k].body_lo(), seg[k].body_bytes(), &s_bar);
+        }
       }
       if ((int)threadIdx.x < 4 * ncols) {
         // Unaligned heads and tails: (column, segment, head or tail) per thread.
@@ -1060,12 +1069,17 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         for (uint32_t g = lo; g < hi; ++g) dst[g - sp.g0] = __ldg(src + g);
       }
       {
-        // Bounded wait for the bulk copies; a wait that gives up flags the
-        // context and waits once more (bounded) for the copies in flight.
+        // Bounded wait for the bulk copies.  A wait that gives up flags the
+        // context, waits once more (bounded) for copies still in flight, so
+        // that none lands after the CTA has stopped, and stops the CTA: all
+        // threads leave the unit loop after the barrier below, nothing is
+        // flushed, and the call reports QFG_ERR_TIMEOUT.  (Should the second
+        // wait give up too, the CTA stops all the same.)
         int64_t it = 0;
         while (!mbar_try_wait(&s_bar, phase)) {
           if (++it > a.wait_limit) {
             atomicExch(a.error_flag, 1);
+            s_abort = 1u;
             for (int64_t k2 = 0; k2 < a.wait_limit && !mbar_try_wait(&s_bar, phase); ++k2) {
             }
             break;
@@ -1074,6 +1088,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         phase ^= 1u;
       }
       __syncthreads();
+      if (s_abort != 0u) break;
       // Distinct join keys of the tile: owner = first row + 1, claimed by
       // CAS; the count atomics return each row's rank within its key and
       // label (positive count low half, negative count high half).
@@ -1219,6 +1234,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
       __syncthreads();
       if (threadIdx.x == 0) s_nkeys = 0u;  // read by every thread above; next read after a barrier
     }
+    if (s_abort != 0u) break;  // read after the barrier that follows the wait
     // Threads' entries are contiguous and increasing, so equal literals sit
     // on consecutive lanes; idle lanes (Lrun = -1) trail.
     cp = seg_scan(cp, Lrun);
@@ -1236,6 +1252,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     __syncthreads();
   }
   __syncthreads();
+  if (s_abort != 0u) return;
   for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) {
     const unsigned long long v = acc[i];
     if (v != 0ull) atomicAdd(&a.counts[4 * a.lits[i >> 2].out + (i & 3)], v);
@@ -1658,6 +1675,7 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     ea.rec = recs;
     ea.error_flag = ctx->error_flag;
     ea.wait_limit = ctx->wait_limit;
+    ea.withhold_copies = ctx->withhold_copies ? 1 : 0;
     ea.counts = counts;
     ea.max_cols = 1;
     for (size_t g = S.gbeg; g < S.gend; ++g) ea.max_cols = std::max(ea.max_cols, gdesc[g].ncols);
@@ -1910,13 +1928,17 @@ extern "C" int qfg_step_traffic(qfg_ctx* c, const qfg_bindings* b, int32_t n,
       bytes[QFG_STAGE_EVALUATE] += 20 * ne + 32;
     }
   }
-  // The plain path re-partitions the join column per literal (value +
-  // tuple id, 12 bytes a row), reads the relation partition (8 bytes a
-  // tuple) and the join pairs' atom columns are gathered.
+  // The plain path partitions each distinct join column once (value +
+  // tuple id, 12 bytes a row); per literal it reads the binding partition
+  // (8 bytes a row) and the relation partition (8 bytes a tuple), and the
+  // join pairs' atom columns are gathered.
+  std::map<int, int> join_cols;
+  for (int i = 0; i < n; ++i) join_cols[lits[i].vars[lits[i].join_pos]] = 1;
+  bytes[QFG_STAGE_PER_LITERAL] += 12 * nb * (int64_t)join_cols.size();
   for (int i = 0; i < n; ++i) {
     Relation* rel = nullptr;
     QFG_TRY(find_relation(ctx, lits[i].relation_id, &rel));
-    bytes[QFG_STAGE_PER_LITERAL] += 12 * nb + 8 * rel->num_tuples + 32;
+    bytes[QFG_STAGE_PER_LITERAL] += 8 * nb + 8 * rel->num_tuples + 32;
   }
   QFG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return QFG_OK;

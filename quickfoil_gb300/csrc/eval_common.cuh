@@ -15,9 +15,12 @@ int counts_begin(Ctx* ctx, int32_t n, int64_t* counts, int flags, unsigned long 
 // wait that gave up.
 int counts_end(Ctx* ctx, int32_t n, int64_t* counts, int flags, unsigned long long* dev);
 
-// One literal through the plain per-literal chain; counts[0..3] accumulate.
-int evaluate_plain_one(Ctx* ctx, const qfg_bindings* b, const qfg_literal& l,
-                       unsigned long long* counts);
+// The plain per-literal chain: the binding join column partitioned in the
+// reference layout (once per join column), then one literal's build / probe
+// / count over it (counts[0..3] accumulate).
+int plain_partition_bindings(Ctx* ctx, const qfg_bindings* b, int column, int* bits);
+int plain_join_count(Ctx* ctx, const qfg_bindings* b, const qfg_literal& l, int bits,
+                     unsigned long long* counts);
 
 // All literals through the batched engine; counts[4*i..] accumulate.
 int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,

@@ -1,8 +1,10 @@
 // eval_plain.cu -- the plain per-literal GPU path and shared evaluation
 // plumbing (literal validation, count buffers).
 //
-// One literal = one run of the reference chain: RadixPartition of the
-// binding join column (operations/RadixPartition.cpp:179-186), the cached
+// One literal = one run of the reference chain over the binding join column
+// partitioned once per join variable, as the reference partitions it once
+// per Evaluate call (operations/RadixPartition.cpp:179-186,
+// learner/CandidateLiteralEvaluator.cpp:316-323); the cached
 // RadixPartition of the relation join column
 // (learner/CandidateLiteralEvaluator.cpp:296-299), then per partition a
 // chained hash table on the binding side probed by every relation tuple
@@ -18,6 +20,8 @@
 // Binding partitions larger than a tile are processed tile by tile; a
 // binding row belongs to exactly one tile, so covered counts add up.
 #include <algorithm>
+#include <map>
+#include <vector>
 
 #include "eval_common.cuh"
 
@@ -177,20 +181,33 @@ int counts_end(Ctx* ctx, int32_t n, int64_t* counts, int flags, unsigned long lo
   return QFG_OK;
 }
 
-int evaluate_plain_one(Ctx* ctx, const qfg_bindings* b, const qfg_literal& l,
-                       unsigned long long* counts) {
+// Binding join column `column` in the reference partition layout, into the
+// context's binding-partition scratch (the reference's once-per-Evaluate
+// RadixPartition of the binding set, learner/CandidateLiteralEvaluator.cpp:
+// 316-323).  *bits receives the partition bits.
+int plain_partition_bindings(Ctx* ctx, const qfg_bindings* b, int column, int* bits) {
+  const int64_t nb = b->num_positive + b->num_negative;
+  *bits = auto_plain_bits(ctx, nb);
+  const int P = 1 << *bits;
+  QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * 2 * (size_t)std::max<int64_t>(nb, 1)));
+  QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(ctx, sizeof(int64_t) * (size_t)(P + 1)));
+  QFG_TRY(stage_begin(ctx, QFG_STAGE_BIND_PARTITION));
+  QFG_TRY(radix_partition_ref(ctx, b->columns[column], nb, *bits,
+                              ctx->scratch[kScrBindPart].as<int32_t>(),
+                              ctx->scratch[kScrBindOffsets].as<int64_t>()));
+  QFG_TRY(stage_end(ctx, QFG_STAGE_BIND_PARTITION));
+  return QFG_OK;
+}
+
+// One literal's build / probe / filter / count chain over the binding
+// partition left by plain_partition_bindings (same join column and bits).
+int plain_join_count(Ctx* ctx, const qfg_bindings* b, const qfg_literal& l, int bits,
+                     unsigned long long* counts) {
   Relation* rel = nullptr;
   QFG_TRY(find_relation(ctx, l.relation_id, &rel));
   const int64_t nb = b->num_positive + b->num_negative;
   if (nb == 0 || rel->num_tuples == 0) return QFG_OK;
-  const int bits = auto_plain_bits(ctx, nb);
   const int P = 1 << bits;
-  // Binding side: partitioned for this literal.
-  QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * 2 * (size_t)nb));
-  QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(ctx, sizeof(int64_t) * (size_t)(P + 1)));
-  const int j = l.vars[l.join_pos];
-  QFG_TRY(radix_partition_ref(ctx, b->columns[j], nb, bits, ctx->scratch[kScrBindPart].as<int32_t>(),
-                              ctx->scratch[kScrBindOffsets].as<int64_t>()));
   // Relation side: cached for the run.
   PartitionedColumn* rp = nullptr;
   QFG_TRY(relation_partitions(ctx, rel, l.join_pos, bits, &rp));
@@ -228,6 +245,17 @@ extern "C" int qfg_evaluate_per_literal(qfg_ctx* c, const qfg_bindings* b, int32
   QFG_TRY(validate_literals(ctx, b, n, lits));
   unsigned long long* dev = nullptr;
   QFG_TRY(counts_begin(ctx, n, counts, flags, &dev));
-  for (int32_t i = 0; i < n; ++i) QFG_TRY(evaluate_plain_one(ctx, b, lits[i], dev + 4 * i));
+  const int64_t nb = b->num_positive + b->num_negative;
+  if (nb > 0) {
+    // As the reference: the binding set partitioned once per clause join
+    // variable (once per Evaluate call), then one chain per literal.
+    std::map<int, std::vector<int32_t>> by_column;
+    for (int32_t i = 0; i < n; ++i) by_column[lits[i].vars[lits[i].join_pos]].push_back(i);
+    for (const auto& kv : by_column) {
+      int bits = 0;
+      QFG_TRY(plain_partition_bindings(ctx, b, kv.first, &bits));
+      for (int32_t i : kv.second) QFG_TRY(plain_join_count(ctx, b, lits[i], bits, dev + 4 * i));
+    }
+  }
   return counts_end(ctx, n, counts, flags, dev);
 }

@@ -9,13 +9,18 @@
 // an exclusive scan in digit-major order turns the counts into output
 // cursors, and a scatter pass re-reads the chunk and writes each row at its
 // cursor plus its rank among same-digit lanes below it.  Chunks are disjoint
-// and scanned in row order, so the result is stable.
+// and scanned in row order, so the result is stable.  Up to 8 radix bits one
+// such pass writes the tuples; wider digits take two stable LSD passes of at
+// most 8 bits each (low digit into (value, row) scratch, then high digit into
+// the tuples), so the per-warp count table stays small and the grid fills
+// the GPU at every bit count.
 //
 // The same stable pass, applied LSD-style to bucket ids, rebuilds the
 // reference's chained FoilHashTable byte for byte: a chain lists the
 // partition positions of one bucket in descending order, so after a stable
 // sort by (partition, bucket) each element's `next` is its predecessor in the
 // sorted order and the bucket head is the last one.
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -35,6 +40,18 @@ struct RefTupleIO {
   __device__ __forceinline__ uint32_t key(int64_t i) const { return (uint32_t)values[i]; }
   __device__ __forceinline__ void write(int64_t pos, int64_t i, uint32_t k) const {
     out[pos] = make_int2((int32_t)k, (int32_t)i);
+  }
+};
+
+// Second LSD pass of a wide RadixPartition: (value, row) pairs in
+// structure-of-arrays form, written as PartitionTuple{value, tuple_id}.
+struct SoAToRefIO {
+  const uint32_t* keys_in;
+  const int32_t* payload_in;
+  int2* out;
+  __device__ __forceinline__ uint32_t key(int64_t i) const { return keys_in[i]; }
+  __device__ __forceinline__ void write(int64_t pos, int64_t i, uint32_t k) const {
+    out[pos] = make_int2((int32_t)k, payload_in[i]);
   }
 };
 
@@ -276,6 +293,28 @@ __global__ void table_bucket_ids_kernel(const int32_t* const* __restrict__ keys,
   }
 }
 
+// Count of every full radix digit (value & (P - 1)), privatised per block in
+// shared memory (P <= 2^15 words), added to hist (zeroed) once per block.
+__global__ void digit_hist_kernel(const int32_t* __restrict__ values, int64_t n, uint32_t P,
+                                  uint32_t* __restrict__ hist) {
+  extern __shared__ uint32_t sh[];
+  for (uint32_t d = threadIdx.x; d < P; d += blockDim.x) sh[d] = 0u;
+  __syncthreads();
+  const uint32_t mask = P - 1u;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&sh[(uint32_t)__ldg(values + i) & mask], 1u);
+  __syncthreads();
+  for (uint32_t d = threadIdx.x; d < P; d += blockDim.x)
+    if (sh[d] != 0u) atomicAdd(&hist[d], sh[d]);
+}
+
+__global__ void offsets_to_i64_kernel(const uint32_t* __restrict__ scanned, uint32_t P, int64_t n,
+                                      int64_t* __restrict__ offsets) {
+  for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d <= P; d += gridDim.x * blockDim.x)
+    offsets[d] = d == P ? n : (int64_t)scanned[d];
+}
+
 int bits_for(uint64_t x) {  // smallest b with 2^b > x - 1, at least 1
   int b = 1;
   while (b < 32 && (uint64_t(1) << b) < x) ++b;
@@ -294,15 +333,53 @@ int sort_pairs_u32(Ctx* ctx, uint32_t* k0, int32_t* p0, uint32_t* k1, int32_t* p
   return stable_sort_pairs(ctx, k0, p0, k1, p1, n, key_bits, k_out, p_out);
 }
 
+// Widest digit one stable pass takes: its per-warp count table (4 * 2^bits
+// bytes) then leaves room for eight warps a block and the warp chunk stays
+// at 2048 rows, so grids fill the GPU.  Wider partitions take two passes.
+constexpr int kMaxOnePassRefBits = 8;
+
 int radix_partition_ref(Ctx* ctx, const int32_t* values, int64_t n, int bits, int32_t* out_tuples,
                         int64_t* out_offsets) {
+  const uint32_t P = 1u << bits;
   if (n == 0) {
-    const uint32_t P = 1u << bits;
     QFG_CUDA(ctx, cudaMemsetAsync(out_offsets, 0, sizeof(int64_t) * (P + 1), ctx->stream));
     return QFG_OK;
   }
-  RefTupleIO io{values, reinterpret_cast<int2*>(out_tuples)};
-  return stable_pass(ctx, io, n, 0, bits, out_offsets);
+  if (bits <= kMaxOnePassRefBits) {
+    RefTupleIO io{values, reinterpret_cast<int2*>(out_tuples)};
+    return stable_pass(ctx, io, n, 0, bits, out_offsets);
+  }
+  // Two stable LSD passes: the low digit (value, row index into SoA
+  // scratch), then the high digit, writing the tuples.  Both are stable, so
+  // the result is ordered by the full digit and, within it, by row: the
+  // reference's partition order.  The offsets come from a count of the full
+  // digit.
+  const int lo = bits / 2, hi = bits - lo;
+  QFG_TRY(ctx->scratch[kScrSortA].reserve(ctx, 2 * sizeof(uint32_t) * (size_t)n));
+  uint32_t* mid_keys = ctx->scratch[kScrSortA].as<uint32_t>();
+  int32_t* mid_rows = reinterpret_cast<int32_t*>(mid_keys + n);
+  SortIO a{reinterpret_cast<const uint32_t*>(values), nullptr, mid_keys, mid_rows};
+  QFG_TRY(stable_pass(ctx, a, n, 0, lo, nullptr));
+  SoAToRefIO b{mid_keys, mid_rows, reinterpret_cast<int2*>(out_tuples)};
+  QFG_TRY(stable_pass(ctx, b, n, lo, hi, nullptr));
+  QFG_TRY(ctx->scratch[kScrTmpA].reserve(ctx, sizeof(uint32_t) * (size_t)(P + 1)));
+  uint32_t* hist = ctx->scratch[kScrTmpA].as<uint32_t>();
+  QFG_CUDA(ctx, cudaMemsetAsync(hist, 0, sizeof(uint32_t) * P, ctx->stream));
+  const size_t smem = sizeof(uint32_t) * P;
+  if (smem > 48 * 1024)
+    QFG_CUDA(ctx, cudaFuncSetAttribute(digit_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+  int per_sm = 0;
+  QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, digit_hist_kernel, 512, smem));
+  const int64_t want = (n + 512 * 16 - 1) / (512 * 16);
+  const unsigned grid = (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>(want, (int64_t)ctx->num_sms * std::max(per_sm, 1)));
+  digit_hist_kernel<<<grid, 512, smem, ctx->stream>>>(values, n, P, hist);
+  QFG_LAUNCHED(ctx);
+  QFG_TRY(exclusive_scan_u32(ctx, hist, hist, P, nullptr));
+  offsets_to_i64_kernel<<<(P + 256) / 256, 256, 0, ctx->stream>>>(hist, P, n, out_offsets);
+  QFG_LAUNCHED(ctx);
+  return QFG_OK;
 }
 
 int relation_partitions(Ctx* ctx, Relation* rel, int column, int bits, PartitionedColumn** out) {
@@ -451,7 +528,9 @@ static __device__ __align__(256) uint32_t g_static_scratch[kStaticScratchWords];
 
 // Device address of g_static_scratch per device ordinal, looked up once with
 // that device current (a host-side name of a __device__ array is not a device
-// address).
+// address).  The cache lives as long as the process: after cudaDeviceReset
+// the module is loaded again and the cached address is stale, so the entry
+// point must not be used across a device reset.
 std::mutex g_static_mutex;
 std::map<int, uint32_t*> g_static_ptr;
 
@@ -565,12 +644,18 @@ extern "C" int qfg_radix_partition_static(void* stream, const int32_t* d_values,
                     std::to_string(bits) + " radix bits need " + std::to_string(entries + tiles) +
                     " scratch words, more than the " + std::to_string(kStaticScratchWords) +
                     " of the static scratch array");
+  // An error left pending by the caller's own earlier CUDA work would be
+  // returned by the launch checks below as if a launch of this call had
+  // failed; report it as what it is and leave it pending.
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess)
+    return fail(QFG_ERR_CUDA, std::string("qfg_radix_partition_static: a CUDA error was pending "
+                                          "before the call: ") + cudaGetErrorString(e));
   uint32_t* scratch = nullptr;
   int st = static_scratch_for_current_device(&scratch, &err);
   if (st != QFG_OK) return fail(st, err);
   cudaStream_t strm = static_cast<cudaStream_t>(stream);
   const uint32_t P = 1u << bits;
-  cudaError_t e = cudaSuccess;
   if (n == 0) {
     e = cudaMemsetAsync(d_offsets, 0, sizeof(int64_t) * (P + 1), strm);
     return e == cudaSuccess ? QFG_OK : fail(QFG_ERR_CUDA, cudaGetErrorString(e));
@@ -586,15 +671,26 @@ extern "C" int qfg_radix_partition_static(void* stream, const int32_t* d_values,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
     if (e != cudaSuccess) return fail(QFG_ERR_CUDA, cudaGetErrorString(e));
   }
+  // Each launch is checked on its own, so a failure names its kernel.
+  auto launched = [&](const char* kernel) -> int {
+    const cudaError_t le = cudaGetLastError();
+    if (le == cudaSuccess) return QFG_OK;
+    return fail(QFG_ERR_CUDA, std::string("qfg_radix_partition_static: launch of ") + kernel +
+                                  " failed: " + cudaGetErrorString(le));
+  };
   stable_hist_kernel<RefTupleIO><<<s.grid, 32 * s.warps, s.smem, strm>>>(io, n, 0, bits, s.chunk,
                                                                           s.num_chunks, hist);
+  QFG_TRY(launched("stable_hist_kernel"));
   static_scan_tiles_kernel<<<(unsigned)tiles, kStaticScanThreads, 0, strm>>>(hist, entries, tile_sums);
+  QFG_TRY(launched("static_scan_tiles_kernel"));
   static_scan_sums_kernel<<<1, 32, 0, strm>>>(tile_sums, (int)tiles);
+  QFG_TRY(launched("static_scan_sums_kernel"));
   static_scan_add_kernel<<<(unsigned)tiles, kStaticScanThreads, 0, strm>>>(hist, entries, tile_sums);
+  QFG_TRY(launched("static_scan_add_kernel"));
   digit_offsets_kernel<<<(P + 256) / 256, 256, 0, strm>>>(hist, s.num_chunks, bits, n, d_offsets);
+  QFG_TRY(launched("digit_offsets_kernel"));
   stable_scatter_kernel<RefTupleIO><<<s.grid, 32 * s.warps, s.smem, strm>>>(io, n, 0, bits, s.chunk,
                                                                              s.num_chunks, hist);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return fail(QFG_ERR_CUDA, cudaGetErrorString(e));
+  QFG_TRY(launched("stable_scatter_kernel"));
   return QFG_OK;
 }

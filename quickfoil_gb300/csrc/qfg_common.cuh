@@ -170,6 +170,8 @@ struct Ctx {
   int num_radix_bits = 5;
   int eval_bits = 0;
   int64_t wait_limit = 1 << 26;
+  bool withhold_copies = false;  // QFG_OPT_TEST_WITHHOLD_COPIES
+  bool coverage_compat = false;  // QFG_OPT_COVERAGE_COMPAT
   int use_graphs = 0;
   // QFG_OPT_USE_GRAPHS: captured steps by key (see step_runtime.cu).
   std::map<std::string, qfg_step_graph*> graph_cache;
@@ -316,6 +318,22 @@ int relation_key_table(Ctx* ctx, Relation* rel, const std::vector<int>& position
                        KeyTable** out);
 
 int find_relation(Ctx* ctx, int32_t id, Relation** out);
+
+// BuildHashTableAfterSemiJoin in the reference's layout (after_semijoin.cu):
+// nk key columns of n rows, readable past the end up to `readable` rows (a
+// chain position beyond compares unequal), semi-join bits, chunk rows (<= 0:
+// one chunk), FoilHashTable(num_build_tuples) arrays.
+int after_semijoin_table(Ctx* ctx, const int32_t* const* cols, int nk, int64_t n, int64_t readable,
+                         const uint64_t* d_bits, int64_t chunk_rows, int32_t num_build_tuples,
+                         int32_t* d_buckets, int32_t* d_next, uint32_t* mask_out);
+
+// Coverage as the reference computes it, through its chunk-relative
+// projection tables (QFG_OPT_COVERAGE_COMPAT; after_semijoin.cu).  ex_cols[s]
+// / ex_n[s]: the uncovered positives (s = 0) and the negatives (s = 1,
+// ex_n 0 to skip); num_covered[2] and the positives' bits as qfg_coverage.
+int coverage_compat(Ctx* ctx, const qfg_bindings* b, const qfg_literal* lit, int k,
+                    const int32_t* const* ex_cols[2], const int64_t ex_n[2],
+                    uint64_t* d_positive_bits, int64_t* num_covered);
 
 }  // namespace qfg
 

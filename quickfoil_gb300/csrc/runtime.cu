@@ -441,6 +441,12 @@ extern "C" int qfg_ctx_set_option(qfg_ctx* c, int option, int64_t value) {
         return set_error(ctx, QFG_ERR_INVALID, "server depth out of range [1, 8]");
       ctx->server_depth = (int)value;
       return QFG_OK;
+    case QFG_OPT_TEST_WITHHOLD_COPIES:
+      ctx->withhold_copies = value != 0;
+      return QFG_OK;
+    case QFG_OPT_COVERAGE_COMPAT:
+      ctx->coverage_compat = value != 0;
+      return QFG_OK;
     default:
       return set_error(ctx, QFG_ERR_INVALID, "unknown option " + std::to_string(option));
   }

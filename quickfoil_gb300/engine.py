@@ -377,6 +377,25 @@ class Engine:
             nxt.data_ptr(), ctypes.byref(mask)), self.ctx, "qfg_build_hash_table_on_table")
         return buckets, nxt, mask.value
 
+    def build_hash_table_after_semijoin(self, keys, bits, chunk_rows: int, num_build_tuples: int):
+        """BuildHashTableAfterSemiJoin over the semi-join's projected device
+        columns `keys` and its bit blocks `bits` (int64/uint64 device
+        tensor), cut into chunk_rows-row chunks (<= 0: one chunk): (buckets,
+        next, mask)."""
+        import torch
+        n = keys[0].numel()
+        nb = 1
+        while nb < num_build_tuples:
+            nb <<= 1
+        buckets = torch.empty(nb, dtype=torch.int32, device=keys[0].device)
+        nxt = torch.empty(num_build_tuples, dtype=torch.int32, device=keys[0].device)
+        mask = ctypes.c_uint32()
+        C.check(self.lib.qfg_build_hash_table_after_semijoin(
+            self.ctx, C.ptr_array([k.data_ptr() for k in keys]), len(keys), n, bits.data_ptr(),
+            chunk_rows, num_build_tuples, buckets.data_ptr(), nxt.data_ptr(), ctypes.byref(mask)),
+            self.ctx, "qfg_build_hash_table_after_semijoin")
+        return buckets, nxt, mask.value
+
     def _semijoin(self, fn, probe_keys, build_keys, nrows):
         import torch
         bits = torch.empty(max(1, (nrows + 63) // 64), dtype=torch.int64, device=probe_keys[0].device)

@@ -231,7 +231,8 @@ def bongard(seed: int = 1, pictures: int = 300, mean_objects: float = 10.0,
     hit = sorted({pic_of[a] for a, b in inside if shape_of[a] == 0 and shape_of[b] == 1})
     pos = set(int(v) for v in rng.permutation(hit)[:max_positive])
     positives = sorted(pos)
-    negatives = [p for p in range(pictures) if p not in set(hit)]
+    hit_set = set(hit)
+    negatives = [p for p in range(pictures) if p not in hit_set]
     cols = lambda pairs, k: np.array([x[k] for x in pairs], dtype=np.int32)
     element = [(int(p), int(o)) for p, o in zip(obj_pic, obj_ids)]
     relations = [[cols(element, 0), cols(element, 1)],
@@ -242,6 +243,52 @@ def bongard(seed: int = 1, pictures: int = 300, mean_objects: float = 10.0,
     target = np.array(positives + negatives, dtype=np.int32)
     return LearnTask("bongard", relations, ["element", "circle", "triangle", "square", "inside"],
                      [target], len(positives), max_clause_length)
+
+
+def bongard_kb(seed: int = 4, pictures: int = 1_000_000, mean_objects: float = 10.0,
+               inside_per_object: float = 2.0, max_positive: int = 100_000,
+               max_clause_length: int = 4) -> LearnTask:
+    """The Bongard-like knowledge base of the full-scale learn loop, generated
+    with array operations (seconds for a million pictures): the rules of
+    `bongard` -- Poisson(mean_objects) objects per picture (at least one),
+    one of three shapes per object uniformly, Poisson(inside_per_object x
+    objects) ordered within-picture object pairs per picture with pairs of an
+    object with itself dropped and repeats merged, positives = up to
+    `max_positive` pictures with a circle inside a triangle, negatives =
+    every picture without one -- drawn in a different order, so its knowledge
+    base differs from `bongard`'s for the same seed.  At the defaults:
+    element 10M, inside about 16M tuples, 100K positives."""
+    rng = np.random.default_rng(seed)
+    counts = np.maximum(rng.poisson(mean_objects, pictures), 1).astype(np.int64)
+    obj_pic = np.repeat(np.arange(pictures, dtype=np.int64), counts)
+    nobj = len(obj_pic)
+    obj_ids = (pictures + np.arange(nobj)).astype(np.int32)
+    shape = rng.integers(0, 3, nobj)
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    m = rng.poisson(inside_per_object * counts)
+    m[counts < 2] = 0
+    pair_pic = np.repeat(np.arange(pictures, dtype=np.int64), m)
+    c = counts[pair_pic]
+    a = (rng.random(len(pair_pic)) * c).astype(np.int64)
+    b = (rng.random(len(pair_pic)) * c).astype(np.int64)
+    keep = a != b
+    ga = starts[pair_pic[keep]] + a[keep]
+    gb = starts[pair_pic[keep]] + b[keep]
+    code = np.unique(ga * nobj + gb)  # sorted by (a, b): object ids grow with the index
+    ia, ib = code // nobj, code % nobj
+    hit = np.unique(obj_pic[ia[(shape[ia] == 0) & (shape[ib] == 1)]])
+    pos = np.sort(rng.permutation(hit)[:max_positive])
+    is_hit = np.zeros(pictures, dtype=bool)
+    is_hit[hit] = True
+    neg = np.nonzero(~is_hit)[0]
+    relations = [[obj_pic.astype(np.int32), obj_ids],
+                 [obj_ids[shape == 0].copy()],
+                 [obj_ids[shape == 1].copy()],
+                 [obj_ids[shape == 2].copy()],
+                 [obj_ids[ia], obj_ids[ib]]]
+    target = np.concatenate([pos, neg]).astype(np.int32)
+    return LearnTask("bongard_kb", relations, ["element", "circle", "triangle", "square", "inside"],
+                     [target], len(pos), max_clause_length)
 
 
 def facts_text(columns) -> bytes:

@@ -43,6 +43,15 @@ code (oracle/_ref, built from the reference sources by oracle/build_ref.sh).
                       than the relation, where the reference's chunk-relative
                       row ids make its counts differ from set membership.
 
+* bongard_kb_trace.npz (--bongard-kb, about a minute) -- BASELINE config 4
+                      at full scale (1M pictures): the reference learner's
+                      compact trace (checksums in place of binding sets,
+                      coverage steps included), its clauses and its times.
+* after_semijoin_cases.npz (--after-semijoin) -- the reference's
+                      BuildHashTableAfterSemiJoin tables (buckets, the
+                      next links chains reach, mask) for seeded projected
+                      columns and semi-join bits in one or many chunks.
+
 Only this script reads the reference; the tests read the fixtures, so they
 also run where the reference sources are absent.
 """
@@ -337,6 +346,87 @@ def text_cases():
     out["rejects_accepted"] = np.array(accepted)
     print("reference accepted", sum(accepted), "of", len(bad), "rejected texts")
     np.savez_compressed(os.path.join(HERE, "text_cases.npz"), **out)
+
+
+def after_semijoin_cases():
+    """The reference's BuildHashTableAfterSemiJoin on seeded projected columns
+    and semi-join bits: one chunk (a right semi-join's output) and several
+    32768-row chunks (a left semi-join's), where positions are chunk-relative
+    (operations/LeftSemiJoin.hpp:55-83), plus short chunks, no or all bits
+    set and more than six keys (Hash<k> over every key, utility/Hash.hpp:
+    47-55).  num_build_tuples is the projected side's row count, as the
+    learner passes it (learner/QuickFoil.cpp:515-517)."""
+    rng = np.random.default_rng(77)
+    specs = [  # rows, keys, key domain, chunk rows, density of set bits
+        (1000, 1, 300, 0, 0.5), (5000, 2, 40, 0, 0.7), (3000, 3, 8, 0, 0.9),
+        (100_000, 1, 5000, 32768, 0.6), (100_000, 2, 60, 32768, 0.5), (70_000, 3, 12, 32768, 0.8),
+        (20_000, 2, 30, 1000, 0.5), (4000, 2, 50, 0, 0.0), (4000, 2, 50, 0, 1.0),
+        (2000, 7, 3, 0, 0.6), (33_000, 1, 100_000, 32768, 0.9)]
+    out = {"num_cases": np.array([len(specs)])}
+    for j, (n, k, dom, chunk, dens) in enumerate(specs):
+        keys = [rng.integers(0, dom, n).astype(np.int32) for _ in range(k)]
+        flags = rng.random(n) < dens
+        bits = np.packbits(np.concatenate([flags, np.zeros((-n) % 64, bool)]).reshape(-1, 64)[:, ::-1],
+                           axis=1).view(">u8").astype(np.uint64).ravel()
+        # In a short last chunk the reference compares against chain positions
+        # past the chunk's end, reading past the end of its columns.  The
+        # columns handed to it are padded with -1 (outside every key domain
+        # here), so those reads compare unequal, as the engine defines them.
+        padded = [np.concatenate([c, np.full(max(chunk, 1), -1, np.int32)]) for c in keys]
+        buckets, nxt, mask = ref.build_after_semijoin(padded, bits, chunk, n, num_rows=n)
+        out[f"c{j}_meta"] = np.array([n, k, chunk, n, mask], dtype=np.int64)
+        for q, c in enumerate(keys):
+            out[f"c{j}_k{q}"] = c
+        out[f"c{j}_bits"] = bits
+        out[f"c{j}_buckets"] = buckets
+        out[f"c{j}_next"] = nxt
+    np.savez_compressed(os.path.join(HERE, "after_semijoin_cases.npz"), **out)
+    print("after_semijoin_cases.npz:", len(specs), "cases")
+
+
+def column_checksum(v):
+    """The trace's column checksum (oracle/ref_driver.cpp ColumnChecksum)."""
+    v = (np.asarray(v, dtype=np.int32).view(np.uint32).astype(np.uint64) + np.uint64(0x9E3779B9))
+    r = np.arange(len(v), dtype=np.uint64) * np.uint64(2) + np.uint64(1)
+    return int(np.sum(v * r, dtype=np.uint64))
+
+
+def bongard_kb_trace():
+    """BASELINE config 4 at full scale: the Bongard-like knowledge base of
+    workloads.bongard_kb() (1M pictures, element 10M, inside about 16M,
+    100K positives) and the reference learner's compact trace on it --
+    every Evaluate call (binding-set checksums, literals, counts), every
+    binding-set extension (input and output checksums), every coverage step
+    (relation and bound arguments, label-side checksums, examples' checksum,
+    covered count and bit sums) -- with its learnt clauses and its times."""
+    k = workloads.bongard_kb()
+    path = os.path.join(HERE, "_bongard_kb_trace.txt")
+    clauses, secs = ref.learn_compact(k.relations, k.target_columns, k.num_positive,
+                                      k.max_clause_length, path)
+    with open(path, "rb") as f:
+        text = f.read()
+    os.remove(path)
+    out = {"trace": np.frombuffer(text, dtype=np.uint8),
+           "params": np.array([4, 1_000_000, 100_000, k.max_clause_length]),
+           "relation_checksums": np.array([column_checksum(c) for r in k.relations for c in r],
+                                          dtype=np.uint64),
+           "target_checksum": np.array([column_checksum(k.target_columns[0]), k.num_positive],
+                                       dtype=np.uint64),
+           "clauses": np.array(clauses),
+           "reference_seconds": np.array(secs),
+           "reference_host": np.array(["x86_64 build container, 1 thread, -O3"])}
+    np.savez_compressed(os.path.join(HERE, "bongard_kb_trace.npz"), **out)
+    print("bongard_kb_trace.npz:", text.count(b"\n"), "lines;", clauses, secs)
+
+
+if __name__ == "__main__" and "--bongard-kb" in sys.argv:
+    bongard_kb_trace()
+    sys.exit(0)
+
+
+if __name__ == "__main__" and "--after-semijoin" in sys.argv:
+    after_semijoin_cases()
+    sys.exit(0)
 
 
 if __name__ == "__main__" and "--batched-step" not in sys.argv:
