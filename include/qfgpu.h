@@ -71,9 +71,14 @@ enum {
                                    so its bounded wait runs out (QFG_OPT_WAIT_LIMIT polls) and
                                    the call returns QFG_ERR_TIMEOUT; nothing is in flight when
                                    the CTAs stop.  Default 0 */
-  QFG_OPT_COVERAGE_COMPAT = 12  /* 1 = qfg_coverage / qfg_coverage_examples compute coverage as
+  QFG_OPT_COVERAGE_COMPAT = 12, /* 1 = qfg_coverage / qfg_coverage_examples compute coverage as
                                    the reference does, through its chunk-relative projection
                                    tables (see qfg_coverage); 0 (default) = set membership */
+  QFG_OPT_EVAL_MODE = 13        /* batched evaluation: 1 = tiled (binding-row tiles in shared
+                                   memory, relation entries probing them), 2 = streamed
+                                   (relation entries in shared memory, binding rows streamed
+                                   past them), 0 (default) = automatic (the autotuner's choice
+                                   for the size class, else streamed) */
 };
 
 /* Evaluation stages timed under QFG_OPT_STAGE_TIMING (the GPU counterpart of

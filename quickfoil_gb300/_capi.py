@@ -42,6 +42,7 @@ QFG_OPT_PASS1_BITS = 9
 QFG_OPT_SERVER_DEPTH = 10
 QFG_OPT_TEST_WITHHOLD_COPIES = 11
 QFG_OPT_COVERAGE_COMPAT = 12
+QFG_OPT_EVAL_MODE = 13
 
 STAGES = ("key_tables", "bind_partition", "evaluate", "per_literal", "unit_plan",
           "coverage_scan", "coverage_examples")

@@ -30,6 +30,7 @@
 // int64 accumulators and flushed to global memory once per CTA.
 #include <algorithm>
 #include <cstring>
+#include <set>
 #include <unordered_map>
 
 #include "bulk.cuh"
@@ -678,10 +679,21 @@ struct GroupDesc {
   const uint32_t* fstart;   // (2 << bits) + 1 segment starts
   int bits, sbits, ncols;
   int lit_begin, lit_end;
+  int sig_begin, sig_end;   // streamed path: the group's key signatures
   int has_atoms;
   uint32_t p_lo;            // first partition of this context's shard
   int64_t item_begin;
 };
+
+// Streamed path: a key signature is the ascending list of group columns
+// (besides the join column) that a literal's further bound arguments are
+// compared with.  Literals with the same signature share one composite key
+// (join key, the signature columns' values) in the entry table.
+struct SigDesc {
+  int32_t ncols;
+  int32_t col[kGroupCols - 1];
+};
+static_assert(sizeof(SigDesc) == 32, "signature record");
 
 struct LitDesc {
   const int32_t* keys;       // nk SoA columns of `stride` entries
@@ -691,6 +703,8 @@ struct LitDesc {
   int nk;
   int out;                   // literal index in the caller's array
   int8_t atom_col[QFG_MAX_ARITY];  // key q >= 1 is compared with group column atom_col[q]
+  int sig;                   // streamed path: signature (index into the launch's SigDesc array)
+  int8_t spos[QFG_MAX_ARITY];  // key q >= 1: its position in the signature, -1: must equal key 0
 };
 
 struct WorkUnit {
@@ -737,6 +751,10 @@ struct EvalArgs {
   int* error_flag;           // set when a bounded wait gave up
   int64_t wait_limit;        // iterations of a bounded wait
   int withhold_copies;       // tests: arm the tile barrier, issue no copy
+  const SigDesc* sigs;       // streamed path: signatures of the launch's groups
+  uint32_t piece;            // relation entries per work unit
+  uint32_t row_chunk;        // streamed path: binding rows per work unit (0 = all)
+  int records;               // tiled path: units reserve entry records
 };
 
 // Shared-memory stride of a tile column: room for the alignment shifts of
@@ -799,8 +817,10 @@ __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
           const uint32_t* off = a.lits[L].offsets;
           E += __ldg(off + q1) - __ldg(off + q0);
         }
-        nch = (E + kChunk - 1) / kChunk;
-        if (nch > 0) espace = (nch - 1) * kChunk + ((E - (nch - 1) * kChunk + 3u) & ~3u);
+        nch = (E + a.piece - 1) / a.piece;
+        if (a.row_chunk > 0) nch *= 1u + (u.Pp + u.Np - 1u) / a.row_chunk;
+        if (nch > 0 && a.records)
+          espace = (nch - 1) * a.piece + ((E - (nch - 1) * a.piece + 3u) & ~3u);
       }
     }
     // Warp-aggregated reservation of unit slots and entry records.
@@ -821,11 +841,29 @@ __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
     }
     ub = __shfl_sync(kFullMask, ub, 31) + x - nch;
     eb = __shfl_sync(kFullMask, eb, 31) + y - espace;
+    if (a.row_chunk > 0) {
+      // Streamed path: (entry piece, row chunk) pairs; a unit's rows are
+      // [pad, pad + ecnt2) of the item's positives-then-negatives order,
+      // kept in eoff (first row) and pad (row count).
+      const uint32_t rows = u.Pp + u.Np;
+      const uint32_t nrc = rows == 0 ? 1u : 1u + (rows - 1u) / a.row_chunk;
+      for (uint32_t k = 0; k < nch; ++k) {
+        if (ub + k >= a.unit_cap) break;
+        const uint32_t piece = k / nrc, rc = k % nrc;
+        WorkUnit v = u;
+        v.f0 = piece * a.piece;
+        v.ecnt = umin(E - piece * a.piece, a.piece);
+        v.eoff = rc * a.row_chunk;
+        v.pad = umin(rows - rc * a.row_chunk, a.row_chunk);
+        a.units[ub + k] = v;
+      }
+      continue;
+    }
     for (uint32_t k = 0; k < nch; ++k) {
       if (ub + k >= a.unit_cap) break;  // never read: the evaluation stops at unit_cap
-      u.f0 = k * kChunk;
-      u.ecnt = umin(E - k * kChunk, (uint32_t)kChunk);
-      u.eoff = eb + k * kChunk;
+      u.f0 = k * a.piece;
+      u.ecnt = umin(E - k * a.piece, a.piece);
+      u.eoff = eb + k * a.piece;
       if ((uint64_t)u.eoff + ((u.ecnt + 3u) & ~3u) > a.entry_cap) {
         // Out of entry records (the capacity is an upper bound, so this does
         // not happen): an empty unit keeps the list well formed.
@@ -1259,6 +1297,251 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
   }
 }
 
+// ----------------------------------------------------------------------------
+// Streamed evaluation.
+//
+// Work unit = (item, piece of at most kSEntries relation entries, chunk of at
+// most row_chunk binding rows).  The CTA loads the piece's entries -- every
+// literal's distinct key tuples in the item's key range -- into a
+// shared-memory table keyed by (signature, join key, signature columns'
+// keys), chained through 32-bit links (atomicExch on the slot heads); then
+// its threads stream the unit's binding rows straight from the partitioned
+// columns (coalesced loads, no staging) and probe the table once per
+// signature of the group.  A probe that finds an entry of its signature
+// with the row's keys adds 1 to the entry's positive or negative counter.
+// After the rows, each entry adds its counters to its literal: covered +=
+// count, binding += multiplicity x count (a binding row matches at most one
+// distinct key tuple of a literal), and the counters start again at zero.
+
+constexpr int kSThreads = 512;
+constexpr int kSEntries = 2048;        // relation entries per unit
+constexpr int kSSlots = 4096;          // hash slots (twice the entries)
+constexpr int kSMaxSigs = 64;          // signatures of one group
+constexpr uint32_t kSRowTarget = 32768;  // mean binding rows of an item (partition bits)
+constexpr uint32_t kSEntryTarget = kSEntries / 2;  // mean relation entries of an item
+static_assert((kSSlots & (kSSlots - 1)) == 0, "slot count is a power of two");
+
+size_t stream_smem_bytes(int num_lits) {
+  return sizeof(unsigned long long) * 4 * (size_t)num_lits + sizeof(int32_t) * kSSlots +
+         sizeof(int32_t) * 9 * (size_t)kSEntries;
+}
+
+// Hash of a composite key: the join key's mix, salted by the signature,
+// folded with every signature column's key.  Entries and probing rows use
+// the same function.
+__device__ __forceinline__ uint32_t skey_start(uint32_t hk, int sig) {
+  return hk + (uint32_t)sig * 0x61c88647u;
+}
+__device__ __forceinline__ uint32_t skey_fold(uint32_t h, int32_t v) {
+  return (h ^ (uint32_t)v) * 0x85ebca6bu;
+}
+__device__ __forceinline__ uint32_t skey_slot(uint32_t h) { return (h ^ (h >> 15)) & (kSSlots - 1); }
+
+__device__ __forceinline__ int32_t pick(const int32_t (&v)[kGroupCols], int c) {
+  int32_t x = v[0];
+#pragma unroll
+  for (int q = 1; q < kGroupCols; ++q) x = c == q ? v[q] : x;
+  return x;
+}
+
+__global__ void __launch_bounds__(kSThreads, 2) stream_eval_kernel(EvalArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem);
+  int32_t* head = reinterpret_cast<int32_t*>(acc + 4 * a.num_lits);  // kSSlots
+  int32_t* e_k0 = head + kSSlots;                                    // kSEntries each:
+  int32_t* e_s1 = e_k0 + kSEntries;
+  int32_t* e_s2 = e_s1 + kSEntries;
+  uint32_t* e_meta = reinterpret_cast<uint32_t*>(e_s2 + kSEntries);  // literal | sig << 10 | valid << 31
+  int32_t* e_mult = reinterpret_cast<int32_t*>(e_meta + kSEntries);
+  uint32_t* e_cp = reinterpret_cast<uint32_t*>(e_mult + kSEntries);
+  uint32_t* e_cn = e_cp + kSEntries;
+  int32_t* e_next = reinterpret_cast<int32_t*>(e_cn + kSEntries);
+  int32_t* e_gidx = e_next + kSEntries;  // key-table index (signatures of more than two columns)
+  __shared__ uint32_t s_lstart[kMaxGroupLits + 1];
+  __shared__ uint32_t s_le0[kMaxGroupLits];
+  __shared__ SigDesc s_sig[kSMaxSigs];
+  __shared__ WorkUnit s_unit;
+  __shared__ uint32_t s_idx, s_count;
+  __shared__ int s_group;  // group whose signatures s_sig holds
+
+  for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) acc[i] = 0ull;
+  for (int i = threadIdx.x; i < kSSlots; i += blockDim.x) head[i] = -1;
+  for (int i = threadIdx.x; i < kSEntries; i += blockDim.x) {
+    e_cp[i] = 0u;
+    e_cn[i] = 0u;
+  }
+  if (threadIdx.x == 0) {
+    s_count = umin(a.unit_count[0], a.unit_cap);
+    s_idx = atomicAdd(a.work_counter, 1u);
+    if (s_idx < s_count) s_unit = a.units[s_idx];
+    s_group = -1;
+  }
+  __syncthreads();
+  const int lane = lane_id(), warp = warp_id();
+
+  for (;;) {
+    const uint32_t idx = s_idx;
+    if (idx >= s_count) break;
+    const WorkUnit U = s_unit;
+    const GroupDesc& G = a.groups[U.group];
+    const int m = G.lit_end - G.lit_begin;
+    const int nsig = G.sig_end - G.sig_begin;
+    uint32_t nidx = 0;
+    if (threadIdx.x == 0) nidx = atomicAdd(a.work_counter, 1u);
+    // The item's literal-major entry space (warp 0) and the group's
+    // signatures (warp 1) in shared memory.
+    if (warp == 0) {
+      const int rshift = kRelPartitionBits - G.bits;
+      const uint32_t q0 = U.p << rshift, q1 = (U.p + 1) << rshift;
+      uint32_t run = 0;
+      for (int L0 = 0; L0 < m; L0 += 32) {
+        const int L = L0 + lane;
+        uint32_t c = 0;
+        if (L < m) {
+          const uint32_t* off = a.lits[G.lit_begin + L].offsets;
+          const uint32_t e0 = __ldg(off + q0);
+          c = __ldg(off + q1) - e0;
+          s_le0[L] = e0;
+        }
+        uint32_t x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(kFullMask, x, o);
+          if (lane >= o) x += y;
+        }
+        if (L < m) s_lstart[L] = run + x - c;
+        run += __shfl_sync(kFullMask, x, 31);
+      }
+      if (lane == 0) s_lstart[m] = run;
+    } else if (warp == 1 && s_group != (int)U.group) {
+      for (int q = lane; q < nsig; q += 32) s_sig[q] = a.sigs[G.sig_begin + q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_group = (int)U.group;
+    // The unit's entries into the table.
+    for (uint32_t j = threadIdx.x; j < U.ecnt; j += blockDim.x) {
+      const uint32_t f = U.f0 + j;
+      int lo = 0, hi = m - 1;  // largest L with s_lstart[L] <= f
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_lstart[mid] <= f) lo = mid; else hi = mid - 1;
+      }
+      const LitDesc& d = a.lits[G.lit_begin + lo];
+      const uint32_t e = s_le0[lo] + (f - s_lstart[lo]);
+      const int32_t k0 = __ldg(d.keys + e);
+      const int sg = d.sig - G.sig_begin;
+      const SigDesc& S = s_sig[sg];
+      int32_t sk[kGroupCols - 1];
+#pragma unroll
+      for (int i = 0; i < kGroupCols - 1; ++i) sk[i] = 0;
+      uint32_t filled = 0;
+      bool valid = true;
+      for (int q = 1; q < d.nk; ++q) {
+        const int32_t kq = __ldg(d.keys + q * d.stride + e);
+        const int pq = d.spos[q];
+        if (pq < 0) {
+          valid &= kq == k0;
+        } else {
+#pragma unroll
+          for (int i = 0; i < kGroupCols - 1; ++i) {
+            if (i != pq) continue;
+            if (filled & (1u << i)) valid &= sk[i] == kq;
+            sk[i] = kq;
+          }
+          filled |= 1u << pq;
+        }
+      }
+      uint32_t h = skey_start(mix32((uint32_t)k0), sg);
+#pragma unroll
+      for (int i = 0; i < kGroupCols - 1; ++i)
+        if (i < S.ncols) h = skey_fold(h, sk[i]);
+      e_k0[j] = k0;
+      e_s1[j] = sk[0];
+      e_s2[j] = sk[1];
+      e_mult[j] = __ldg(d.mult + e);
+      e_gidx[j] = (int32_t)e;
+      e_meta[j] = (uint32_t)lo | ((uint32_t)sg << 10) | (valid ? 0x80000000u : 0u);
+      e_next[j] = valid ? atomicExch(&head[skey_slot(h)], (int32_t)j) : -1;
+    }
+    __syncthreads();
+    // The unit's binding rows, positives then negatives, against the table.
+    {
+      const int ncols = G.ncols;
+      const int64_t stride = G.n;
+      const uint32_t r0 = U.eoff, r1 = U.eoff + U.pad;  // rows of the item, positives first
+      for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const bool pos = r < U.Pp;
+        const uint32_t row = pos ? U.ps + r : U.ns + (r - U.Pp);
+        int32_t v[kGroupCols];
+#pragma unroll
+        for (int q = 0; q < kGroupCols; ++q) v[q] = q < ncols ? __ldg(G.cols + q * stride + row) : 0;
+        uint32_t* cnt = pos ? e_cp : e_cn;
+        const uint32_t hk = mix32((uint32_t)v[0]);
+        for (int sg = 0; sg < nsig; ++sg) {
+          const SigDesc& S = s_sig[sg];
+          uint32_t h = skey_start(hk, sg);
+          for (int i = 0; i < S.ncols; ++i) h = skey_fold(h, pick(v, S.col[i]));
+          for (int e = head[skey_slot(h)]; e >= 0; e = e_next[e]) {
+            if ((int)((e_meta[e] >> 10) & 0x3ffu) != sg || e_k0[e] != v[0]) continue;
+            if (S.ncols >= 1 && e_s1[e] != pick(v, S.col[0])) continue;
+            if (S.ncols >= 2 && e_s2[e] != pick(v, S.col[1])) continue;
+            if (S.ncols > 2) {
+              // Further signature columns from the key table.
+              const LitDesc& d = a.lits[G.lit_begin + (e_meta[e] & 0x3ffu)];
+              bool ok = true;
+              for (int q = 1; q < d.nk && ok; ++q) {
+                const int pq = d.spos[q];
+                if (pq >= 2) ok = __ldg(d.keys + q * d.stride + e_gidx[e]) == pick(v, S.col[pq]);
+              }
+              if (!ok) continue;
+            }
+            atomicAdd(&cnt[e], 1u);
+          }
+        }
+      }
+    }
+    if (threadIdx.x == 0 && nidx < s_count) s_unit = a.units[nidx];
+    __syncthreads();
+    // Entry counters into the literals' sums; entries are literal-major, so
+    // equal literals sit on consecutive lanes (segmented warp scans).
+    for (uint32_t j0 = 0; j0 < U.ecnt; j0 += blockDim.x) {
+      const uint32_t j = j0 + threadIdx.x;
+      int L = -1;
+      long long cp = 0, cn = 0, bp = 0, bn = 0;
+      if (j < U.ecnt) {
+        const uint32_t meta = e_meta[j];
+        L = (int)(meta & 0x3ffu);
+        const uint32_t p = e_cp[j], q = e_cn[j];
+        if (p | q) {
+          const long long mlt = e_mult[j];
+          cp = p;
+          cn = q;
+          bp = mlt * p;
+          bn = mlt * q;
+          e_cp[j] = 0u;
+          e_cn[j] = 0u;
+        }
+      }
+      cp = seg_scan(cp, L);
+      cn = seg_scan(cn, L);
+      bp = seg_scan(bp, L);
+      bn = seg_scan(bn, L);
+      const int next_L = __shfl_down_sync(kFullMask, L, 1);
+      if ((lane == 31 || next_L != L) && L >= 0 && (cp | cn | bp | bn) != 0)
+        flush_acc(acc + 4 * (G.lit_begin + L), cp, cn, bp, bn);
+    }
+    // Every slot head back to empty (a few stores a thread).
+    for (int i = threadIdx.x; i < kSSlots; i += blockDim.x) head[i] = -1;
+    if (threadIdx.x == 0) s_idx = nidx;
+    __syncthreads();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) {
+    const unsigned long long v = acc[i];
+    if (v != 0ull) atomicAdd(&a.counts[4 * a.lits[i >> 2].out + (i & 3)], v);
+  }
+}
+
 // Binding-size class of the autotuner: floor(log2(rows)).
 int size_class(int64_t n) {
   int c = 0;
@@ -1371,7 +1654,10 @@ struct StepPlan {
   std::vector<HostGroup> groups;
 };
 
-static int plan_step(Ctx* ctx, int32_t n, const qfg_literal* lits, StepPlan* plan) {
+// max_sigs > 0 (streamed path): a group holds literals of at most max_sigs
+// distinct key signatures (sets of further bound binding columns).
+static int plan_step(Ctx* ctx, int32_t n, const qfg_literal* lits, StepPlan* plan,
+                     int max_sigs = 0) {
   plan->tables.assign(n, nullptr);
   plan->bind_cols.assign(n, {});
   for (int i = 0; i < n; ++i) {
@@ -1402,22 +1688,35 @@ static int plan_step(Ctx* ctx, int32_t n, const qfg_literal* lits, StepPlan* pla
     }
     return add;
   };
+  auto signature = [&](int i) {
+    std::vector<int> sig;
+    for (size_t q = 1; q < bind_cols[i].size(); ++q)
+      if (bind_cols[i][q] != bind_cols[i][0]) sig.push_back(bind_cols[i][q]);
+    std::sort(sig.begin(), sig.end());
+    sig.erase(std::unique(sig.begin(), sig.end()), sig.end());
+    return sig;
+  };
   for (auto& kv : by_col) {
     HostGroup cur;
+    std::set<std::vector<int>> sigs;
     cur.join_col = kv.first;
     cur.cols = {kv.first};
     for (int i : kv.second) {
       std::vector<int> add = missing_cols(cur, i);
+      const std::vector<int> sig = signature(i);
       if ((int)(cur.cols.size() + add.size()) > kGroupCols ||
-          (int)cur.lits.size() >= kMaxGroupLits) {
+          (int)cur.lits.size() >= kMaxGroupLits ||
+          (max_sigs > 0 && !sigs.count(sig) && (int)sigs.size() >= max_sigs)) {
         groups.push_back(cur);
         cur = HostGroup();
+        sigs.clear();
         cur.join_col = kv.first;
         cur.cols = {kv.first};
         add = missing_cols(cur, i);
       }
       cur.cols.insert(cur.cols.end(), add.begin(), add.end());
       cur.lits.push_back(i);
+      sigs.insert(sig);
       if (bind_cols[i].size() > 1) cur.has_atoms = true;
     }
     groups.push_back(cur);
@@ -1431,8 +1730,11 @@ static int plan_step(Ctx* ctx, int32_t n, const qfg_literal* lits, StepPlan* pla
 // synchronization), so a prepared step can be enqueued directly or captured
 // into a CUDA graph and replayed on new binding data of the same shape.
 struct PartJob {
-  BPartArgs pa;
+  BPartArgs pa;             // pa.bits / pa.cbits: this group's partition shape
   bool vec;
+  bool two_pass;
+  int np1, sbits;
+  size_t p1_smem, p2_smem;
   int32_t* final_out;
   uint32_t* fstart;
 };
@@ -1443,14 +1745,14 @@ struct LaunchJob {
   int grid;
   int plan_grid;
   int gather_grid;
+  bool streamed;
 };
 
 struct PreparedStep {
-  int bits = 0, cbits = 0, sbits = 0, np1 = 0;
-  bool two_pass = false;
+  int mode = 0;             // kModeTiled or kModeStreamed
   unsigned pgrid = 0;
-  size_t p1_smem = 0, p2_smem = 0;
   uint32_t* p1_tot = nullptr;
+  uint32_t* p1_base = nullptr;
   uint32_t* p1_start = nullptr;   // padded bin starts (two passes)
   uint32_t* p1_unp = nullptr;     // unpadded bin starts (two passes)
   uint32_t* chunk_start = nullptr;  // first pass-2 chunk of every bin
@@ -1466,6 +1768,60 @@ struct PreparedStep {
   unsigned int* counter = nullptr;  // [work counter, unit count, entry-record count]
 };
 
+constexpr int kModeTiled = 1;
+constexpr int kModeStreamed = 2;
+
+int step_mode(Ctx* ctx) { return ctx->eval_mode == kModeTiled ? kModeTiled : kModeStreamed; }
+
+// Partition bits of one literal group.  Tiled: from the binding-set size
+// (rows per shared-memory tile).  Streamed: enough partitions that the mean
+// item holds at most kSEntryTarget of the group's relation entries (they
+// must fit the shared-memory table) and at most kSRowTarget binding rows
+// (work balance).  QFG_OPT_EVAL_BITS fixes the bits of every group.
+int group_bits(Ctx* ctx, int mode, int64_t nb, int64_t entries) {
+  if (mode == kModeTiled || ctx->eval_bits > 0) return auto_group_bits(ctx, nb);
+  int bits = 1;
+  while (bits < kMaxPartitionBits &&
+         ((entries >> bits) > (int64_t)kSEntryTarget || (nb >> bits) > (int64_t)kSRowTarget))
+    ++bits;
+  return bits;
+}
+
+// The key signatures of a group (streamed path) and, per literal, its
+// signature and the signature position of every further key.
+void group_signatures(const HostGroup& g, const std::vector<std::vector<int>>& bind_cols,
+                      std::vector<SigDesc>* sigs, std::vector<int>* lit_sig,
+                      std::vector<std::vector<int8_t>>* lit_spos) {
+  std::vector<std::vector<int>> lists;
+  lit_sig->clear();
+  lit_spos->clear();
+  for (int i : g.lits) {
+    std::vector<int> cols;
+    for (size_t q = 1; q < bind_cols[i].size(); ++q) {
+      const int c = (int)(std::find(g.cols.begin(), g.cols.end(), bind_cols[i][q]) - g.cols.begin());
+      if (c != 0 && std::find(cols.begin(), cols.end(), c) == cols.end()) cols.push_back(c);
+    }
+    std::sort(cols.begin(), cols.end());
+    int sig = (int)(std::find(lists.begin(), lists.end(), cols) - lists.begin());
+    if (sig == (int)lists.size()) lists.push_back(cols);
+    std::vector<int8_t> spos(QFG_MAX_ARITY, -1);
+    for (size_t q = 1; q < bind_cols[i].size(); ++q) {
+      const int c = (int)(std::find(g.cols.begin(), g.cols.end(), bind_cols[i][q]) - g.cols.begin());
+      spos[q] = c == 0 ? -1 : (int8_t)(std::find(cols.begin(), cols.end(), c) - cols.begin());
+    }
+    lit_sig->push_back(sig);
+    lit_spos->push_back(spos);
+  }
+  sigs->clear();
+  for (const auto& l : lists) {
+    SigDesc d;
+    memset(&d, 0, sizeof(d));
+    d.ncols = (int32_t)l.size();
+    for (size_t i = 0; i < l.size(); ++i) d.col[i] = l[i];
+    sigs->push_back(d);
+  }
+}
+
 int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* lits,
                  unsigned long long* counts, PreparedStep* ps) {
   const int64_t nb = b->num_positive + b->num_negative;
@@ -1473,86 +1829,99 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   ps->launches.clear();
   ps->blob.clear();
   if (n == 0 || nb == 0) return QFG_OK;
+  const int mode = step_mode(ctx);
+  ps->mode = mode;
 
   QFG_TRY(stage_begin(ctx, QFG_STAGE_KEY_TABLES));
   StepPlan plan;
-  QFG_TRY(plan_step(ctx, n, lits, &plan));
+  QFG_TRY(plan_step(ctx, n, lits, &plan, mode == kModeStreamed ? kSMaxSigs : 0));
   QFG_TRY(stage_end(ctx, QFG_STAGE_KEY_TABLES));
   const auto& tables = plan.tables;
   const auto& bind_cols = plan.bind_cols;
   const auto& groups = plan.groups;
-
-  // Partition shape and shard.
-  const int bits = auto_group_bits(ctx, nb);
   if (ctx->shard_index >= ctx->shard_count)
     return set_error(ctx, QFG_ERR_INVALID, "shard index must be below the shard count");
-  // Shard s owns partitions [s * 2^bits / S, (s + 1) * 2^bits / S).
-  const uint32_t shard_lo = (uint32_t)(((int64_t)ctx->shard_index << bits) / ctx->shard_count);
-  const uint32_t shard_hi = (uint32_t)(((int64_t)(ctx->shard_index + 1) << bits) / ctx->shard_count);
-  ps->bits = bits;
-  ps->two_pass = bits > kMaxSinglePassBits;
-  ps->cbits = ps->two_pass ? coarse_bits(ctx, nb, bits) : bits;
-  ps->sbits = bits - ps->cbits;
-  const int nfine = 2 << bits;
-  ps->np1 = 2 << ps->cbits;
+
+  // Partition shape of every group.
   ps->pgrid = (unsigned)ctx->num_sms;
   // Partitioned columns: stride a multiple of 4 rows, so every column of a
   // group has the same 16-byte alignment (the evaluation's bulk copies).
   ps->col_stride = ((int64_t)nb + 3) & ~int64_t(3);
-  size_t part_words = 0;
-  int max_ncols = 1;
-  for (auto& g : groups) {
+  std::vector<int> gbits(groups.size());
+  size_t part_words = 0, fs_words = 0;
+  int max_ncols = 1, np1_max = 2, sbits_max = 0;
+  bool any_two_pass = false;
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const HostGroup& g = groups[gi];
+    int64_t entries = 0;
+    for (int i : g.lits) entries += tables[i]->num_entries;
+    gbits[gi] = group_bits(ctx, mode, nb, entries);
     part_words += g.cols.size() * (size_t)ps->col_stride;
+    fs_words += ((size_t)2 << gbits[gi]) + 1;
     max_ncols = std::max(max_ncols, (int)g.cols.size());
+    const bool two = gbits[gi] > kMaxSinglePassBits;
+    const int cb = two ? coarse_bits(ctx, nb, gbits[gi]) : gbits[gi];
+    np1_max = std::max(np1_max, 2 << cb);
+    if (two) {
+      any_two_pass = true;
+      sbits_max = std::max(sbits_max, gbits[gi] - cb);
+    }
   }
   // Pass-1 output: bins padded to multiples of 4 rows, 16-byte aligned columns.
-  ps->tmp_stride = ps->two_pass ? (((int64_t)nb + 3) & ~int64_t(3)) + 4 * (int64_t)ps->np1 : 0;
+  ps->tmp_stride = any_two_pass ? (((int64_t)nb + 3) & ~int64_t(3)) + 4 * (int64_t)np1_max : 0;
   const size_t tmp_off = (part_words + 63) & ~size_t(63);
-  const size_t tmp_words = ps->two_pass ? (size_t)max_ncols * (size_t)ps->tmp_stride : 0;
-  const size_t fs_words = (size_t)nfine + 1;
+  const size_t tmp_words = any_two_pass ? (size_t)max_ncols * (size_t)ps->tmp_stride : 0;
   const size_t h2_words =
-      ps->two_pass ? ((size_t)nb / kP2Chunk + (size_t)ps->np1 + 1) * ((size_t)1 << ps->sbits) : 0;
-  const size_t chunk_words = ps->two_pass ? (size_t)nb / kP2Chunk + (size_t)ps->np1 + 1 : 0;
-  const size_t bins_words = (size_t)ps->np1 + 1 + (size_t)ps->pgrid * ps->np1 +
-                            3 * ((size_t)ps->np1 + 1) + h2_words + chunk_words;
+      any_two_pass ? ((size_t)nb / kP2Chunk + (size_t)np1_max + 1) * ((size_t)1 << sbits_max) : 0;
+  const size_t chunk_words = any_two_pass ? (size_t)nb / kP2Chunk + (size_t)np1_max + 1 : 0;
+  const size_t bins_words = (size_t)np1_max + 1 + (size_t)ps->pgrid * np1_max +
+                            3 * ((size_t)np1_max + 1) + h2_words + chunk_words;
   QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * (tmp_off + tmp_words)));
-  QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(
-      ctx, sizeof(uint32_t) * (groups.size() * fs_words + bins_words)));
+  QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(ctx, sizeof(uint32_t) * (fs_words + bins_words)));
   int32_t* part_base = ctx->scratch[kScrBindPart].as<int32_t>();
   ps->tmp_cols = part_base + tmp_off;
   uint32_t* fstarts = ctx->scratch[kScrBindOffsets].as<uint32_t>();
-  ps->p1_tot = fstarts + groups.size() * fs_words;
-  uint32_t* p1_base = ps->p1_tot + ps->np1 + 1;
-  ps->p1_start = p1_base + (size_t)ps->pgrid * ps->np1;
-  ps->p1_unp = ps->p1_start + ps->np1 + 1;
-  ps->chunk_start = ps->p1_unp + ps->np1 + 1;
-  ps->h2 = ps->chunk_start + ps->np1 + 1;
+  ps->p1_tot = fstarts + fs_words;
+  ps->p1_base = ps->p1_tot + np1_max + 1;
+  ps->p1_start = ps->p1_base + (size_t)ps->pgrid * np1_max;
+  ps->p1_unp = ps->p1_start + np1_max + 1;
+  ps->chunk_start = ps->p1_unp + np1_max + 1;
+  ps->h2 = ps->chunk_start + np1_max + 1;
   ps->chunk_bin = ps->h2 + h2_words;
-  ps->p1_smem = pass_smem_bytes(ps->np1);
-  ps->p2_smem = pass_smem_bytes(1 << ps->sbits);
   QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)ps->p1_smem));
+                                     (int)pass_smem_bytes(np1_max)));
   QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)ps->p2_smem));
+                                     (int)pass_smem_bytes(1 << std::max(sbits_max, 1))));
 
   std::vector<GroupDesc> gdesc(groups.size());
   std::vector<LitDesc> ldesc;
-  size_t off = 0;
+  std::vector<SigDesc> sdesc;
+  size_t off = 0, fs_off = 0;
   int64_t items = 0;
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     const HostGroup& g = groups[gi];
+    const int bits = gbits[gi];
+    // Shard s owns partitions [s * 2^bits / S, (s + 1) * 2^bits / S).
+    const uint32_t shard_lo = (uint32_t)(((int64_t)ctx->shard_index << bits) / ctx->shard_count);
+    const uint32_t shard_hi = (uint32_t)(((int64_t)(ctx->shard_index + 1) << bits) / ctx->shard_count);
     PartJob job;
+    job.two_pass = bits > kMaxSinglePassBits;
+    const int cbits = job.two_pass ? coarse_bits(ctx, nb, bits) : bits;
+    job.sbits = bits - cbits;
+    job.np1 = 2 << cbits;
+    job.p1_smem = pass_smem_bytes(job.np1);
+    job.p2_smem = pass_smem_bytes(1 << std::max(job.sbits, 1));
     BPartArgs& pa = job.pa;
     pa.ncols = (int)g.cols.size();
     for (int c = 0; c < pa.ncols; ++c) pa.cols[c] = b->columns[g.cols[c]];
     pa.n = nb;
     pa.npos = b->num_positive;
     pa.bits = bits;
-    pa.cbits = ps->cbits;
+    pa.cbits = cbits;
     pa.p1_tot = ps->p1_tot;
-    pa.p1_base = p1_base;
+    pa.p1_base = ps->p1_base;
     job.final_out = part_base + off;
-    job.fstart = fstarts + gi * fs_words;
+    job.fstart = fstarts + fs_off;
     job.vec = true;
     for (int c = 0; c < pa.ncols; ++c)
       if (reinterpret_cast<uintptr_t>(pa.cols[c]) % 16 != 0) job.vec = false;
@@ -1563,14 +1932,22 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     d.n = ps->col_stride;
     d.fstart = job.fstart;
     d.bits = bits;
-    d.sbits = ps->sbits;
+    d.sbits = job.sbits;
     d.ncols = pa.ncols;
     d.lit_begin = (int)ldesc.size();
     d.has_atoms = g.has_atoms ? 1 : 0;
     d.p_lo = shard_lo;
     d.item_begin = items;
     items += (int64_t)(shard_hi - shard_lo);
-    for (int i : g.lits) {
+    std::vector<SigDesc> gsig;
+    std::vector<int> lit_sig;
+    std::vector<std::vector<int8_t>> lit_spos;
+    if (mode == kModeStreamed) group_signatures(g, bind_cols, &gsig, &lit_sig, &lit_spos);
+    d.sig_begin = (int)sdesc.size();
+    sdesc.insert(sdesc.end(), gsig.begin(), gsig.end());
+    d.sig_end = (int)sdesc.size();
+    for (size_t li = 0; li < g.lits.size(); ++li) {
+      const int i = g.lits[li];
       LitDesc ld;
       memset(&ld, 0, sizeof(ld));
       KeyTable* kt = tables[i];
@@ -1582,21 +1959,29 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
       for (int q = 1; q < ld.nk; ++q)
         ld.atom_col[q] = (int8_t)(std::find(g.cols.begin(), g.cols.end(), bind_cols[i][q]) - g.cols.begin());
       ld.out = i;
+      if (mode == kModeStreamed) {
+        ld.sig = d.sig_begin + lit_sig[li];
+        for (int q = 0; q < QFG_MAX_ARITY; ++q) ld.spos[q] = lit_spos[li][q];
+      }
       ldesc.push_back(ld);
     }
     d.lit_end = (int)ldesc.size();
     off += g.cols.size() * (size_t)ps->col_stride;
+    fs_off += ((size_t)2 << bits) + 1;
   }
 
   // Launches of at most kMaxLitsPerLaunch literals (groups never straddle a
   // launch: they are capped below that size); each launch gets a rebased copy
-  // of its groups, and all descriptors go up in one copy.
+  // of its groups (literal and signature indices relative to the launch),
+  // and all descriptors go up in one copy.
   struct Span {
     size_t gbeg, gend;
-    int lit0, nl;
+    int lit0, nl, sig0;
   };
   std::vector<Span> spans;
   std::vector<GroupDesc> sub_all;
+  std::vector<LitDesc> lit_all;
+  std::vector<SigDesc> sig_all;
   for (size_t gbeg = 0; gbeg < gdesc.size();) {
     size_t gend = gbeg;
     int nl = 0;
@@ -1606,36 +1991,53 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
       ++gend;
     }
     const int lit0 = gdesc[gbeg].lit_begin;
+    const int sig0 = gdesc[gbeg].sig_begin;
     const int64_t item0 = gdesc[gbeg].item_begin;
     for (size_t g = gbeg; g < gend; ++g) {
       GroupDesc sd = gdesc[g];
       sd.lit_begin -= lit0;
       sd.lit_end -= lit0;
+      sd.sig_begin -= sig0;
+      sd.sig_end -= sig0;
       sd.item_begin -= item0;
       sub_all.push_back(sd);
     }
-    spans.push_back({gbeg, gend, lit0, nl});
+    for (int l = lit0; l < lit0 + nl; ++l) {
+      LitDesc ld = ldesc[l];
+      ld.sig -= sig0;
+      lit_all.push_back(ld);
+    }
+    spans.push_back({gbeg, gend, lit0, nl, sig0});
     gbeg = gend;
   }
+  for (const SigDesc& sd : sdesc) sig_all.push_back(sd);
   const size_t gbytes = sizeof(GroupDesc) * sub_all.size();
-  const size_t lbytes = sizeof(LitDesc) * ldesc.size();
-  ps->blob.resize(gbytes + lbytes);
+  const size_t lbytes = sizeof(LitDesc) * lit_all.size();
+  const size_t sbytes = sizeof(SigDesc) * sig_all.size();
+  ps->blob.resize(gbytes + lbytes + sbytes);
   memcpy(ps->blob.data(), sub_all.data(), gbytes);
-  memcpy(ps->blob.data() + gbytes, ldesc.data(), lbytes);
+  memcpy(ps->blob.data() + gbytes, lit_all.data(), lbytes);
+  if (sbytes) memcpy(ps->blob.data() + gbytes + lbytes, sig_all.data(), sbytes);
   QFG_TRY(ctx->scratch[kScrLits].reserve(ctx, ps->blob.size() + 64));
-  // Work units: at most one per item plus one per kChunk entries; entry
-  // records: every entry once, each unit's block padded to 4 records.
+  // Work units: at most one per item plus one per `piece` entries; entry
+  // records (tiled path): every entry once, each unit's block padded to 4.
+  const uint32_t piece = mode == kModeStreamed ? (uint32_t)kSEntries : (uint32_t)kChunk;
   std::vector<int64_t> caps, ecaps;
   int64_t max_cap = 1, max_ecap = 4;
   for (const Span& S : spans) {
     int64_t cap = 1, ecap = 4;
-    for (size_t g = S.gbeg; g < S.gend; ++g) cap += (int64_t)(shard_hi - shard_lo);
+    for (size_t g = S.gbeg; g < S.gend; ++g) {
+      const int bits = gbits[g];
+      cap += (int64_t)((((int64_t)(ctx->shard_index + 1) << bits) / ctx->shard_count) -
+                       (((int64_t)ctx->shard_index << bits) / ctx->shard_count));
+    }
     for (int l = S.lit0; l < S.lit0 + S.nl; ++l) {
-      cap += ldesc[l].stride / kChunk + 1;
+      cap += ldesc[l].stride / piece + 1;
       ecap += ldesc[l].stride;
     }
     ecap += 4 * cap;
     ecap = (ecap + 3) & ~int64_t(3);
+    if (mode == kModeStreamed) ecap = 4;
     if (cap > (int64_t)UINT32_MAX || ecap > (int64_t)UINT32_MAX)
       return set_error(ctx, QFG_ERR_INVALID, "too many work units");
     caps.push_back(cap);
@@ -1656,17 +2058,27 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   }
   GroupDesc* gdev = ctx->scratch[kScrLits].as<GroupDesc>();
   LitDesc* ldev = reinterpret_cast<LitDesc*>(gdev + sub_all.size());
+  SigDesc* sdev = reinterpret_cast<SigDesc*>(ldev + lit_all.size());
   ps->blob_dev = gdev;
-  ps->counter = reinterpret_cast<unsigned int*>(ldev + ldesc.size());
+  ps->counter = reinterpret_cast<unsigned int*>(sdev + sig_all.size());
   for (size_t si = 0; si < spans.size(); ++si) {
     const Span& S = spans[si];
     LaunchJob L;
+    L.streamed = mode == kModeStreamed;
     EvalArgs& ea = L.ea;
+    memset(&ea, 0, sizeof(ea));
     ea.groups = gdev + S.gbeg;
     ea.num_groups = (int)(S.gend - S.gbeg);
     ea.lits = ldev + S.lit0;
     ea.num_lits = S.nl;
-    ea.total_items = (int64_t)(S.gend - S.gbeg) * (int64_t)(shard_hi - shard_lo);
+    ea.sigs = sdev + S.sig0;
+    int64_t total = 0;
+    for (size_t g = S.gbeg; g < S.gend; ++g) {
+      const int bits = gbits[g];
+      total += (int64_t)((((int64_t)(ctx->shard_index + 1) << bits) / ctx->shard_count) -
+                         (((int64_t)ctx->shard_index << bits) / ctx->shard_count));
+    }
+    ea.total_items = total;
     ea.work_counter = ps->counter;
     ea.units = ctx->scratch[kScrWork].as<WorkUnit>();
     ea.unit_count = ps->counter + 1;
@@ -1677,14 +2089,25 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     ea.wait_limit = ctx->wait_limit;
     ea.withhold_copies = ctx->withhold_copies ? 1 : 0;
     ea.counts = counts;
+    ea.piece = piece;
+    ea.row_chunk = L.streamed ? 0xffffffffu : 0u;  // streamed: a unit streams all its item's rows
+    ea.records = L.streamed ? 0 : 1;
     ea.max_cols = 1;
     for (size_t g = S.gbeg; g < S.gend; ++g) ea.max_cols = std::max(ea.max_cols, gdesc[g].ncols);
-    L.smem = eval_smem_bytes(S.nl, ea.max_cols);
-    QFG_CUDA(ctx, cudaFuncSetAttribute(eval_batched_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
     int per_sm = 0;
-    QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_batched_kernel,
-                                                               kEvalThreads, L.smem));
+    if (L.streamed) {
+      L.smem = stream_smem_bytes(S.nl);
+      QFG_CUDA(ctx, cudaFuncSetAttribute(stream_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)L.smem));
+      QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stream_eval_kernel,
+                                                                 kSThreads, L.smem));
+    } else {
+      L.smem = eval_smem_bytes(S.nl, ea.max_cols);
+      QFG_CUDA(ctx, cudaFuncSetAttribute(eval_batched_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+      QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_batched_kernel,
+                                                                 kEvalThreads, L.smem));
+    }
     L.grid = ctx->num_sms * std::max(per_sm, 1);
     // One wave of resident gather blocks: each block strides over the units,
     // so blocks beyond what the SMs hold at once would run as a second wave.
@@ -1704,32 +2127,32 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
   if (ps.parts.empty()) return QFG_OK;
   QFG_TRY(stage_begin(ctx, QFG_STAGE_BIND_PARTITION));
   for (const PartJob& job : ps.parts) {
-    QFG_CUDA(ctx, cudaMemsetAsync(ps.p1_tot, 0, sizeof(uint32_t) * (size_t)ps.np1, ctx->stream));
+    QFG_CUDA(ctx, cudaMemsetAsync(ps.p1_tot, 0, sizeof(uint32_t) * (size_t)job.np1, ctx->stream));
     if (job.vec)
       bpart_hist_kernel<true><<<ps.pgrid, kPartThreads, 0, ctx->stream>>>(job.pa);
     else
       bpart_hist_kernel<false><<<ps.pgrid, kPartThreads, 0, ctx->stream>>>(job.pa);
     QFG_LAUNCHED(ctx);
-    if (ps.two_pass) {
-      pad_scan_kernel<<<1, 512, 0, ctx->stream>>>(ps.p1_tot, ps.np1, ps.p1_start, ps.p1_unp,
+    if (job.two_pass) {
+      pad_scan_kernel<<<1, 512, 0, ctx->stream>>>(ps.p1_tot, job.np1, ps.p1_start, ps.p1_unp,
                                                   ps.chunk_start, ps.chunk_bin);
       QFG_LAUNCHED(ctx);
-      bpart_pass1_kernel<<<ps.pgrid, kPassThreads, ps.p1_smem, ctx->stream>>>(
+      bpart_pass1_kernel<<<ps.pgrid, kPassThreads, job.p1_smem, ctx->stream>>>(
           job.pa, ps.p1_start, ps.tmp_cols, ps.tmp_stride, job.vec ? 1 : 0);
       QFG_LAUNCHED(ctx);
       bpart_p2hist_kernel<<<ps.pgrid * 2, 512, 0, ctx->stream>>>(
           job.pa, ps.p1_start, ps.p1_unp, ps.chunk_start, ps.chunk_bin, ps.tmp_cols, ps.h2);
       QFG_LAUNCHED(ctx);
-      bpart_p2scan_kernel<<<ps.np1, 512, 0, ctx->stream>>>(job.pa, ps.p1_unp, ps.chunk_start, ps.h2,
-                                                           job.fstart);
+      bpart_p2scan_kernel<<<job.np1, 512, 0, ctx->stream>>>(job.pa, ps.p1_unp, ps.chunk_start, ps.h2,
+                                                            job.fstart);
       QFG_LAUNCHED(ctx);
-      bpart_pass2_kernel<<<ps.pgrid, kPassThreads, ps.p2_smem, ctx->stream>>>(
+      bpart_pass2_kernel<<<ps.pgrid, kPassThreads, job.p2_smem, ctx->stream>>>(
           job.pa, ps.p1_start, ps.p1_unp, ps.chunk_start, ps.chunk_bin, ps.h2, ps.tmp_cols,
           ps.tmp_stride, job.final_out, ps.col_stride);
       QFG_LAUNCHED(ctx);
     } else {
-      QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, job.fstart, ps.np1, job.fstart + ps.np1));
-      bpart_pass1_kernel<<<ps.pgrid, kPassThreads, ps.p1_smem, ctx->stream>>>(
+      QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, job.fstart, job.np1, job.fstart + job.np1));
+      bpart_pass1_kernel<<<ps.pgrid, kPassThreads, job.p1_smem, ctx->stream>>>(
           job.pa, job.fstart, job.final_out, ps.col_stride, job.vec ? 1 : 0);
       QFG_LAUNCHED(ctx);
     }
@@ -1740,11 +2163,16 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
     QFG_CUDA(ctx, cudaMemsetAsync(ps.counter, 0, 3 * sizeof(unsigned int), ctx->stream));
     plan_units_kernel<<<L.plan_grid, 256, 0, ctx->stream>>>(L.ea);
     QFG_LAUNCHED(ctx);
-    gather_entries_kernel<<<L.gather_grid, 32 * kGatherWarps, 0, ctx->stream>>>(L.ea);
-    QFG_LAUNCHED(ctx);
+    if (!L.streamed) {
+      gather_entries_kernel<<<L.gather_grid, 32 * kGatherWarps, 0, ctx->stream>>>(L.ea);
+      QFG_LAUNCHED(ctx);
+    }
     QFG_TRY(stage_end(ctx, QFG_STAGE_UNIT_PLAN));
     QFG_TRY(stage_begin(ctx, QFG_STAGE_EVALUATE));
-    eval_batched_kernel<<<L.grid, kEvalThreads, L.smem, ctx->stream>>>(L.ea);
+    if (L.streamed)
+      stream_eval_kernel<<<L.grid, kSThreads, L.smem, ctx->stream>>>(L.ea);
+    else
+      eval_batched_kernel<<<L.grid, kEvalThreads, L.smem, ctx->stream>>>(L.ea);
     QFG_LAUNCHED(ctx);
     QFG_TRY(stage_end(ctx, QFG_STAGE_EVALUATE));
   }
@@ -1767,29 +2195,39 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
   *bytes = 0;
   const int64_t nb = b->num_positive + b->num_negative;
   if (n == 0 || nb == 0) return QFG_OK;
+  const int mode = step_mode(ctx);
   StepPlan plan;
-  QFG_TRY(plan_step(ctx, n, lits, &plan));
-  const int bits = auto_group_bits(ctx, nb);
-  const bool two_pass = bits > kMaxSinglePassBits;
-  const int cb = two_pass ? coarse_bits(ctx, nb, bits) : bits;
-  const int np1 = 2 << cb;
-  int64_t words = 0;
-  int max_ncols = 1;
+  QFG_TRY(plan_step(ctx, n, lits, &plan, mode == kModeStreamed ? kSMaxSigs : 0));
+  int64_t words = 0, units = 0, entries = 0;
+  int max_ncols = 1, np1_max = 2, sbits_max = 0;
+  bool two_pass = false;
   for (auto& g : plan.groups) {
+    int64_t ge = 0;
+    for (int i : g.lits) ge += plan.tables[i]->num_entries;
+    const int bits = group_bits(ctx, mode, nb, ge);
     words += (int64_t)g.cols.size() * (nb + 4) + (2 << bits) + 1;
     max_ncols = std::max(max_ncols, (int)g.cols.size());
+    const bool two = bits > kMaxSinglePassBits;
+    const int cb = two ? coarse_bits(ctx, nb, bits) : bits;
+    np1_max = std::max(np1_max, 2 << cb);
+    if (two) {
+      two_pass = true;
+      sbits_max = std::max(sbits_max, bits - cb);
+    }
+    units += (int64_t)1 << bits;
   }
-  if (two_pass) words += (int64_t)max_ncols * (nb + 4 + 4 * np1) + 64;
-  words += (int64_t)np1 * (ctx->num_sms * 2 + 5);
-  if (two_pass) words += (nb / kP2Chunk + np1 + 1) * ((1 << (bits - cb)) + 1);
-  int64_t units = (int64_t)plan.groups.size() << bits;
-  int64_t entries = 0;
+  if (two_pass) words += (int64_t)max_ncols * (nb + 4 + 4 * np1_max) + 64;
+  words += (int64_t)np1_max * (ctx->num_sms * 2 + 5);
+  if (two_pass) words += (nb / kP2Chunk + np1_max + 1) * ((1 << sbits_max) + 1);
+  const int64_t piece = mode == kModeStreamed ? kSEntries : kChunk;
   for (KeyTable* kt : plan.tables) {
-    units += kt->num_entries / kChunk + 1;
+    units += kt->num_entries / piece + 1;
     entries += std::max<int64_t>(kt->num_entries, 1);
   }
-  words += units * (int64_t)(sizeof(WorkUnit) / 4) + 5 * (entries + 4 * units + 8);
-  *bytes = 4 * words + (int64_t)(sizeof(GroupDesc) + sizeof(LitDesc)) * n + 32 * (int64_t)n;
+  words += units * (int64_t)(sizeof(WorkUnit) / 4) +
+           (mode == kModeStreamed ? 20 : 5 * (entries + 4 * units + 8));
+  *bytes = 4 * words + (int64_t)(sizeof(GroupDesc) + sizeof(LitDesc) + sizeof(SigDesc)) * n +
+           32 * (int64_t)n;
   return QFG_OK;
 }
 
@@ -1802,7 +2240,10 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
   return enqueue_step(ctx, &ps);
 }
 
-int step_partition_bits(Ctx* ctx, int64_t nb) { return auto_group_bits(ctx, nb); }
+int step_partition_bits(Ctx* ctx, int64_t nb) {
+  // The graph cache key: the tiled path's bits, with the evaluation mode.
+  return auto_group_bits(ctx, nb) | (step_mode(ctx) << 8);
+}
 
 }  // namespace qfg
 
@@ -1896,9 +2337,9 @@ extern "C" int qfg_step_traffic(qfg_ctx* c, const qfg_bindings* b, int32_t n,
   for (int s = 0; s < QFG_NUM_STAGES; ++s) bytes[s] = 0;
   const int64_t nb = b->num_positive + b->num_negative;
   if (n == 0) return QFG_OK;
+  const int mode = step_mode(ctx);
   StepPlan plan;
-  QFG_TRY(plan_step(ctx, n, lits, &plan));
-  const int bits_for_traffic = auto_group_bits(ctx, nb);
+  QFG_TRY(plan_step(ctx, n, lits, &plan, mode == kModeStreamed ? kSMaxSigs : 0));
   // Key tables: read the projected relation columns once, write the table.
   std::map<const KeyTable*, int> seen;
   for (int i = 0; i < n; ++i) {
@@ -1911,21 +2352,29 @@ extern "C" int qfg_step_traffic(qfg_ctx* c, const qfg_bindings* b, int32_t n,
                                    4 * kt->num_entries * (kt->num_keys + 1);
   }
   for (const HostGroup& g : plan.groups) {
+    int64_t ge = 0;
+    for (int i : g.lits) ge += plan.tables[i]->num_entries;
+    const int bits = group_bits(ctx, mode, nb, ge);
     // Partition: each carried column read once and written once.
     bytes[QFG_STAGE_BIND_PARTITION] += 8 * nb * (int64_t)g.cols.size();
-    // Evaluate: partitioned columns read once, every literal's key tuples
-    // and multiplicities read once, four int64 counts written.
-    // Work units: each literal's offsets pair per partition read; entry
-    // records written once (join key, two further keys, meta, multiplicity)
-    // after the key tables' keys and multiplicities were read.
-    // Evaluation kernel: partitioned columns read once, entry records read
-    // once, four int64 counts per literal written.
+    // Evaluation: the partitioned columns read once, four int64 counts
+    // written per literal.  Work units: each literal's offsets pair per
+    // partition read.  Tiled path: entry records written once (join key, two
+    // further keys, meta, multiplicity) after the key tables' keys and
+    // multiplicities were read, and read once by the evaluation kernel.
+    // Streamed path: the evaluation kernel reads the key tables' keys and
+    // multiplicities itself.
     bytes[QFG_STAGE_EVALUATE] += 4 * nb * (int64_t)g.cols.size();
     for (int i : g.lits) {
       const int64_t ne = plan.tables[i]->num_entries;
-      bytes[QFG_STAGE_UNIT_PLAN] += 8 * ((int64_t)1 << bits_for_traffic) +
-                                    4 * ne * (plan.tables[i]->num_keys + 1) + 20 * ne;
-      bytes[QFG_STAGE_EVALUATE] += 20 * ne + 32;
+      const int64_t tab = 4 * ne * (plan.tables[i]->num_keys + 1);
+      bytes[QFG_STAGE_UNIT_PLAN] += 8 * ((int64_t)1 << bits);
+      if (mode == kModeStreamed) {
+        bytes[QFG_STAGE_EVALUATE] += tab + 32;
+      } else {
+        bytes[QFG_STAGE_UNIT_PLAN] += tab + 20 * ne;
+        bytes[QFG_STAGE_EVALUATE] += 20 * ne + 32;
+      }
     }
   }
   // The plain path partitions each distinct join column once (value +

@@ -172,6 +172,7 @@ struct Ctx {
   int64_t wait_limit = 1 << 26;
   bool withhold_copies = false;  // QFG_OPT_TEST_WITHHOLD_COPIES
   bool coverage_compat = false;  // QFG_OPT_COVERAGE_COMPAT
+  int eval_mode = 0;             // QFG_OPT_EVAL_MODE (0 automatic, 1 tiled, 2 streamed)
   int use_graphs = 0;
   // QFG_OPT_USE_GRAPHS: captured steps by key (see step_runtime.cu).
   std::map<std::string, qfg_step_graph*> graph_cache;

@@ -447,6 +447,12 @@ extern "C" int qfg_ctx_set_option(qfg_ctx* c, int option, int64_t value) {
     case QFG_OPT_COVERAGE_COMPAT:
       ctx->coverage_compat = value != 0;
       return QFG_OK;
+    case QFG_OPT_EVAL_MODE:
+      if (value < 0 || value > 2)
+        return set_error(ctx, QFG_ERR_INVALID, "evaluation mode out of range [0, 2]");
+      ctx->eval_mode = (int)value;
+      graph_cache_clear(ctx);
+      return QFG_OK;
     default:
       return set_error(ctx, QFG_ERR_INVALID, "unknown option " + std::to_string(option));
   }

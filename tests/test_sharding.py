@@ -109,3 +109,48 @@ def test_engine_shards_match_oracle_and_sum(engine):
         engine.set_option(C.QFG_OPT_SHARD_COUNT, 1)
         engine.set_option(C.QFG_OPT_EVAL_BITS, 0)
     np.testing.assert_array_equal(total, full)
+
+
+def _gpu_rank_main(rank, world, port, result_path):
+    """One rank of a 2-rank gloo world on the one GPU: its own engine
+    (context), the shared step, its shard through sharding.evaluate_sharded;
+    rank 0 keeps the summed counts.  The ranks' kernels never wait on each
+    other: the only exchange is the host-side sum of the counters."""
+    import torch
+    import torch.distributed as dist
+    from quickfoil_gb300 import Engine
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    try:
+        torch.zeros(1, device="cuda")
+        eng = Engine(0)
+        w = workloads.batched_step(n_bindings=300_000, num_relations=8, min_tuples=100,
+                                   max_tuples=80_000, num_literals=40, domain=20_000, seed=33)
+        for rid, cols in enumerate(w.relations):
+            eng.register_relation(rid, cols)
+        b = eng.bindings(w.binding_columns, w.num_positive)
+        got = sharding.evaluate_sharded(eng, b, w.literals)
+        if rank == 0:
+            np.save(result_path, got)
+        b.close()
+        eng.close()
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_two_gloo_ranks_evaluate_shards_on_the_gpu(tmp_path):
+    """sharding.evaluate_sharded on 2 gloo ranks, each a process with its own
+    engine on the one GPU: the summed counts equal the oracle's full step."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import torch.multiprocessing as mp
+    path = str(tmp_path / "gpu_counts.npy")
+    mp.start_processes(_gpu_rank_main, args=(2, _free_port(), path), nprocs=2, join=True,
+                       start_method="spawn")
+    w = workloads.batched_step(n_bindings=300_000, num_relations=8, min_tuples=100,
+                               max_tuples=80_000, num_literals=40, domain=20_000, seed=33)
+    full = oracle.evaluate(w.relations, w.binding_columns, w.num_positive,
+                           [l.as_tuple() for l in w.literals], bits=5)
+    np.testing.assert_array_equal(np.load(path), full)
