@@ -1300,30 +1300,32 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
 // ----------------------------------------------------------------------------
 // Streamed evaluation.
 //
-// Work unit = (item, piece of at most kSEntries relation entries, chunk of at
-// most row_chunk binding rows).  The CTA loads the piece's entries -- every
-// literal's distinct key tuples in the item's key range -- into a
-// shared-memory table keyed by (signature, join key, signature columns'
-// keys), chained through 32-bit links (atomicExch on the slot heads); then
-// its threads stream the unit's binding rows straight from the partitioned
-// columns (coalesced loads, no staging) and probe the table once per
-// signature of the group.  A probe that finds an entry of its signature
-// with the row's keys adds 1 to the entry's positive or negative counter.
-// After the rows, each entry adds its counters to its literal: covered +=
-// count, binding += multiplicity x count (a binding row matches at most one
-// distinct key tuple of a literal), and the counters start again at zero.
+// Work unit = (item, piece of at most kSEntries relation entries).  The CTA
+// loads the piece's entries -- every literal's distinct key tuples in the
+// item's key range -- and files each under its composite key (signature,
+// join key, the signature columns' keys) in a shared-memory key table
+// (open addressing; the first entry with a composite key claims its slot by
+// atomicCAS, later ones with the same key -- other literals -- share it).
+// Then its threads stream the item's binding rows straight from the
+// partitioned columns (coalesced loads, no staging) and look each row's
+// composite key up once per signature of the group; a hit adds 1 to the
+// slot's positive or negative row counter, so a row costs one atomic per
+// signature it matches, however many literals share that key.  Afterwards
+// every entry takes its slot's counts: covered += count, binding +=
+// multiplicity x count (a binding row matches at most one distinct key tuple
+// of a literal).
 
 constexpr int kSThreads = 512;
-constexpr int kSEntries = 2048;        // relation entries per unit
-constexpr int kSSlots = 4096;          // hash slots (twice the entries)
+constexpr int kSEntries = 1536;        // relation entries per unit
+constexpr int kSSlots = 4096;          // key-table slots (more than twice the entries)
 constexpr int kSMaxSigs = 64;          // signatures of one group
 constexpr uint32_t kSRowTarget = 32768;  // mean binding rows of an item (partition bits)
-constexpr uint32_t kSEntryTarget = kSEntries / 2;  // mean relation entries of an item
-static_assert((kSSlots & (kSSlots - 1)) == 0, "slot count is a power of two");
+constexpr uint32_t kSEntryTarget = 1024;  // mean relation entries of an item
+static_assert((kSSlots & (kSSlots - 1)) == 0 && kSSlots > 2 * kSEntries, "slot table shape");
 
 size_t stream_smem_bytes(int num_lits) {
-  return sizeof(unsigned long long) * 4 * (size_t)num_lits + sizeof(int32_t) * kSSlots +
-         sizeof(int32_t) * 9 * (size_t)kSEntries;
+  return sizeof(unsigned long long) * 4 * (size_t)num_lits + sizeof(int32_t) * 3 * kSSlots +
+         sizeof(int32_t) * 7 * (size_t)kSEntries;
 }
 
 // Hash of a composite key: the join key's mix, salted by the signature,
@@ -1344,19 +1346,28 @@ __device__ __forceinline__ int32_t pick(const int32_t (&v)[kGroupCols], int c) {
   return x;
 }
 
+// Key q >= 2 of a signature position of entry e (signatures of more than
+// two columns keep those in the key table).
+__device__ __forceinline__ int32_t sig_key_from_table(const LitDesc& d, int32_t gidx, int pos) {
+  int32_t x = 0;
+  for (int q = 1; q < d.nk; ++q)
+    if (d.spos[q] == pos) x = __ldg(d.keys + q * d.stride + gidx);
+  return x;
+}
+
 __global__ void __launch_bounds__(kSThreads, 2) stream_eval_kernel(EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem);
-  int32_t* head = reinterpret_cast<int32_t*>(acc + 4 * a.num_lits);  // kSSlots
-  int32_t* e_k0 = head + kSSlots;                                    // kSEntries each:
+  int32_t* owner = reinterpret_cast<int32_t*>(acc + 4 * a.num_lits);  // kSSlots: entry or -1
+  uint32_t* kcp = reinterpret_cast<uint32_t*>(owner + kSSlots);       // kSSlots
+  uint32_t* kcn = kcp + kSSlots;                                       // kSSlots
+  int32_t* e_k0 = reinterpret_cast<int32_t*>(kcn + kSSlots);           // kSEntries each:
   int32_t* e_s1 = e_k0 + kSEntries;
   int32_t* e_s2 = e_s1 + kSEntries;
-  uint32_t* e_meta = reinterpret_cast<uint32_t*>(e_s2 + kSEntries);  // literal | sig << 10 | valid << 31
+  uint32_t* e_meta = reinterpret_cast<uint32_t*>(e_s2 + kSEntries);    // literal | sig << 10 | valid << 31
   int32_t* e_mult = reinterpret_cast<int32_t*>(e_meta + kSEntries);
-  uint32_t* e_cp = reinterpret_cast<uint32_t*>(e_mult + kSEntries);
-  uint32_t* e_cn = e_cp + kSEntries;
-  int32_t* e_next = reinterpret_cast<int32_t*>(e_cn + kSEntries);
-  int32_t* e_gidx = e_next + kSEntries;  // key-table index (signatures of more than two columns)
+  int32_t* e_slot = e_mult + kSEntries;
+  int32_t* e_gidx = e_slot + kSEntries;  // key-table index of the entry
   __shared__ uint32_t s_lstart[kMaxGroupLits + 1];
   __shared__ uint32_t s_le0[kMaxGroupLits];
   __shared__ SigDesc s_sig[kSMaxSigs];
@@ -1365,10 +1376,10 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_eval_kernel(EvalArgs a) {
   __shared__ int s_group;  // group whose signatures s_sig holds
 
   for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) acc[i] = 0ull;
-  for (int i = threadIdx.x; i < kSSlots; i += blockDim.x) head[i] = -1;
-  for (int i = threadIdx.x; i < kSEntries; i += blockDim.x) {
-    e_cp[i] = 0u;
-    e_cn[i] = 0u;
+  for (int i = threadIdx.x; i < kSSlots; i += blockDim.x) {
+    owner[i] = -1;
+    kcp[i] = 0u;
+    kcn[i] = 0u;
   }
   if (threadIdx.x == 0) {
     s_count = umin(a.unit_count[0], a.unit_cap);
@@ -1418,7 +1429,7 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_eval_kernel(EvalArgs a) {
     }
     __syncthreads();
     if (threadIdx.x == 0) s_group = (int)U.group;
-    // The unit's entries into the table.
+    // The unit's entries into the key table.
     for (uint32_t j = threadIdx.x; j < U.ecnt; j += blockDim.x) {
       const uint32_t f = U.f0 + j;
       int lo = 0, hi = m - 1;  // largest L with s_lstart[L] <= f
@@ -1430,7 +1441,7 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_eval_kernel(EvalArgs a) {
       const uint32_t e = s_le0[lo] + (f - s_lstart[lo]);
       const int32_t k0 = __ldg(d.keys + e);
       const int sg = d.sig - G.sig_begin;
-      const SigDesc& S = s_sig[sg];
+      const int sn = s_sig[sg].ncols;
       int32_t sk[kGroupCols - 1];
 #pragma unroll
       for (int i = 0; i < kGroupCols - 1; ++i) sk[i] = 0;
@@ -1440,12 +1451,12 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_eval_kernel(EvalArgs a) {
         const int32_t kq = __ldg(d.keys + q * d.stride + e);
         const int pq = d.spos[q];
         if (pq < 0) {
-          valid &= kq == k0;
+          valid &= kq == k0;  // compared with the join column itself
         } else {
 #pragma unroll
           for (int i = 0; i < kGroupCols - 1; ++i) {
             if (i != pq) continue;
-            if (filled & (1u << i)) valid &= sk[i] == kq;
+            if (filled & (1u << i)) valid &= sk[i] == kq;  // two arguments, one variable
             sk[i] = kq;
           }
           filled |= 1u << pq;
@@ -1454,17 +1465,43 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_eval_kernel(EvalArgs a) {
       uint32_t h = skey_start(mix32((uint32_t)k0), sg);
 #pragma unroll
       for (int i = 0; i < kGroupCols - 1; ++i)
-        if (i < S.ncols) h = skey_fold(h, sk[i]);
+        if (i < sn) h = skey_fold(h, sk[i]);
       e_k0[j] = k0;
       e_s1[j] = sk[0];
       e_s2[j] = sk[1];
       e_mult[j] = __ldg(d.mult + e);
       e_gidx[j] = (int32_t)e;
       e_meta[j] = (uint32_t)lo | ((uint32_t)sg << 10) | (valid ? 0x80000000u : 0u);
-      e_next[j] = valid ? atomicExch(&head[skey_slot(h)], (int32_t)j) : -1;
+      int32_t slot = -1;
+      if (valid) {
+        // The entry's keys are visible to the block before it may own a slot.
+        __threadfence_block();
+        uint32_t sl = skey_slot(h);
+        for (int probe = 0; probe < kSSlots; ++probe) {
+          const int32_t o = atomicCAS(&owner[sl], -1, (int32_t)j);
+          if (o < 0) {
+            slot = (int32_t)sl;
+            break;
+          }
+          const uint32_t om = e_meta[o];
+          bool same = (int)((om >> 10) & 0x3ffu) == sg && e_k0[o] == k0 && e_s1[o] == sk[0] &&
+                      e_s2[o] == sk[1];
+          if (same && sn > 2) {
+            const LitDesc& od = a.lits[G.lit_begin + (om & 0x3ffu)];
+            for (int i = 2; i < sn && same; ++i)
+              same = sig_key_from_table(od, e_gidx[o], i) == sig_key_from_table(d, (int32_t)e, i);
+          }
+          if (same) {
+            slot = (int32_t)sl;
+            break;
+          }
+          sl = (sl + 1) & (kSSlots - 1);
+        }
+      }
+      e_slot[j] = slot;
     }
     __syncthreads();
-    // The unit's binding rows, positives then negatives, against the table.
+    // The item's binding rows, positives then negatives, against the table.
     {
       const int ncols = G.ncols;
       const int64_t stride = G.n;
@@ -1475,51 +1512,54 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_eval_kernel(EvalArgs a) {
         int32_t v[kGroupCols];
 #pragma unroll
         for (int q = 0; q < kGroupCols; ++q) v[q] = q < ncols ? __ldg(G.cols + q * stride + row) : 0;
-        uint32_t* cnt = pos ? e_cp : e_cn;
+        uint32_t* cnt = pos ? kcp : kcn;
         const uint32_t hk = mix32((uint32_t)v[0]);
         for (int sg = 0; sg < nsig; ++sg) {
           const SigDesc& S = s_sig[sg];
           uint32_t h = skey_start(hk, sg);
           for (int i = 0; i < S.ncols; ++i) h = skey_fold(h, pick(v, S.col[i]));
-          for (int e = head[skey_slot(h)]; e >= 0; e = e_next[e]) {
-            if ((int)((e_meta[e] >> 10) & 0x3ffu) != sg || e_k0[e] != v[0]) continue;
-            if (S.ncols >= 1 && e_s1[e] != pick(v, S.col[0])) continue;
-            if (S.ncols >= 2 && e_s2[e] != pick(v, S.col[1])) continue;
-            if (S.ncols > 2) {
-              // Further signature columns from the key table.
-              const LitDesc& d = a.lits[G.lit_begin + (e_meta[e] & 0x3ffu)];
+          uint32_t sl = skey_slot(h);
+          for (int probe = 0; probe < kSSlots; ++probe) {
+            const int32_t o = owner[sl];
+            if (o < 0) break;
+            const uint32_t om = e_meta[o];
+            if ((int)((om >> 10) & 0x3ffu) == sg && e_k0[o] == v[0] &&
+                (S.ncols < 1 || e_s1[o] == pick(v, S.col[0])) &&
+                (S.ncols < 2 || e_s2[o] == pick(v, S.col[1]))) {
               bool ok = true;
-              for (int q = 1; q < d.nk && ok; ++q) {
-                const int pq = d.spos[q];
-                if (pq >= 2) ok = __ldg(d.keys + q * d.stride + e_gidx[e]) == pick(v, S.col[pq]);
+              if (S.ncols > 2) {
+                const LitDesc& d = a.lits[G.lit_begin + (om & 0x3ffu)];
+                for (int i = 2; i < S.ncols && ok; ++i)
+                  ok = sig_key_from_table(d, e_gidx[o], i) == pick(v, S.col[i]);
               }
-              if (!ok) continue;
+              if (ok) {
+                atomicAdd(&cnt[sl], 1u);
+                break;
+              }
             }
-            atomicAdd(&cnt[e], 1u);
+            sl = (sl + 1) & (kSSlots - 1);
           }
         }
       }
     }
     if (threadIdx.x == 0 && nidx < s_count) s_unit = a.units[nidx];
     __syncthreads();
-    // Entry counters into the literals' sums; entries are literal-major, so
+    // Entry counts into the literals' sums; entries are literal-major, so
     // equal literals sit on consecutive lanes (segmented warp scans).
     for (uint32_t j0 = 0; j0 < U.ecnt; j0 += blockDim.x) {
       const uint32_t j = j0 + threadIdx.x;
       int L = -1;
       long long cp = 0, cn = 0, bp = 0, bn = 0;
       if (j < U.ecnt) {
-        const uint32_t meta = e_meta[j];
-        L = (int)(meta & 0x3ffu);
-        const uint32_t p = e_cp[j], q = e_cn[j];
-        if (p | q) {
+        L = (int)(e_meta[j] & 0x3ffu);
+        const int32_t sl = e_slot[j];
+        if (sl >= 0) {
+          const uint32_t p = kcp[sl], q = kcn[sl];
           const long long mlt = e_mult[j];
           cp = p;
           cn = q;
           bp = mlt * p;
           bn = mlt * q;
-          e_cp[j] = 0u;
-          e_cn[j] = 0u;
         }
       }
       cp = seg_scan(cp, L);
@@ -1530,8 +1570,16 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_eval_kernel(EvalArgs a) {
       if ((lane == 31 || next_L != L) && L >= 0 && (cp | cn | bp | bn) != 0)
         flush_acc(acc + 4 * (G.lit_begin + L), cp, cn, bp, bn);
     }
-    // Every slot head back to empty (a few stores a thread).
-    for (int i = threadIdx.x; i < kSSlots; i += blockDim.x) head[i] = -1;
+    __syncthreads();
+    // The slots this unit used back to empty.
+    for (uint32_t j = threadIdx.x; j < U.ecnt; j += blockDim.x) {
+      const int32_t sl = e_slot[j];
+      if (sl >= 0) {
+        owner[sl] = -1;
+        kcp[sl] = 0u;
+        kcn[sl] = 0u;
+      }
+    }
     if (threadIdx.x == 0) s_idx = nidx;
     __syncthreads();
   }
