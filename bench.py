@@ -308,7 +308,7 @@ def run_gb300(args):
     if not args.eval_bits:
         bits, cbits, tms = eng.autotune_step(b, w.literals)
         eng.set_option(C.QFG_OPT_AUTOTUNE, 1)
-        tune = {"partition_bits": bits, "pass1_bits": cbits, "ms_per_step": tms}
+        tune = dict(eng.autotune_choice(w.num_bindings), ms_per_step=tms)
 
     for _ in range(args.warmup):
         eng.evaluate_step_device(b, lits_c, n, counts.data_ptr())

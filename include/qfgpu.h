@@ -78,7 +78,7 @@ enum {
                                    memory, relation entries probing them), 2 = streamed
                                    (relation entries in shared memory, binding rows streamed
                                    past them), 0 (default) = automatic (the autotuner's choice
-                                   for the size class, else streamed) */
+                                   for the size class, else tiled) */
 };
 
 /* Evaluation stages timed under QFG_OPT_STAGE_TIMING (the GPU counterpart of
@@ -215,18 +215,29 @@ int qfg_step_scratch_bytes(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t n
                            const qfg_literal* literals, int64_t* bytes);
 
 /* Autotuner.  No reference counterpart (the reference reads FLAGS_num_radix_bits).
- * Times the batched step over `bindings` at a few partition-bit settings
- * around the automatic choice -- the bits fix the partition pass count (one
- * pass up to 8 bits, two above) and the rows per shared-memory table -- and,
- * with two passes, both splits of the bits between the passes (7 or 8
- * pass-1 bits); records the fastest for the binding set's size class
- * (floor(log2(rows))).  Under QFG_OPT_AUTOTUNE = 1 every batched step of that
- * size class uses the recorded setting (QFG_OPT_EVAL_BITS > 0 still
- * overrides).  Counts do not depend on it.  Returns the chosen partition
- * bits, pass-1 bits (0 = one pass) and time per step. */
+ * Times the batched step over `bindings` in both evaluation modes (see
+ * QFG_OPT_EVAL_MODE): the tiled path at a few partition-bit settings around
+ * its automatic choice -- the bits fix the partition pass count (one pass up
+ * to 8 bits, two above) and the rows per shared-memory tile -- with both
+ * splits of the bits between two passes (7 or 8 pass-1 bits), and the
+ * streamed path with its per-group partition bits (chosen from each
+ * literal group's relation entries, so that a partition's entries fit the
+ * shared-memory table) offset by -1 .. +2; records the fastest for the
+ * binding set's size class (floor(log2(rows))).  Under QFG_OPT_AUTOTUNE = 1
+ * every batched step of that size class uses the recorded setting
+ * (QFG_OPT_EVAL_MODE and QFG_OPT_EVAL_BITS still override).  Counts do not
+ * depend on it.  best_bits / best_pass1_bits receive the tiled path's
+ * partition and pass-1 bits (0 = one pass), or 0 and the bits offset when
+ * the streamed path won; best_ms the time per step.  qfg_autotune_choice
+ * reads the recorded setting of a size class back. */
 int qfg_autotune_step(qfg_ctx* ctx, const qfg_bindings* bindings, int32_t num_literals,
                       const qfg_literal* literals, int32_t* best_bits, int32_t* best_pass1_bits,
                       double* best_ms);
+/* The autotuner's setting for binding sets of num_rows rows: *mode (1 tiled,
+ * 2 streamed, 0 = none recorded), *bits and *pass1_bits (tiled), *bias
+ * (streamed: offset of the per-group partition bits). */
+int qfg_autotune_choice(const qfg_ctx* ctx, int64_t num_rows, int32_t* mode, int32_t* bits,
+                        int32_t* pass1_bits, int32_t* bias);
 
 /* ---- batched steps replayed from CUDA graphs ---------------------------- */
 /* No reference counterpart.  Captures the batched evaluation of `literals`

@@ -105,6 +105,9 @@ SIGNATURES = [
     ("qfg_autotune_step", ctypes.c_int,
      [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i32p, c_i32p,
       ctypes.POINTER(ctypes.c_double)]),
+    ("qfg_autotune_choice", ctypes.c_int,
+     [c_vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+      ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     ("qfg_step_scratch_bytes", ctypes.c_int,
      [c_vp, c_vp, ctypes.c_int32, ctypes.POINTER(QfgLiteral), c_i64p]),
     ("qfg_step_graph_create", ctypes.c_int,

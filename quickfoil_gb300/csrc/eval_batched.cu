@@ -183,6 +183,9 @@ struct BPartArgs {
   int cbits;                // pass-1 bits (== bits: single pass)
   uint32_t* p1_tot;         // 2 << cbits bin totals (zeroed)
   uint32_t* p1_base;        // gridDim.x * (2 << cbits) per-CTA bases
+  // Rows whose top cbits hash bits fall outside [keep_lo, keep_hi] belong to
+  // other shards' partitions and are dropped in pass 1 (QFG_OPT_SHARD_*).
+  uint32_t keep_lo, keep_hi;
 };
 
 // Rows [r0, r1) of this CTA; r0 is a multiple of 4 so that 16-byte loads
@@ -212,7 +215,8 @@ __global__ void __launch_bounds__(kPartThreads, 1) bpart_hist_kernel(BPartArgs a
   cta_range4(a.n, &r0, &r1);
   const int32_t* __restrict__ key = a.cols[0];
   auto count = [&](int32_t k, int64_t r) {
-    atomicAdd(&p1[(top_bits(k, a.cbits) << 1) | (r >= a.npos ? 1u : 0u)], 1u);
+    const uint32_t t = top_bits(k, a.cbits);
+    if (t >= a.keep_lo && t <= a.keep_hi) atomicAdd(&p1[(t << 1) | (r >= a.npos ? 1u : 0u)], 1u);
   };
   int64_t rs = r0;
   if (kVec) {
@@ -261,17 +265,19 @@ constexpr int kPassRows = 16384;                              // rows per round
 constexpr int kPassRowsPerThread = kPassRows / kPassThreads;  // 16
 constexpr int kPassPieces = kPassRows / (4 * kPassThreads);   // 4-row copy pieces per thread
 static_assert(kPassRows <= 65536, "a round's row index packs into 16 bits");
-static_assert((2 << kMaxCoarseBits) <= kPassThreads && (1 << kMaxSubBits) <= kPassThreads,
-              "one thread per bin in the round scan");
+static_assert((2 << kMaxCoarseBits) < kPassThreads && (1 << kMaxSubBits) < kPassThreads,
+              "one thread per bin (and the drop bin) in the round scan");
 
+// Bin arrays hold nbins + 1 entries: bin nbins collects the rows a shard
+// drops; it sorts last, so a round writes only its first sorted positions.
 struct PassSmem {
   int32_t* buf0;      // kPassRows: one column of a round
   int32_t* buf1;      // kPassRows: the column after it
   uint32_t* perm;     // kPassRows: row | bin << 16 at each sorted position
-  uint32_t* lcount;   // nbins
-  uint32_t* lstart;   // nbins
-  uint32_t* gpos;     // nbins: output position of sorted position 0 of bin b
-  uint32_t* cursor;   // nbins: output cursor of each bin (pass 1)
+  uint32_t* lcount;   // nbins + 1
+  uint32_t* lstart;   // nbins + 1
+  uint32_t* gpos;     // nbins + 1: output position of sorted position 0 of bin b
+  uint32_t* cursor;   // nbins + 1: output cursor of each bin (pass 1)
 };
 
 __device__ __forceinline__ PassSmem carve_pass(unsigned char* smem, int nbins) {
@@ -280,14 +286,14 @@ __device__ __forceinline__ PassSmem carve_pass(unsigned char* smem, int nbins) {
   S.buf1 = S.buf0 + kPassRows;
   S.perm = reinterpret_cast<uint32_t*>(S.buf1 + kPassRows);
   S.lcount = S.perm + kPassRows;
-  S.lstart = S.lcount + nbins;
-  S.gpos = S.lstart + nbins;
-  S.cursor = S.gpos + nbins;
+  S.lstart = S.lcount + nbins + 1;
+  S.gpos = S.lstart + nbins + 1;
+  S.cursor = S.gpos + nbins + 1;
   return S;
 }
 
 size_t pass_smem_bytes(int nbins) {
-  return sizeof(uint32_t) * (3 * (size_t)kPassRows + 4 * (size_t)nbins);
+  return sizeof(uint32_t) * (3 * (size_t)kPassRows + 4 * ((size_t)nbins + 1));
 }
 
 __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
@@ -384,11 +390,13 @@ __device__ __forceinline__ void stream_pass(const PassSmem& S, const int32_t* co
           }
         }
         __syncthreads();
-        const uint32_t c = t < nbins ? S.lcount[t] : 0u;
+        const uint32_t c = t <= nbins ? S.lcount[t] : 0u;
         const uint32_t ex = block_scan_excl(c, s_warp, s_total);
-        if (t < nbins) {
+        if (t <= nbins) {
           S.lstart[t] = ex;
-          if (h2 != nullptr) {
+          if (t == nbins) {
+            S.gpos[t] = 0u;  // dropped rows: never written
+          } else if (h2 != nullptr) {
             S.gpos[t] = hb - ex;
           } else {
             S.gpos[t] = S.cursor[t] - ex;
@@ -418,10 +426,11 @@ __device__ __forceinline__ void stream_pass(const PassSmem& S, const int32_t* co
         }
       }
       int32_t* __restrict__ out = dst[q];
+      const int nkeep = (int)S.lstart[nbins];  // sorted positions before the drop bin
 #pragma unroll
       for (int j = 0; j < J; ++j) {
         const int kk = t + j * T;
-        if (kk < nt) out[oidx[j]] = cbuf[(rowp[j >> 1] >> (16 * (j & 1))) & 0xffffu];
+        if (kk < nkeep) out[oidx[j]] = cbuf[(rowp[j >> 1] >> (16 * (j & 1))) & 0xffffu];
       }
       slot = !slot;
     }
@@ -442,8 +451,8 @@ bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* 
   __shared__ int32_t* s_dst[kGroupCols];
   const int np1 = 2 << a.cbits;
   const PassSmem S = carve_pass(smem, np1);
-  for (int i = threadIdx.x; i < np1; i += blockDim.x) {
-    S.cursor[i] = p1_start[i] + a.p1_base[(int64_t)blockIdx.x * np1 + i];
+  for (int i = threadIdx.x; i <= np1; i += blockDim.x) {
+    S.cursor[i] = i < np1 ? p1_start[i] + a.p1_base[(int64_t)blockIdx.x * np1 + i] : 0u;
     S.lcount[i] = 0u;
   }
   if (threadIdx.x == 0) {
@@ -461,6 +470,7 @@ bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* 
   const uint32_t r0 = (uint32_t)r0l, r1 = (uint32_t)r1l;
   const int cbits = a.cbits;
   const uint32_t npos = (uint32_t)a.npos;
+  const uint32_t keep_lo = a.keep_lo, keep_hi = a.keep_hi;
   PassRound first;
   first.rr = r0;
   first.re = r0 < r1 ? round_end(r0, r0, r1, npos, kPassRows) : r0;
@@ -476,7 +486,10 @@ bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* 
         n.chunk = 0;
         return n;
       },
-      [=](int32_t key, uint32_t r) { return (top_bits(key, cbits) << 1) | (r >= npos ? 1u : 0u); });
+      [=](int32_t key, uint32_t r) {
+        const uint32_t tb = top_bits(key, cbits);
+        return (tb >= keep_lo && tb <= keep_hi) ? (tb << 1) | (r >= npos ? 1u : 0u) : (uint32_t)np1;
+      });
 }
 
 // Rows of a pass-2 work chunk: coarse bins (up to 9x apart in size, since
@@ -617,7 +630,7 @@ bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ pad, const uint32_t
   const PassSmem S = carve_pass(smem, nsub);
   const uint32_t mask = (uint32_t)(nsub - 1);
   const int bits = a.bits;
-  for (int i = threadIdx.x; i < nsub; i += blockDim.x) S.lcount[i] = 0u;
+  for (int i = threadIdx.x; i <= nsub; i += blockDim.x) S.lcount[i] = 0u;
   if (threadIdx.x == 0) {
     for (int q = 0; q < a.ncols; ++q) {
       s_src[q] = in + (int64_t)q * in_stride;
@@ -1819,7 +1832,29 @@ struct PreparedStep {
 constexpr int kModeTiled = 1;
 constexpr int kModeStreamed = 2;
 
-int step_mode(Ctx* ctx) { return ctx->eval_mode == kModeTiled ? kModeTiled : kModeStreamed; }
+// The evaluation mode of a batched step over nb binding rows: the option,
+// else the autotuner's choice for the size class, else tiled (measured on
+// the 32M x 6, 256-literal step: evaluation 4.1 ms tiled (+0.8 ms unit
+// planning and entry gather) against 7.9 ms streamed (+0.05 ms)).
+int step_mode(Ctx* ctx, int64_t nb) {
+  if (ctx->eval_mode == kModeTiled || ctx->eval_mode == kModeStreamed) return ctx->eval_mode;
+  if (ctx->autotune) {
+    auto it = ctx->tuned_mode.find(size_class(nb));
+    if (it != ctx->tuned_mode.end()) return it->second.first;
+  }
+  return kModeTiled;
+}
+
+// Offset of the streamed path's partition bits: a tuning trial's, else the
+// autotuner's choice for the size class, else 0.
+int stream_bias(Ctx* ctx, int64_t nb) {
+  if (ctx->stream_bias != 0) return ctx->stream_bias;
+  if (ctx->autotune) {
+    auto it = ctx->tuned_mode.find(size_class(nb));
+    if (it != ctx->tuned_mode.end() && it->second.first == kModeStreamed) return it->second.second;
+  }
+  return 0;
+}
 
 // Partition bits of one literal group.  Tiled: from the binding-set size
 // (rows per shared-memory tile).  Streamed: enough partitions that the mean
@@ -1832,7 +1867,7 @@ int group_bits(Ctx* ctx, int mode, int64_t nb, int64_t entries) {
   while (bits < kMaxPartitionBits &&
          ((entries >> bits) > (int64_t)kSEntryTarget || (nb >> bits) > (int64_t)kSRowTarget))
     ++bits;
-  return bits;
+  return std::max(1, std::min(kMaxPartitionBits, bits + stream_bias(ctx, nb)));
 }
 
 // The key signatures of a group (streamed path) and, per literal, its
@@ -1877,7 +1912,7 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   ps->launches.clear();
   ps->blob.clear();
   if (n == 0 || nb == 0) return QFG_OK;
-  const int mode = step_mode(ctx);
+  const int mode = step_mode(ctx, nb);
   ps->mode = mode;
 
   QFG_TRY(stage_begin(ctx, QFG_STAGE_KEY_TABLES));
@@ -1968,6 +2003,11 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     pa.cbits = cbits;
     pa.p1_tot = ps->p1_tot;
     pa.p1_base = ps->p1_base;
+    // The shard's partitions [shard_lo, shard_hi) cover these pass-1 hash
+    // ranges; rows of other ranges are dropped before their columns move.
+    pa.keep_lo = shard_lo >> job.sbits;
+    pa.keep_hi = shard_hi > shard_lo ? (shard_hi - 1) >> job.sbits : 0u;
+    if (shard_hi <= shard_lo) pa.keep_lo = 1u;  // an empty shard keeps nothing
     job.final_out = part_base + off;
     job.fstart = fstarts + fs_off;
     job.vec = true;
@@ -2243,7 +2283,7 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
   *bytes = 0;
   const int64_t nb = b->num_positive + b->num_negative;
   if (n == 0 || nb == 0) return QFG_OK;
-  const int mode = step_mode(ctx);
+  const int mode = step_mode(ctx, nb);
   StepPlan plan;
   QFG_TRY(plan_step(ctx, n, lits, &plan, mode == kModeStreamed ? kSMaxSigs : 0));
   int64_t words = 0, units = 0, entries = 0;
@@ -2289,8 +2329,9 @@ int evaluate_batched(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_liter
 }
 
 int step_partition_bits(Ctx* ctx, int64_t nb) {
-  // The graph cache key: the tiled path's bits, with the evaluation mode.
-  return auto_group_bits(ctx, nb) | (step_mode(ctx) << 8);
+  // The graph cache key: the tiled path's bits, the evaluation mode and the
+  // streamed path's bits offset.
+  return auto_group_bits(ctx, nb) | (step_mode(ctx, nb) << 8) | ((stream_bias(ctx, nb) + 16) << 12);
 }
 
 }  // namespace qfg
@@ -2318,62 +2359,97 @@ extern "C" int qfg_autotune_step(qfg_ctx* c, const qfg_bindings* b, int32_t n,
   Ctx* ctx = &c->impl;
   QFG_TRY(validate_literals(ctx, b, n, lits));
   const int64_t nb = b->num_positive + b->num_negative;
-  const int saved_bits = ctx->eval_bits, saved_cbits = ctx->eval_cbits;
+  const int saved_bits = ctx->eval_bits, saved_cbits = ctx->eval_cbits, saved_mode = ctx->eval_mode;
   const bool saved_tune = ctx->autotune, saved_timing = ctx->stage_timing;
   ctx->eval_bits = 0;
   ctx->autotune = false;
   const int base = auto_group_bits(ctx, nb);
+  // Trials: the tiled path at partition bits around its automatic choice,
+  // with both splits of the bits between two passes; the streamed path with
+  // its per-group bits offset by -1 .. +2.
+  struct Trial {
+    int mode, bits, cbits, bias;
+  };
+  std::vector<Trial> trials;
+  for (int cand = std::max(1, base - 2); cand <= std::min(kMaxPartitionBits, base + 1); ++cand) {
+    const int cb_lo = cand > kMaxSinglePassBits ? kDefaultCoarseBits : 0;
+    const int cb_hi = cand > kMaxSinglePassBits ? kMaxCoarseBits : 0;
+    for (int cb = cb_lo; cb <= cb_hi; ++cb)
+      if (cb == 0 || cand - cb <= kMaxSubBits) trials.push_back({kModeTiled, cand, cb, 0});
+  }
+  for (int bias = -1; bias <= 2; ++bias) trials.push_back({kModeStreamed, 0, 0, bias});
   QFG_TRY(ctx->scratch[kScrCounts].reserve(ctx, sizeof(int64_t) * 4 * (size_t)std::max(n, 1)));
   unsigned long long* dev = ctx->scratch[kScrCounts].as<unsigned long long>();
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int st = QFG_OK;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     st = cuda_error(ctx, cudaGetLastError(), "cudaEventCreate");
-  int best = base, best_cb = 0;
+  Trial best{kModeTiled, base, 0, 0};
   float best_t = -1.0f;
   ctx->stage_timing = false;
-  for (int cand = std::max(1, base - 2); st == QFG_OK && cand <= std::min(kMaxPartitionBits, base + 1);
-       ++cand) {
-    // Two passes: try both pass-1 widths (how the bits split between passes).
-    const int cb_lo = cand > kMaxSinglePassBits ? kDefaultCoarseBits : 0;
-    const int cb_hi = cand > kMaxSinglePassBits ? kMaxCoarseBits : 0;
-    for (int cb = cb_lo; st == QFG_OK && cb <= cb_hi; ++cb) {
-      if (cb > 0 && cand - cb > kMaxSubBits) continue;
-      ctx->eval_bits = cand;
-      ctx->eval_cbits = cb;
-      st = evaluate_batched(ctx, b, n, lits, dev);  // sizes the scratch of this setting
-      if (st != QFG_OK) break;
-      if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) {
-        st = cuda_error(ctx, cudaGetLastError(), "cudaEventRecord");
-        break;
-      }
-      for (int rep = 0; rep < 2 && st == QFG_OK; ++rep) st = evaluate_batched(ctx, b, n, lits, dev);
-      if (st != QFG_OK) break;
-      float ms = 0.0f;
-      if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
-        st = cuda_error(ctx, cudaGetLastError(), "timing");
-        break;
-      }
-      ms *= 0.5f;
-      if (best_t < 0.0f || ms < best_t) {
-        best_t = ms;
-        best = cand;
-        best_cb = cb;
-      }
+  for (const Trial& t : trials) {
+    if (st != QFG_OK) break;
+    ctx->eval_mode = t.mode;
+    ctx->eval_bits = t.bits;
+    ctx->eval_cbits = t.cbits;
+    ctx->stream_bias = t.bias;
+    st = evaluate_batched(ctx, b, n, lits, dev);  // sizes the scratch of this setting
+    if (st != QFG_OK) break;
+    if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) {
+      st = cuda_error(ctx, cudaGetLastError(), "cudaEventRecord");
+      break;
+    }
+    for (int rep = 0; rep < 2 && st == QFG_OK; ++rep) st = evaluate_batched(ctx, b, n, lits, dev);
+    if (st != QFG_OK) break;
+    float ms = 0.0f;
+    if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      st = cuda_error(ctx, cudaGetLastError(), "timing");
+      break;
+    }
+    ms *= 0.5f;
+    if (best_t < 0.0f || ms < best_t) {
+      best_t = ms;
+      best = t;
     }
   }
   ctx->eval_cbits = saved_cbits;
+  ctx->eval_mode = saved_mode;
+  ctx->stream_bias = 0;
   if (e0 != nullptr) cudaEventDestroy(e0);
   if (e1 != nullptr) cudaEventDestroy(e1);
   ctx->eval_bits = saved_bits;
   ctx->autotune = saved_tune;
   ctx->stage_timing = saved_timing;
   if (st != QFG_OK) return st;
-  ctx->tuned_bits[size_class(nb)] = std::make_pair(best, best_cb);
-  if (best_bits != nullptr) *best_bits = best;
-  if (best_pass1_bits != nullptr) *best_pass1_bits = best_cb;
+  if (best.mode == kModeTiled) ctx->tuned_bits[size_class(nb)] = std::make_pair(best.bits, best.cbits);
+  ctx->tuned_mode[size_class(nb)] = std::make_pair(best.mode, best.bias);
+  graph_cache_clear(ctx);
+  if (best_bits != nullptr) *best_bits = best.mode == kModeTiled ? best.bits : 0;
+  if (best_pass1_bits != nullptr) *best_pass1_bits = best.mode == kModeTiled ? best.cbits : best.bias;
   if (best_ms != nullptr) *best_ms = best_t;
+  return QFG_OK;
+}
+
+extern "C" int qfg_autotune_choice(const qfg_ctx* c, int64_t num_rows, int32_t* mode, int32_t* bits,
+                                   int32_t* pass1_bits, int32_t* bias) {
+  if (c == nullptr || mode == nullptr || bits == nullptr || pass1_bits == nullptr || bias == nullptr)
+    return QFG_ERR_INVALID;
+  const Ctx* ctx = &c->impl;
+  const int cls = size_class(num_rows);
+  *mode = *bits = *pass1_bits = *bias = 0;
+  auto m = ctx->tuned_mode.find(cls);
+  if (m == ctx->tuned_mode.end()) return QFG_OK;
+  *mode = m->second.first;
+  if (*mode == kModeStreamed) {
+    *bias = m->second.second;
+  } else {
+    auto t = ctx->tuned_bits.find(cls);
+    if (t != ctx->tuned_bits.end()) {
+      *bits = t->second.first;
+      *pass1_bits = t->second.second;
+    }
+  }
   return QFG_OK;
 }
 
@@ -2385,7 +2461,7 @@ extern "C" int qfg_step_traffic(qfg_ctx* c, const qfg_bindings* b, int32_t n,
   for (int s = 0; s < QFG_NUM_STAGES; ++s) bytes[s] = 0;
   const int64_t nb = b->num_positive + b->num_negative;
   if (n == 0) return QFG_OK;
-  const int mode = step_mode(ctx);
+  const int mode = step_mode(ctx, nb);
   StepPlan plan;
   QFG_TRY(plan_step(ctx, n, lits, &plan, mode == kModeStreamed ? kSMaxSigs : 0));
   // Key tables: read the projected relation columns once, write the table.

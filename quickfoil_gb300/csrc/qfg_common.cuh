@@ -173,6 +173,10 @@ struct Ctx {
   bool withhold_copies = false;  // QFG_OPT_TEST_WITHHOLD_COPIES
   bool coverage_compat = false;  // QFG_OPT_COVERAGE_COMPAT
   int eval_mode = 0;             // QFG_OPT_EVAL_MODE (0 automatic, 1 tiled, 2 streamed)
+  // Autotuner's evaluation mode and streamed-path bits offset per
+  // binding-size class; stream_bias is the offset a tuning trial uses.
+  std::map<int, std::pair<int, int>> tuned_mode;
+  int stream_bias = 0;
   int use_graphs = 0;
   // QFG_OPT_USE_GRAPHS: captured steps by key (see step_runtime.cu).
   std::map<std::string, qfg_step_graph*> graph_cache;

@@ -312,6 +312,15 @@ class Engine:
                 self.ctx, "qfg_autotune_step")
         return bits.value, cbits.value, ms.value
 
+    def autotune_choice(self, num_rows: int):
+        """The autotuner's setting for binding sets of num_rows rows:
+        {"mode": "tiled" | "streamed" | None, "bits", "pass1_bits", "bias"}."""
+        v = [ctypes.c_int32() for _ in range(4)]
+        C.check(self.lib.qfg_autotune_choice(self.ctx, num_rows, *[ctypes.byref(x) for x in v]),
+                self.ctx, "qfg_autotune_choice")
+        mode = {1: "tiled", 2: "streamed"}.get(v[0].value)
+        return {"mode": mode, "bits": v[1].value, "pass1_bits": v[2].value, "bias": v[3].value}
+
     def step_scratch_bytes(self, bindings: BindingSet, literals: Sequence[Literal]) -> int:
         """Device scratch a batched step of these literals needs."""
         lits = (C.QfgLiteral * max(1, len(literals)))(*[l.to_c() for l in literals])

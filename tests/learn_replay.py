@@ -251,5 +251,5 @@ class _DeviceColumn:
     __cuda_array_interface__, so torch can wrap it without a copy."""
 
     def __init__(self, ptr: int, n: int):
-        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (ptr, True),
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (ptr, False),
                                          "version": 3, "strides": None}
