@@ -69,6 +69,8 @@ def parse_args():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop leg")
     ap.add_argument("--no-coverage", action="store_true",
                     help="skip the coverage, test-runner and loader legs")
+    ap.add_argument("--no-learn", action="store_true",
+                    help="skip the full-scale learn-loop (config 4) leg")
     return ap.parse_args()
 
 
@@ -456,6 +458,9 @@ def run_gb300(args):
         coverage = run_coverage(eng, w, b, dev, torch, measured_peak_hbm()[0], args.no_cpu)
         testrun = run_test_runner(eng, w, dev, torch, args.no_cpu)
         loader = run_loader(eng, dev, torch, measured_peak_hbm()[0], args.no_cpu)
+    learn = None
+    if args.workload == "batched_step" and not args.no_learn and rank == 0:
+        learn = run_learn_loop(torch)
 
     if rank == 0:
         peak, peak_kind = measured_peak_hbm()
@@ -509,6 +514,8 @@ def run_gb300(args):
             line["serving"] = serving
         if radix is not None:
             line["radix_partition"] = radix
+        if learn is not None:
+            line["learn_loop"] = learn
         if coverage is not None:
             line["coverage"] = coverage
         if testrun is not None:
@@ -563,6 +570,38 @@ def run_radix_partition(eng, values, stream, torch, peak, bits: int = 15, reps: 
     return {"kernel": "qfg_radix_partition (two stable 7/8-bit passes)", "rows": n, "bits": bits,
             "ms": ms, "algorithmic_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9,
             "frac": alg / (ms * 1e-3) / 1e9 / peak, "peak": peak, "stable_partition": ok}
+
+
+def run_learn_loop(torch):
+    """BASELINE config 4 at full scale (1M pictures): the reference learner's
+    recorded run replayed call by call on the device (tests/learn_replay.py,
+    every result checked against the reference's), in a fresh engine.  GPU
+    seconds of the replayed calls (each timed with a device synchronize on
+    both sides) beside the reference's own seconds inside the same calls and
+    in Learn as a whole (one x86 core, recorded when the trace was made)."""
+    from quickfoil_gb300 import Engine
+    from tests import learn_replay
+    # A warm-up replay in a first engine loads the kernels; the timed replay
+    # runs in a fresh engine, so its relation key tables are built on first
+    # use inside the calls, as in a learn run.
+    for _ in range(2):
+        eng = Engine(torch.cuda.current_device())
+        try:
+            t0 = time.perf_counter()
+            out = learn_replay.replay(eng, torch)
+            wall = time.perf_counter() - t0
+        finally:
+            eng.close()
+    ref = out["reference_seconds"]
+    ref_calls = ref["evaluate"] + ref["extend"] + ref["coverage"]
+    return {"metric": "full-scale learn loop (config 4): seconds in the data-parallel calls",
+            "gpu_seconds": out["gpu_seconds_total"], "gpu_seconds_by_call": out["gpu_seconds"],
+            "reference_seconds_in_calls": ref_calls, "reference_learn_seconds": ref["learn"],
+            "reference_seconds_by_call": ref, "speedup_in_calls": ref_calls / out["gpu_seconds_total"],
+            "calls": out["calls"], "knowledge_base": out["knowledge_base"],
+            "replay_wall_seconds_incl_checks": wall,
+            "results_equal_reference": True, "learnt_clauses": out["reference_clauses"],
+            "reference_host": "x86_64 build container, 1 core (the reference cannot run on the GPU host)"}
 
 
 def run_serving(eng, w, dev, torch, n_requests: int = 64, lits_per_request: int = 64, slots: int = 8):

@@ -175,14 +175,29 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* s_warp
 // own sub-bins, so no global fine histogram exists.  With bits <= 8 a single
 // pass writes the partitions directly.
 
+// One literal group's partition job.  Every partition kernel takes the
+// array of all groups' jobs and serves group blockIdx.y, so one launch of
+// each kernel covers the whole step (the groups' scratch is separate).
 struct BPartArgs {
   const int32_t* cols[kGroupCols];  // cols[0] = join column
   int ncols;
   int64_t n, npos;
   int bits;                 // partition bits
   int cbits;                // pass-1 bits (== bits: single pass)
+  int two_pass;
+  int vec;                  // every source column 16-byte aligned
   uint32_t* p1_tot;         // 2 << cbits bin totals (zeroed)
   uint32_t* p1_base;        // gridDim.x * (2 << cbits) per-CTA bases
+  uint32_t* p1_pad;         // (2 << cbits) + 1 padded bin starts (two passes)
+  uint32_t* p1_unp;         // (2 << cbits) + 1 bin starts (one pass: the segment starts)
+  uint32_t* chunk_start;    // (2 << cbits) + 1 first pass-2 chunk of every bin
+  uint32_t* chunk_bin;      // coarse bin of every pass-2 chunk
+  uint32_t* h2;             // pass-2 chunk sub-bin counts, then cursors
+  int32_t* tmp;             // pass-1 output (two passes), column stride tmp_stride
+  int64_t tmp_stride;
+  int32_t* out;             // partitioned columns, column stride out_stride
+  int64_t out_stride;
+  uint32_t* fstart;         // (2 << bits) + 1 segment starts
   // Rows whose top cbits hash bits fall outside [keep_lo, keep_hi] belong to
   // other shards' partitions and are dropped in pass 1 (QFG_OPT_SHARD_*).
   uint32_t keep_lo, keep_hi;
@@ -206,8 +221,7 @@ __device__ __forceinline__ int lane_of(const int4& v, int k) {
 }
 
 template <bool kVec>
-__global__ void __launch_bounds__(kPartThreads, 1) bpart_hist_kernel(BPartArgs a) {
-  __shared__ uint32_t p1[2 << (kMaxCoarseBits + 1)];
+__device__ __forceinline__ void bpart_hist_body(const BPartArgs& a, uint32_t* p1) {
   const int np1 = 2 << a.cbits;
   for (int i = threadIdx.x; i < np1; i += blockDim.x) p1[i] = 0;
   __syncthreads();
@@ -244,6 +258,15 @@ __global__ void __launch_bounds__(kPartThreads, 1) bpart_hist_kernel(BPartArgs a
     const uint32_t c = p1[i];
     a.p1_base[(int64_t)blockIdx.x * np1 + i] = c ? atomicAdd(&a.p1_tot[i], c) : 0u;
   }
+}
+
+__global__ void __launch_bounds__(kPartThreads, 1) bpart_hist_kernel(const BPartArgs* __restrict__ A) {
+  __shared__ uint32_t p1[2 << (kMaxCoarseBits + 1)];
+  const BPartArgs& a = A[blockIdx.y];
+  if (a.vec)
+    bpart_hist_body<true>(a, p1);
+  else
+    bpart_hist_body<false>(a, p1);
 }
 
 // Round processing.  A round is up to kPassRows consecutive rows of one
@@ -441,10 +464,15 @@ __device__ __forceinline__ void stream_pass(const PassSmem& S, const int32_t* co
 
 // Pass 1: the CTA's chunk of the original columns into pass-1 bins at
 // p1_start[bin] + this CTA's base (out: column stride out_stride).
-__global__ void __launch_bounds__(kPassThreads, 1)
-bpart_pass1_kernel(BPartArgs a, const uint32_t* __restrict__ p1_start, int32_t* __restrict__ out,
-                   int64_t out_stride, int aligned) {
+__global__ void __launch_bounds__(kPassThreads, 1) bpart_pass1_kernel(const BPartArgs* __restrict__ A) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const BPartArgs& a = A[blockIdx.y];
+  // Two passes: into the padded coarse bins of the scratch; one pass: into
+  // the partitions themselves.
+  const uint32_t* __restrict__ p1_start = a.two_pass ? a.p1_pad : a.p1_unp;
+  int32_t* __restrict__ out = a.two_pass ? a.tmp : a.out;
+  const int64_t out_stride = a.two_pass ? a.tmp_stride : a.out_stride;
+  const int aligned = a.vec;
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   __shared__ const int32_t* s_src[kGroupCols];
@@ -503,11 +531,17 @@ static_assert(kP2Chunk <= (uint32_t)kPassRows, "a pass-2 chunk is one round");
 // unpadded (where pass 2 writes); the first pass-2 chunk of every bin
 // (chunk_start[nbins] = number of chunks) and the bin of every chunk.  One
 // block, nbins <= blockDim.x.
-__global__ void pad_scan_kernel(const uint32_t* __restrict__ tot, int nbins, uint32_t* __restrict__ pad,
-                                uint32_t* __restrict__ unp, uint32_t* __restrict__ chunk_start,
-                                uint32_t* __restrict__ chunk_bin) {
+__global__ void pad_scan_kernel(const BPartArgs* __restrict__ A) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
+  const BPartArgs& a = A[blockIdx.x];
+  const uint32_t* __restrict__ tot = a.p1_tot;
+  const int nbins = 2 << a.cbits;
+  uint32_t* __restrict__ pad = a.p1_pad;
+  uint32_t* __restrict__ unp = a.p1_unp;
+  uint32_t* __restrict__ chunk_start = a.chunk_start;
+  uint32_t* __restrict__ chunk_bin = a.chunk_bin;
+  const bool two = a.two_pass != 0;
   const uint32_t c = (int)threadIdx.x < nbins ? tot[threadIdx.x] : 0u;
   const uint32_t ex = block_scan_excl(c, s_warp, &s_total);
   const uint32_t total = s_total;
@@ -516,15 +550,19 @@ __global__ void pad_scan_kernel(const uint32_t* __restrict__ tot, int nbins, uin
   const uint32_t exc = block_scan_excl((c + kP2Chunk - 1u) / kP2Chunk, s_warp, &s_total);
   if ((int)threadIdx.x < nbins) {
     unp[threadIdx.x] = ex;
-    pad[threadIdx.x] = exp;
-    chunk_start[threadIdx.x] = exc;
-    const uint32_t nch = (c + kP2Chunk - 1u) / kP2Chunk;
-    for (uint32_t j = 0; j < nch; ++j) chunk_bin[exc + j] = threadIdx.x;
+    if (two) {
+      pad[threadIdx.x] = exp;
+      chunk_start[threadIdx.x] = exc;
+      const uint32_t nch = (c + kP2Chunk - 1u) / kP2Chunk;
+      for (uint32_t j = 0; j < nch; ++j) chunk_bin[exc + j] = threadIdx.x;
+    }
   }
   if (threadIdx.x == 0) {
     unp[nbins] = total;
-    pad[nbins] = total_pad;
-    chunk_start[nbins] = s_total;
+    if (two) {
+      pad[nbins] = total_pad;
+      chunk_start[nbins] = s_total;
+    }
   }
 }
 
@@ -549,13 +587,16 @@ __device__ __forceinline__ P2Chunk p2_chunk(const uint32_t* __restrict__ chunk_b
 }
 
 // Sub-bin counts of every pass-2 chunk: h2[c * nsub + sub].
-__global__ void __launch_bounds__(512) bpart_p2hist_kernel(BPartArgs a, const uint32_t* __restrict__ pad,
-                                                           const uint32_t* __restrict__ unp,
-                                                           const uint32_t* __restrict__ chunk_start,
-                                                           const uint32_t* __restrict__ chunk_bin,
-                                                           const int32_t* __restrict__ keys,
-                                                           uint32_t* __restrict__ h2) {
+__global__ void __launch_bounds__(512) bpart_p2hist_kernel(const BPartArgs* __restrict__ A) {
   __shared__ uint32_t cntr[1 << kMaxSubBits];
+  const BPartArgs& a = A[blockIdx.y];
+  if (!a.two_pass) return;
+  const uint32_t* __restrict__ pad = a.p1_pad;
+  const uint32_t* __restrict__ unp = a.p1_unp;
+  const uint32_t* __restrict__ chunk_start = a.chunk_start;
+  const uint32_t* __restrict__ chunk_bin = a.chunk_bin;
+  const int32_t* __restrict__ keys = a.tmp;  // the join column of the pass-1 output
+  uint32_t* __restrict__ h2 = a.h2;
   const int np1 = 2 << a.cbits;
   const int bits = a.bits;
   const int nsub = 1 << (a.bits - a.cbits);
@@ -584,15 +625,18 @@ __global__ void __launch_bounds__(512) bpart_p2hist_kernel(BPartArgs a, const ui
 // counts into output cursors (sub-bin start + the counts of the bin's earlier
 // chunks) and records where each sub-bin starts: fine_start[(b << sbits) +
 // sub] (the last block also writes the end, n).
-__global__ void __launch_bounds__(512) bpart_p2scan_kernel(BPartArgs a, const uint32_t* __restrict__ unp,
-                                                           const uint32_t* __restrict__ chunk_start,
-                                                           uint32_t* __restrict__ h2,
-                                                           uint32_t* __restrict__ fine_start) {
+__global__ void __launch_bounds__(512) bpart_p2scan_kernel(const BPartArgs* __restrict__ A) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
+  const BPartArgs& a = A[blockIdx.y];
+  const int np1 = 2 << a.cbits;
+  if (!a.two_pass || (int)blockIdx.x >= np1) return;  // block-uniform
+  const uint32_t* __restrict__ unp = a.p1_unp;
+  const uint32_t* __restrict__ chunk_start = a.chunk_start;
+  uint32_t* __restrict__ h2 = a.h2;
+  uint32_t* __restrict__ fine_start = a.fstart;
   const int sbits = a.bits - a.cbits;
   const int nsub = 1 << sbits;
-  const int np1 = 2 << a.cbits;
   const int b = blockIdx.x;
   const uint32_t c0 = chunk_start[b], c1 = chunk_start[b + 1];
   const int sub = threadIdx.x;
@@ -616,11 +660,19 @@ __global__ void __launch_bounds__(512) bpart_p2scan_kernel(BPartArgs a, const ui
 // Pass 2, persistent over chunks: each chunk of a coarse bin, read from the
 // padded layout, is split into sub-bins 0 .. 2^sbits - 1 at its cursors.
 __global__ void __launch_bounds__(kPassThreads, 1)
-bpart_pass2_kernel(BPartArgs a, const uint32_t* __restrict__ pad, const uint32_t* __restrict__ unp,
-                   const uint32_t* __restrict__ chunk_start, const uint32_t* __restrict__ chunk_bin,
-                   const uint32_t* __restrict__ h2, const int32_t* __restrict__ in, int64_t in_stride,
-                   int32_t* __restrict__ out, int64_t out_stride) {
+bpart_pass2_kernel(const BPartArgs* __restrict__ A) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const BPartArgs& a = A[blockIdx.y];
+  if (!a.two_pass) return;
+  const uint32_t* __restrict__ pad = a.p1_pad;
+  const uint32_t* __restrict__ unp = a.p1_unp;
+  const uint32_t* __restrict__ chunk_start = a.chunk_start;
+  const uint32_t* __restrict__ chunk_bin = a.chunk_bin;
+  const uint32_t* __restrict__ h2 = a.h2;
+  const int32_t* __restrict__ in = a.tmp;
+  const int64_t in_stride = a.tmp_stride;
+  int32_t* __restrict__ out = a.out;
+  const int64_t out_stride = a.out_stride;
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   __shared__ const int32_t* s_src[kGroupCols];
@@ -1792,12 +1844,7 @@ static int plan_step(Ctx* ctx, int32_t n, const qfg_literal* lits, StepPlan* pla
 // into a CUDA graph and replayed on new binding data of the same shape.
 struct PartJob {
   BPartArgs pa;             // pa.bits / pa.cbits: this group's partition shape
-  bool vec;
-  bool two_pass;
   int np1, sbits;
-  size_t p1_smem, p2_smem;
-  int32_t* final_out;
-  uint32_t* fstart;
 };
 
 struct LaunchJob {
@@ -1812,15 +1859,12 @@ struct LaunchJob {
 struct PreparedStep {
   int mode = 0;             // kModeTiled or kModeStreamed
   unsigned pgrid = 0;
-  uint32_t* p1_tot = nullptr;
-  uint32_t* p1_base = nullptr;
-  uint32_t* p1_start = nullptr;   // padded bin starts (two passes)
-  uint32_t* p1_unp = nullptr;     // unpadded bin starts (two passes)
-  uint32_t* chunk_start = nullptr;  // first pass-2 chunk of every bin
-  uint32_t* chunk_bin = nullptr;    // coarse bin of every pass-2 chunk
-  uint32_t* h2 = nullptr;         // pass-2 chunk sub-bin counts, then cursors
-  int32_t* tmp_cols = nullptr;
-  int64_t tmp_stride = 0;
+  uint32_t* p1_tot = nullptr;     // every group's pass-1 bin totals, contiguous (zeroed per step)
+  size_t p1_tot_words = 0;
+  int np1_max = 0;                // widest pass-1 fan-out of the groups
+  size_t p1_smem = 0, p2_smem = 0;
+  bool any_two_pass = false;
+  const BPartArgs* part_args_dev = nullptr;  // the groups' jobs in the descriptor blob
   int64_t col_stride = 0;   // column stride of the partitioned layout
   std::vector<PartJob> parts;
   std::vector<LaunchJob> launches;
@@ -1930,51 +1974,52 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   // Partitioned columns: stride a multiple of 4 rows, so every column of a
   // group has the same 16-byte alignment (the evaluation's bulk copies).
   ps->col_stride = ((int64_t)nb + 3) & ~int64_t(3);
-  std::vector<int> gbits(groups.size());
-  size_t part_words = 0, fs_words = 0;
-  int max_ncols = 1, np1_max = 2, sbits_max = 0;
-  bool any_two_pass = false;
-  for (size_t gi = 0; gi < groups.size(); ++gi) {
+  const size_t G = groups.size();
+  std::vector<int> gbits(G), gcbits(G);
+  size_t part_words = 0, fs_words = 0, tot_words = 0, bins_words = 0, tmp_words = 0;
+  ps->np1_max = 2;
+  int sbits_max = 1;
+  ps->any_two_pass = false;
+  for (size_t gi = 0; gi < G; ++gi) {
     const HostGroup& g = groups[gi];
     int64_t entries = 0;
     for (int i : g.lits) entries += tables[i]->num_entries;
     gbits[gi] = group_bits(ctx, mode, nb, entries);
+    const bool two = gbits[gi] > kMaxSinglePassBits;
+    gcbits[gi] = two ? coarse_bits(ctx, nb, gbits[gi]) : gbits[gi];
+    const int np1 = 2 << gcbits[gi];
+    const size_t chunks = (size_t)nb / kP2Chunk + (size_t)np1 + 1;
     part_words += g.cols.size() * (size_t)ps->col_stride;
     fs_words += ((size_t)2 << gbits[gi]) + 1;
-    max_ncols = std::max(max_ncols, (int)g.cols.size());
-    const bool two = gbits[gi] > kMaxSinglePassBits;
-    const int cb = two ? coarse_bits(ctx, nb, gbits[gi]) : gbits[gi];
-    np1_max = std::max(np1_max, 2 << cb);
+    tot_words += (size_t)np1 + 1;
+    bins_words += (size_t)ps->pgrid * np1;  // per-CTA bases
     if (two) {
-      any_two_pass = true;
-      sbits_max = std::max(sbits_max, gbits[gi] - cb);
+      bins_words += 3 * ((size_t)np1 + 1) + chunks + (chunks << (gbits[gi] - gcbits[gi]));
+      tmp_words += g.cols.size() * (size_t)((((int64_t)nb + 3) & ~int64_t(3)) + 4 * (int64_t)np1);
+      sbits_max = std::max(sbits_max, gbits[gi] - gcbits[gi]);
+      ps->any_two_pass = true;
     }
+    ps->np1_max = std::max(ps->np1_max, np1);
   }
-  // Pass-1 output: bins padded to multiples of 4 rows, 16-byte aligned columns.
-  ps->tmp_stride = any_two_pass ? (((int64_t)nb + 3) & ~int64_t(3)) + 4 * (int64_t)np1_max : 0;
   const size_t tmp_off = (part_words + 63) & ~size_t(63);
-  const size_t tmp_words = any_two_pass ? (size_t)max_ncols * (size_t)ps->tmp_stride : 0;
-  const size_t h2_words =
-      any_two_pass ? ((size_t)nb / kP2Chunk + (size_t)np1_max + 1) * ((size_t)1 << sbits_max) : 0;
-  const size_t chunk_words = any_two_pass ? (size_t)nb / kP2Chunk + (size_t)np1_max + 1 : 0;
-  const size_t bins_words = (size_t)np1_max + 1 + (size_t)ps->pgrid * np1_max +
-                            3 * ((size_t)np1_max + 1) + h2_words + chunk_words;
-  QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * (tmp_off + tmp_words)));
-  QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(ctx, sizeof(uint32_t) * (fs_words + bins_words)));
+  QFG_TRY(ctx->scratch[kScrBindPart].reserve(ctx, sizeof(int32_t) * (tmp_off + tmp_words + 64)));
+  QFG_TRY(ctx->scratch[kScrBindOffsets].reserve(
+      ctx, sizeof(uint32_t) * (fs_words + tot_words + bins_words + 64)));
   int32_t* part_base = ctx->scratch[kScrBindPart].as<int32_t>();
-  ps->tmp_cols = part_base + tmp_off;
   uint32_t* fstarts = ctx->scratch[kScrBindOffsets].as<uint32_t>();
   ps->p1_tot = fstarts + fs_words;
-  ps->p1_base = ps->p1_tot + np1_max + 1;
-  ps->p1_start = ps->p1_base + (size_t)ps->pgrid * np1_max;
-  ps->p1_unp = ps->p1_start + np1_max + 1;
-  ps->chunk_start = ps->p1_unp + np1_max + 1;
-  ps->h2 = ps->chunk_start + np1_max + 1;
-  ps->chunk_bin = ps->h2 + h2_words;
+  ps->p1_tot_words = tot_words;
+  ps->p1_smem = pass_smem_bytes(ps->np1_max);
+  ps->p2_smem = pass_smem_bytes(1 << sbits_max);
   QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)pass_smem_bytes(np1_max)));
+                                     (int)ps->p1_smem));
   QFG_CUDA(ctx, cudaFuncSetAttribute(bpart_pass2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)pass_smem_bytes(1 << std::max(sbits_max, 1))));
+                                     (int)ps->p2_smem));
+  // Carving cursors: bin arrays after the totals, pass-1 outputs after the
+  // partitioned columns (each two-pass group's own, 16-byte aligned).
+  uint32_t* bins_cur = ps->p1_tot + tot_words;
+  uint32_t* tot_cur = ps->p1_tot;
+  int32_t* tmp_cur = part_base + tmp_off;
 
   std::vector<GroupDesc> gdesc(groups.size());
   std::vector<LitDesc> ldesc;
@@ -1988,37 +2033,53 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     const uint32_t shard_lo = (uint32_t)(((int64_t)ctx->shard_index << bits) / ctx->shard_count);
     const uint32_t shard_hi = (uint32_t)(((int64_t)(ctx->shard_index + 1) << bits) / ctx->shard_count);
     PartJob job;
-    job.two_pass = bits > kMaxSinglePassBits;
-    const int cbits = job.two_pass ? coarse_bits(ctx, nb, bits) : bits;
+    BPartArgs& pa = job.pa;
+    memset(&pa, 0, sizeof(pa));
+    pa.two_pass = bits > kMaxSinglePassBits ? 1 : 0;
+    const int cbits = gcbits[gi];
     job.sbits = bits - cbits;
     job.np1 = 2 << cbits;
-    job.p1_smem = pass_smem_bytes(job.np1);
-    job.p2_smem = pass_smem_bytes(1 << std::max(job.sbits, 1));
-    BPartArgs& pa = job.pa;
     pa.ncols = (int)g.cols.size();
     for (int c = 0; c < pa.ncols; ++c) pa.cols[c] = b->columns[g.cols[c]];
     pa.n = nb;
     pa.npos = b->num_positive;
     pa.bits = bits;
     pa.cbits = cbits;
-    pa.p1_tot = ps->p1_tot;
-    pa.p1_base = ps->p1_base;
+    pa.vec = 1;
+    for (int c = 0; c < pa.ncols; ++c)
+      if (reinterpret_cast<uintptr_t>(pa.cols[c]) % 16 != 0) pa.vec = 0;
     // The shard's partitions [shard_lo, shard_hi) cover these pass-1 hash
     // ranges; rows of other ranges are dropped before their columns move.
     pa.keep_lo = shard_lo >> job.sbits;
     pa.keep_hi = shard_hi > shard_lo ? (shard_hi - 1) >> job.sbits : 0u;
     if (shard_hi <= shard_lo) pa.keep_lo = 1u;  // an empty shard keeps nothing
-    job.final_out = part_base + off;
-    job.fstart = fstarts + fs_off;
-    job.vec = true;
-    for (int c = 0; c < pa.ncols; ++c)
-      if (reinterpret_cast<uintptr_t>(pa.cols[c]) % 16 != 0) job.vec = false;
+    pa.out = part_base + off;
+    pa.out_stride = ps->col_stride;
+    pa.fstart = fstarts + fs_off;
+    pa.p1_tot = tot_cur;
+    tot_cur += job.np1 + 1;
+    pa.p1_base = bins_cur;
+    bins_cur += (size_t)ps->pgrid * job.np1;
+    if (pa.two_pass) {
+      const size_t chunks = (size_t)nb / kP2Chunk + (size_t)job.np1 + 1;
+      pa.p1_pad = bins_cur;
+      pa.p1_unp = pa.p1_pad + job.np1 + 1;
+      pa.chunk_start = pa.p1_unp + job.np1 + 1;
+      pa.chunk_bin = pa.chunk_start + job.np1 + 1;
+      pa.h2 = pa.chunk_bin + chunks;
+      bins_cur = pa.h2 + (chunks << job.sbits);
+      pa.tmp_stride = ((((int64_t)nb + 3) & ~int64_t(3)) + 4 * (int64_t)job.np1);
+      pa.tmp = tmp_cur;
+      tmp_cur += (size_t)pa.ncols * (size_t)pa.tmp_stride;
+    } else {
+      pa.p1_unp = pa.fstart;  // one pass: the bin starts are the segment starts
+    }
     ps->parts.push_back(job);
 
     GroupDesc& d = gdesc[gi];
-    d.cols = job.final_out;
+    d.cols = pa.out;
     d.n = ps->col_stride;
-    d.fstart = job.fstart;
+    d.fstart = pa.fstart;
     d.bits = bits;
     d.sbits = job.sbits;
     d.ncols = pa.ncols;
@@ -2099,13 +2160,17 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     gbeg = gend;
   }
   for (const SigDesc& sd : sdesc) sig_all.push_back(sd);
+  std::vector<BPartArgs> part_all;
+  for (const PartJob& j : ps->parts) part_all.push_back(j.pa);
   const size_t gbytes = sizeof(GroupDesc) * sub_all.size();
   const size_t lbytes = sizeof(LitDesc) * lit_all.size();
   const size_t sbytes = sizeof(SigDesc) * sig_all.size();
-  ps->blob.resize(gbytes + lbytes + sbytes);
+  const size_t pbytes = sizeof(BPartArgs) * part_all.size();
+  ps->blob.resize(gbytes + lbytes + sbytes + pbytes);
   memcpy(ps->blob.data(), sub_all.data(), gbytes);
   memcpy(ps->blob.data() + gbytes, lit_all.data(), lbytes);
   if (sbytes) memcpy(ps->blob.data() + gbytes + lbytes, sig_all.data(), sbytes);
+  memcpy(ps->blob.data() + gbytes + lbytes + sbytes, part_all.data(), pbytes);
   QFG_TRY(ctx->scratch[kScrLits].reserve(ctx, ps->blob.size() + 64));
   // Work units: at most one per item plus one per `piece` entries; entry
   // records (tiled path): every entry once, each unit's block padded to 4.
@@ -2147,8 +2212,10 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
   GroupDesc* gdev = ctx->scratch[kScrLits].as<GroupDesc>();
   LitDesc* ldev = reinterpret_cast<LitDesc*>(gdev + sub_all.size());
   SigDesc* sdev = reinterpret_cast<SigDesc*>(ldev + lit_all.size());
+  BPartArgs* pdev = reinterpret_cast<BPartArgs*>(sdev + sig_all.size());
   ps->blob_dev = gdev;
-  ps->counter = reinterpret_cast<unsigned int*>(sdev + sig_all.size());
+  ps->part_args_dev = pdev;
+  ps->counter = reinterpret_cast<unsigned int*>(pdev + part_all.size());
   for (size_t si = 0; si < spans.size(); ++si) {
     const Span& S = spans[si];
     LaunchJob L;
@@ -2214,36 +2281,24 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
   const PreparedStep& ps = *pps;
   if (ps.parts.empty()) return QFG_OK;
   QFG_TRY(stage_begin(ctx, QFG_STAGE_BIND_PARTITION));
-  for (const PartJob& job : ps.parts) {
-    QFG_CUDA(ctx, cudaMemsetAsync(ps.p1_tot, 0, sizeof(uint32_t) * (size_t)job.np1, ctx->stream));
-    if (job.vec)
-      bpart_hist_kernel<true><<<ps.pgrid, kPartThreads, 0, ctx->stream>>>(job.pa);
-    else
-      bpart_hist_kernel<false><<<ps.pgrid, kPartThreads, 0, ctx->stream>>>(job.pa);
+  // One launch of each partition kernel covers every literal group
+  // (blockIdx.y = group); groups with one pass skip the pass-2 kernels.
+  const unsigned G = (unsigned)ps.parts.size();
+  const BPartArgs* A = ps.part_args_dev;
+  QFG_CUDA(ctx, cudaMemsetAsync(ps.p1_tot, 0, sizeof(uint32_t) * ps.p1_tot_words, ctx->stream));
+  bpart_hist_kernel<<<dim3(ps.pgrid, G), kPartThreads, 0, ctx->stream>>>(A);
+  QFG_LAUNCHED(ctx);
+  pad_scan_kernel<<<G, 512, 0, ctx->stream>>>(A);
+  QFG_LAUNCHED(ctx);
+  bpart_pass1_kernel<<<dim3(ps.pgrid, G), kPassThreads, ps.p1_smem, ctx->stream>>>(A);
+  QFG_LAUNCHED(ctx);
+  if (ps.any_two_pass) {
+    bpart_p2hist_kernel<<<dim3(ps.pgrid * 2, G), 512, 0, ctx->stream>>>(A);
     QFG_LAUNCHED(ctx);
-    if (job.two_pass) {
-      pad_scan_kernel<<<1, 512, 0, ctx->stream>>>(ps.p1_tot, job.np1, ps.p1_start, ps.p1_unp,
-                                                  ps.chunk_start, ps.chunk_bin);
-      QFG_LAUNCHED(ctx);
-      bpart_pass1_kernel<<<ps.pgrid, kPassThreads, job.p1_smem, ctx->stream>>>(
-          job.pa, ps.p1_start, ps.tmp_cols, ps.tmp_stride, job.vec ? 1 : 0);
-      QFG_LAUNCHED(ctx);
-      bpart_p2hist_kernel<<<ps.pgrid * 2, 512, 0, ctx->stream>>>(
-          job.pa, ps.p1_start, ps.p1_unp, ps.chunk_start, ps.chunk_bin, ps.tmp_cols, ps.h2);
-      QFG_LAUNCHED(ctx);
-      bpart_p2scan_kernel<<<job.np1, 512, 0, ctx->stream>>>(job.pa, ps.p1_unp, ps.chunk_start, ps.h2,
-                                                            job.fstart);
-      QFG_LAUNCHED(ctx);
-      bpart_pass2_kernel<<<ps.pgrid, kPassThreads, job.p2_smem, ctx->stream>>>(
-          job.pa, ps.p1_start, ps.p1_unp, ps.chunk_start, ps.chunk_bin, ps.h2, ps.tmp_cols,
-          ps.tmp_stride, job.final_out, ps.col_stride);
-      QFG_LAUNCHED(ctx);
-    } else {
-      QFG_TRY(exclusive_scan_u32(ctx, ps.p1_tot, job.fstart, job.np1, job.fstart + job.np1));
-      bpart_pass1_kernel<<<ps.pgrid, kPassThreads, job.p1_smem, ctx->stream>>>(
-          job.pa, job.fstart, job.final_out, ps.col_stride, job.vec ? 1 : 0);
-      QFG_LAUNCHED(ctx);
-    }
+    bpart_p2scan_kernel<<<dim3((unsigned)ps.np1_max, G), 512, 0, ctx->stream>>>(A);
+    QFG_LAUNCHED(ctx);
+    bpart_pass2_kernel<<<dim3(ps.pgrid, G), kPassThreads, ps.p2_smem, ctx->stream>>>(A);
+    QFG_LAUNCHED(ctx);
   }
   QFG_TRY(stage_end(ctx, QFG_STAGE_BIND_PARTITION));
   for (const LaunchJob& L : ps.launches) {
@@ -2286,27 +2341,24 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
   const int mode = step_mode(ctx, nb);
   StepPlan plan;
   QFG_TRY(plan_step(ctx, n, lits, &plan, mode == kModeStreamed ? kSMaxSigs : 0));
-  int64_t words = 0, units = 0, entries = 0;
-  int max_ncols = 1, np1_max = 2, sbits_max = 0;
-  bool two_pass = false;
+  int64_t words = 256, units = 0, entries = 0;
   for (auto& g : plan.groups) {
     int64_t ge = 0;
     for (int i : g.lits) ge += plan.tables[i]->num_entries;
     const int bits = group_bits(ctx, mode, nb, ge);
     words += (int64_t)g.cols.size() * (nb + 4) + (2 << bits) + 1;
-    max_ncols = std::max(max_ncols, (int)g.cols.size());
     const bool two = bits > kMaxSinglePassBits;
     const int cb = two ? coarse_bits(ctx, nb, bits) : bits;
-    np1_max = std::max(np1_max, 2 << cb);
+    const int64_t np1 = 2 << cb;
+    words += np1 + 1 + np1 * ctx->num_sms;
     if (two) {
-      two_pass = true;
-      sbits_max = std::max(sbits_max, bits - cb);
+      // each two-pass group keeps its own pass-1 output and bin arrays
+      const int64_t chunks = nb / kP2Chunk + np1 + 1;
+      words += (int64_t)g.cols.size() * (nb + 4 + 4 * np1) + 3 * (np1 + 1) + chunks +
+               (chunks << (bits - cb));
     }
     units += (int64_t)1 << bits;
   }
-  if (two_pass) words += (int64_t)max_ncols * (nb + 4 + 4 * np1_max) + 64;
-  words += (int64_t)np1_max * (ctx->num_sms * 2 + 5);
-  if (two_pass) words += (nb / kP2Chunk + np1_max + 1) * ((1 << sbits_max) + 1);
   const int64_t piece = mode == kModeStreamed ? kSEntries : kChunk;
   for (KeyTable* kt : plan.tables) {
     units += kt->num_entries / piece + 1;
