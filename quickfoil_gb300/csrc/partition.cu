@@ -128,6 +128,152 @@ __global__ void stable_scatter_kernel(IO io, int64_t n, int shift, int bits, int
   }
 }
 
+// Shared-memory staged stable pass (qfg_radix_partition).  A CTA owns a
+// contiguous row range and takes it in rounds of kRTRound rows: the round's
+// keys are staged in shared memory, ranked stably by digit -- waves of one
+// row per thread, a warp's rank from __match_any_sync, the warps' counts of
+// every digit scanned in warp order, the digit's count from earlier waves
+// added -- and written in digit order, consecutive threads on consecutive
+// output positions of a digit's run.  The CTA's cursors come from a
+// digit-major scan of per-CTA digit counts, so the whole pass is stable.
+constexpr int kRTThreads = 512;
+constexpr int kRTWarps = kRTThreads / 32;
+constexpr int kRTWaves = 8;
+constexpr int kRTRound = kRTThreads * kRTWaves;  // 4096 rows a round
+constexpr int kRTMaxBits = 8;
+static_assert(kRTRound <= 65536, "a round's row packs into 16 bits");
+
+size_t round_smem_bytes(int bits) {
+  const size_t P = size_t(1) << bits;
+  return sizeof(uint32_t) * (2 * (size_t)kRTRound + (size_t)kRTWarps * P + 4 * P);
+}
+
+template <class IO>
+__global__ void __launch_bounds__(kRTThreads) round_hist_kernel(IO io, int64_t n, int shift, int bits,
+                                                                int64_t per,
+                                                                uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[1 << kRTMaxBits];
+  const uint32_t P = 1u << bits, mask = P - 1u;
+  for (uint32_t d = threadIdx.x; d < P; d += blockDim.x) h[d] = 0u;
+  __syncthreads();
+  const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(n, r0 + per);
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) atomicAdd(&h[(io.key(r) >> shift) & mask], 1u);
+  __syncthreads();
+  for (uint32_t d = threadIdx.x; d < P; d += blockDim.x) hist[(int64_t)d * gridDim.x + blockIdx.x] = h[d];
+}
+
+template <class IO>
+__global__ void __launch_bounds__(kRTThreads) round_scatter_kernel(IO io, int64_t n, int shift, int bits,
+                                                                   int64_t per,
+                                                                   const uint32_t* __restrict__ cursors) {
+  extern __shared__ uint32_t rs[];
+  const uint32_t P = 1u << bits, mask = P - 1u;
+  uint32_t* keys = rs;                   // kRTRound
+  uint32_t* perm = keys + kRTRound;      // kRTRound: row | digit << 16 by sorted position
+  uint32_t* wcnt = perm + kRTRound;      // kRTWarps * P: a wave's counts, then prefixes
+  uint32_t* dcnt = wcnt + kRTWarps * P;  // P: the round's count of each digit so far
+  uint32_t* dstart = dcnt + P;           // P
+  uint32_t* gpos = dstart + P;           // P
+  uint32_t* cur = gpos + P;              // P: the CTA's output cursors
+  __shared__ uint32_t s_warp[kRTWarps];
+  const int t = threadIdx.x, lane = lane_id(), warp = warp_id();
+  const unsigned lt = lanemask_lt();
+  for (uint32_t d = t; d < P; d += blockDim.x) {
+    cur[d] = cursors[(int64_t)d * gridDim.x + blockIdx.x];
+    dcnt[d] = 0u;
+  }
+  for (uint32_t i = t; i < (uint32_t)kRTWarps * P; i += blockDim.x) wcnt[i] = 0u;
+  __syncthreads();
+  const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(n, r0 + per);
+  for (int64_t rr = r0; rr < r1; rr += kRTRound) {
+    const int nt = (int)min((int64_t)kRTRound, r1 - rr);
+#pragma unroll
+    for (int j = 0; j < kRTWaves; ++j) {
+      const int i = j * kRTThreads + t;
+      if (i < nt) keys[i] = io.key(rr + i);
+    }
+    __syncthreads();
+    uint32_t dj[kRTWaves], rk[kRTWaves];
+#pragma unroll
+    for (int j = 0; j < kRTWaves; ++j) {
+      const int i = j * kRTThreads + t;
+      const bool valid = i < nt;
+      const uint32_t d = valid ? (keys[i] >> shift) & mask : 0u;
+      const unsigned act = __ballot_sync(kFullMask, valid);
+      unsigned peers = 0;
+      if (valid) {
+        peers = __match_any_sync(act, d);
+        if (lane == __ffs(peers) - 1) wcnt[warp * P + d] = __popc(peers);
+      }
+      __syncthreads();
+      // Warp-order prefix of every digit, after the digit's earlier waves.
+      for (uint32_t dd = t; dd < P; dd += blockDim.x) {
+        uint32_t run = dcnt[dd];
+        for (int w = 0; w < kRTWarps; ++w) {
+          const uint32_t c = wcnt[w * P + dd];
+          wcnt[w * P + dd] = run;
+          run += c;
+        }
+        dcnt[dd] = run;
+      }
+      __syncthreads();
+      dj[j] = d;
+      rk[j] = valid ? wcnt[warp * P + d] + __popc(peers & lt) : 0u;
+      __syncthreads();
+      for (uint32_t i2 = t; i2 < (uint32_t)kRTWarps * P; i2 += blockDim.x) wcnt[i2] = 0u;
+      __syncthreads();
+    }
+    // Digit starts within the round (block scan of the P counts) and output
+    // positions: sorted position k of digit d goes to gpos[d] + k.
+    {
+      const uint32_t c = (uint32_t)t < P ? dcnt[t] : 0u;
+      uint32_t x = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFullMask, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane == 31) s_warp[warp] = x;
+      __syncthreads();
+      if (warp == 0) {
+        const uint32_t v = lane < kRTWarps ? s_warp[lane] : 0u;
+        uint32_t sc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(kFullMask, sc, o);
+          if (lane >= o) sc += y;
+        }
+        if (lane < kRTWarps) s_warp[lane] = sc - v;
+      }
+      __syncthreads();
+      if ((uint32_t)t < P) {
+        const uint32_t ex = x - c + s_warp[warp];
+        dstart[t] = ex;
+        gpos[t] = cur[t] - ex;
+        cur[t] += c;
+        dcnt[t] = 0u;
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < kRTWaves; ++j) {
+      const int i = j * kRTThreads + t;
+      if (i < nt) perm[dstart[dj[j]] + rk[j]] = (uint32_t)i | (dj[j] << 16);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRTWaves; ++j) {
+      const int k = j * kRTThreads + t;
+      if (k < nt) {
+        const uint32_t v = perm[k];
+        const uint32_t row = v & 0xffffu;
+        io.write((int64_t)gpos[v >> 16] + k, rr + row, keys[row]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // offsets[d] = cursor of digit d in chunk 0; offsets[P] = n.
 __global__ void digit_offsets_kernel(const uint32_t* __restrict__ scanned, int64_t num_chunks,
                                      int bits, int64_t n, int64_t* __restrict__ offsets) {
@@ -181,6 +327,38 @@ int stable_pass(Ctx* ctx, IO io, int64_t n, int shift, int bits, int64_t* digit_
   }
   stable_scatter_kernel<IO><<<s.grid, 32 * s.warps, s.smem, ctx->stream>>>(
       io, n, shift, bits, s.chunk, s.num_chunks, hist);
+  QFG_LAUNCHED(ctx);
+  return QFG_OK;
+}
+
+// One stable partition pass with the round kernels (bits <= kRTMaxBits):
+// per-CTA digit counts, a digit-major scan, the staged scatter.
+template <class IO>
+int round_pass(Ctx* ctx, IO io, int64_t n, int shift, int bits, int64_t* digit_offsets) {
+  const size_t smem = round_smem_bytes(bits);
+  int per_sm = 0;
+  QFG_CUDA(ctx, cudaFuncSetAttribute(round_scatter_kernel<IO>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  QFG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, round_scatter_kernel<IO>,
+                                                              kRTThreads, smem));
+  // One resident wave of CTAs, each a contiguous range of whole rounds.
+  const int64_t rounds = (n + kRTRound - 1) / kRTRound;
+  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(rounds, (int64_t)ctx->num_sms *
+                                                                          std::max(per_sm, 1)));
+  const int64_t per = ((rounds + grid - 1) / grid) * kRTRound;
+  const unsigned g = (unsigned)((n + per - 1) / per);
+  const int64_t entries = (int64_t)g << bits;
+  QFG_TRY(ctx->scratch[kScrHist].reserve(ctx, sizeof(uint32_t) * (size_t)entries));
+  uint32_t* hist = ctx->scratch[kScrHist].as<uint32_t>();
+  round_hist_kernel<IO><<<g, kRTThreads, 0, ctx->stream>>>(io, n, shift, bits, per, hist);
+  QFG_LAUNCHED(ctx);
+  QFG_TRY(exclusive_scan_u32(ctx, hist, hist, entries, nullptr));
+  if (digit_offsets != nullptr) {
+    const uint32_t P = 1u << bits;
+    digit_offsets_kernel<<<(P + 256) / 256, 256, 0, ctx->stream>>>(hist, g, bits, n, digit_offsets);
+    QFG_LAUNCHED(ctx);
+  }
+  round_scatter_kernel<IO><<<g, kRTThreads, smem, ctx->stream>>>(io, n, shift, bits, per, hist);
   QFG_LAUNCHED(ctx);
   return QFG_OK;
 }
@@ -333,10 +511,10 @@ int sort_pairs_u32(Ctx* ctx, uint32_t* k0, int32_t* p0, uint32_t* k1, int32_t* p
   return stable_sort_pairs(ctx, k0, p0, k1, p1, n, key_bits, k_out, p_out);
 }
 
-// Widest digit one stable pass takes: its per-warp count table (4 * 2^bits
-// bytes) then leaves room for eight warps a block and the warp chunk stays
-// at 2048 rows, so grids fill the GPU.  Wider partitions take two passes.
-constexpr int kMaxOnePassRefBits = 8;
+// Widest digit one staged pass takes (its per-warp digit counts stay small
+// and a round's runs average 16 or more rows a digit); wider partitions take
+// two passes.
+constexpr int kMaxOnePassRefBits = kRTMaxBits;
 
 int radix_partition_ref(Ctx* ctx, const int32_t* values, int64_t n, int bits, int32_t* out_tuples,
                         int64_t* out_offsets) {
@@ -347,7 +525,7 @@ int radix_partition_ref(Ctx* ctx, const int32_t* values, int64_t n, int bits, in
   }
   if (bits <= kMaxOnePassRefBits) {
     RefTupleIO io{values, reinterpret_cast<int2*>(out_tuples)};
-    return stable_pass(ctx, io, n, 0, bits, out_offsets);
+    return round_pass(ctx, io, n, 0, bits, out_offsets);
   }
   // Two stable LSD passes: the low digit (value, row index into SoA
   // scratch), then the high digit, writing the tuples.  Both are stable, so
@@ -359,9 +537,9 @@ int radix_partition_ref(Ctx* ctx, const int32_t* values, int64_t n, int bits, in
   uint32_t* mid_keys = ctx->scratch[kScrSortA].as<uint32_t>();
   int32_t* mid_rows = reinterpret_cast<int32_t*>(mid_keys + n);
   SortIO a{reinterpret_cast<const uint32_t*>(values), nullptr, mid_keys, mid_rows};
-  QFG_TRY(stable_pass(ctx, a, n, 0, lo, nullptr));
+  QFG_TRY(round_pass(ctx, a, n, 0, lo, nullptr));
   SoAToRefIO b{mid_keys, mid_rows, reinterpret_cast<int2*>(out_tuples)};
-  QFG_TRY(stable_pass(ctx, b, n, lo, hi, nullptr));
+  QFG_TRY(round_pass(ctx, b, n, lo, hi, nullptr));
   QFG_TRY(ctx->scratch[kScrTmpA].reserve(ctx, sizeof(uint32_t) * (size_t)(P + 1)));
   uint32_t* hist = ctx->scratch[kScrTmpA].as<uint32_t>();
   QFG_CUDA(ctx, cudaMemsetAsync(hist, 0, sizeof(uint32_t) * P, ctx->stream));
