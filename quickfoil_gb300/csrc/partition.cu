@@ -129,17 +129,22 @@ __global__ void stable_scatter_kernel(IO io, int64_t n, int shift, int bits, int
 }
 
 // Shared-memory staged stable pass (qfg_radix_partition).  A CTA owns a
-// contiguous row range and takes it in rounds of kRTRound rows: the round's
-// keys are staged in shared memory, ranked stably by digit -- waves of one
-// row per thread, a warp's rank from __match_any_sync, the warps' counts of
-// every digit scanned in warp order, the digit's count from earlier waves
-// added -- and written in digit order, consecutive threads on consecutive
-// output positions of a digit's run.  The CTA's cursors come from a
-// digit-major scan of per-CTA digit counts, so the whole pass is stable.
+// contiguous row range and takes it in rounds of kRTRound rows.  In a round
+// warp w owns rows [w * kRTPerWarp, (w + 1) * kRTPerWarp) and walks them 32
+// at a time: a row's rank among the warp's rows of its digit is the warp's
+// running count of the digit plus its rank among the equal-digit lanes below
+// it (__match_any_sync), with no block barrier between the steps.  One scan
+// over the warps of every digit then turns the warps' counts into offsets,
+// so each row's rank within the round is stable; the round's keys, staged in
+// shared memory, are written in digit order, consecutive threads on
+// consecutive output positions of a digit's run.  The CTA's cursors come
+// from a digit-major scan of per-CTA digit counts, so the whole pass is
+// stable.
 constexpr int kRTThreads = 512;
 constexpr int kRTWarps = kRTThreads / 32;
-constexpr int kRTWaves = 8;
-constexpr int kRTRound = kRTThreads * kRTWaves;  // 4096 rows a round
+constexpr int kRTSteps = 8;                       // 32-row steps of a warp per round
+constexpr int kRTPerWarp = 32 * kRTSteps;         // 256 rows
+constexpr int kRTRound = kRTWarps * kRTPerWarp;   // 4096 rows a round
 constexpr int kRTMaxBits = 8;
 static_assert(kRTRound <= 65536, "a round's row packs into 16 bits");
 
@@ -170,59 +175,55 @@ __global__ void __launch_bounds__(kRTThreads) round_scatter_kernel(IO io, int64_
   const uint32_t P = 1u << bits, mask = P - 1u;
   uint32_t* keys = rs;                   // kRTRound
   uint32_t* perm = keys + kRTRound;      // kRTRound: row | digit << 16 by sorted position
-  uint32_t* wcnt = perm + kRTRound;      // kRTWarps * P: a wave's counts, then prefixes
-  uint32_t* dcnt = wcnt + kRTWarps * P;  // P: the round's count of each digit so far
+  uint32_t* wrun = perm + kRTRound;      // kRTWarps * P: a warp's count of each digit, then offset
+  uint32_t* dcnt = wrun + kRTWarps * P;  // P: the round's count of each digit
   uint32_t* dstart = dcnt + P;           // P
   uint32_t* gpos = dstart + P;           // P
   uint32_t* cur = gpos + P;              // P: the CTA's output cursors
   __shared__ uint32_t s_warp[kRTWarps];
   const int t = threadIdx.x, lane = lane_id(), warp = warp_id();
   const unsigned lt = lanemask_lt();
-  for (uint32_t d = t; d < P; d += blockDim.x) {
-    cur[d] = cursors[(int64_t)d * gridDim.x + blockIdx.x];
-    dcnt[d] = 0u;
-  }
-  for (uint32_t i = t; i < (uint32_t)kRTWarps * P; i += blockDim.x) wcnt[i] = 0u;
+  for (uint32_t d = t; d < P; d += blockDim.x) cur[d] = cursors[(int64_t)d * gridDim.x + blockIdx.x];
+  for (uint32_t i = t; i < (uint32_t)kRTWarps * P; i += blockDim.x) wrun[i] = 0u;
   __syncthreads();
+  uint32_t* my = wrun + warp * P;
   const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(n, r0 + per);
   for (int64_t rr = r0; rr < r1; rr += kRTRound) {
     const int nt = (int)min((int64_t)kRTRound, r1 - rr);
+    uint32_t dj[kRTSteps], rk[kRTSteps];
 #pragma unroll
-    for (int j = 0; j < kRTWaves; ++j) {
-      const int i = j * kRTThreads + t;
-      if (i < nt) keys[i] = io.key(rr + i);
+    for (int j = 0; j < kRTSteps; ++j) {
+      const int i = warp * kRTPerWarp + j * 32 + lane;
+      const bool valid = i < nt;
+      uint32_t k = 0;
+      if (valid) {
+        k = io.key(rr + i);
+        keys[i] = k;
+      }
+      const uint32_t d = (k >> shift) & mask;
+      const unsigned act = __ballot_sync(kFullMask, valid);
+      dj[j] = d;
+      rk[j] = 0;
+      if (valid) {
+        const unsigned peers = __match_any_sync(act, d);
+        rk[j] = my[d] + __popc(peers & lt);
+        __syncwarp(act);
+        if (lane == __ffs(peers) - 1) my[d] += __popc(peers);
+      }
+      __syncwarp();
     }
     __syncthreads();
-    uint32_t dj[kRTWaves], rk[kRTWaves];
-#pragma unroll
-    for (int j = 0; j < kRTWaves; ++j) {
-      const int i = j * kRTThreads + t;
-      const bool valid = i < nt;
-      const uint32_t d = valid ? (keys[i] >> shift) & mask : 0u;
-      const unsigned act = __ballot_sync(kFullMask, valid);
-      unsigned peers = 0;
-      if (valid) {
-        peers = __match_any_sync(act, d);
-        if (lane == __ffs(peers) - 1) wcnt[warp * P + d] = __popc(peers);
+    // Offsets of the warps' rows of every digit (warp order is row order).
+    for (uint32_t d = t; d < P; d += blockDim.x) {
+      uint32_t run = 0;
+      for (int w = 0; w < kRTWarps; ++w) {
+        const uint32_t c = wrun[w * P + d];
+        wrun[w * P + d] = run;
+        run += c;
       }
-      __syncthreads();
-      // Warp-order prefix of every digit, after the digit's earlier waves.
-      for (uint32_t dd = t; dd < P; dd += blockDim.x) {
-        uint32_t run = dcnt[dd];
-        for (int w = 0; w < kRTWarps; ++w) {
-          const uint32_t c = wcnt[w * P + dd];
-          wcnt[w * P + dd] = run;
-          run += c;
-        }
-        dcnt[dd] = run;
-      }
-      __syncthreads();
-      dj[j] = d;
-      rk[j] = valid ? wcnt[warp * P + d] + __popc(peers & lt) : 0u;
-      __syncthreads();
-      for (uint32_t i2 = t; i2 < (uint32_t)kRTWarps * P; i2 += blockDim.x) wcnt[i2] = 0u;
-      __syncthreads();
+      dcnt[d] = run;
     }
+    __syncthreads();
     // Digit starts within the round (block scan of the P counts) and output
     // positions: sorted position k of digit d goes to gpos[d] + k.
     {
@@ -251,18 +252,18 @@ __global__ void __launch_bounds__(kRTThreads) round_scatter_kernel(IO io, int64_
         dstart[t] = ex;
         gpos[t] = cur[t] - ex;
         cur[t] += c;
-        dcnt[t] = 0u;
       }
       __syncthreads();
     }
 #pragma unroll
-    for (int j = 0; j < kRTWaves; ++j) {
-      const int i = j * kRTThreads + t;
-      if (i < nt) perm[dstart[dj[j]] + rk[j]] = (uint32_t)i | (dj[j] << 16);
+    for (int j = 0; j < kRTSteps; ++j) {
+      const int i = warp * kRTPerWarp + j * 32 + lane;
+      if (i < nt) perm[dstart[dj[j]] + my[dj[j]] + rk[j]] = (uint32_t)i | (dj[j] << 16);
     }
     __syncthreads();
+    for (uint32_t i = t; i < (uint32_t)kRTWarps * P; i += blockDim.x) wrun[i] = 0u;
 #pragma unroll
-    for (int j = 0; j < kRTWaves; ++j) {
+    for (int j = 0; j < kRTSteps; ++j) {
       const int k = j * kRTThreads + t;
       if (k < nt) {
         const uint32_t v = perm[k];
