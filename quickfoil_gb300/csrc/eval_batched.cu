@@ -941,10 +941,6 @@ __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
 }
 
 constexpr int kGatherWarps = 8;
-// Tiled path: entry records gathered by a kernel of their own (true) or read
-// by the evaluation kernel from the key tables while its tile's copies are
-// in flight (false).
-constexpr bool kGatherRecords = false;
 
 // One warp per unit: the item's literal-major entry space (offsets pair per
 // literal, warp scan), then the unit's entry records.
@@ -1061,10 +1057,6 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_total;
   __shared__ uint32_t s_abort;  // a bounded wait gave up: the CTA stops
-  // Entries read straight from the key tables (no gathered records): the
-  // item's literal-major entry space.
-  __shared__ uint32_t s_lstart[kMaxGroupLits + 1];
-  __shared__ uint32_t s_le0[kMaxGroupLits];
 
   for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) acc[i] = 0ull;
   for (int i = threadIdx.x; i < kSlots; i += blockDim.x) {
@@ -1111,10 +1103,10 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
       sub = threadIdx.x & (tpe - 1u);
     }
     const uint32_t j0 = pairs ? 2u * threadIdx.x : threadIdx.x / tpe;
-    const bool have = j0 < U.ecnt && (!a.records || U.eoff + U.ecnt <= a.entry_cap);
+    const bool have = j0 < U.ecnt && U.eoff + U.ecnt <= a.entry_cap;
     int2 e_k0 = make_int2(0, 0), e_kA = e_k0, e_kB = e_k0, e_mult = e_k0;
     uint2 e_meta = make_uint2(0u, 0u);
-    if (have && a.records) {
+    if (have) {
       const uint32_t r = U.eoff + j0;  // pairs: even, and the block is padded to a multiple of 4
       if (pairs) {
         e_k0 = __ldg(reinterpret_cast<const int2*>(a.rec.k0 + r));
@@ -1178,76 +1170,6 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         const int32_t* src = gcols + (int64_t)q * gn;
         int32_t* dst = raw + q * kTileStride + sp.s0;
         for (uint32_t g = lo; g < hi; ++g) dst[g - sp.g0] = __ldg(src + g);
-      }
-      if (t0 == 0 && !a.records) {
-        // The unit's entries straight from the key tables, while the tile's
-        // copies are in flight: warp 1 forms the item's literal-major entry
-        // space, then every thread reads its entries.
-        const GroupDesc& G = a.groups[U.group];
-        const int m = G.lit_end - G.lit_begin;
-        if (warp_id() == 1) {
-          const int lane = lane_id();
-          const int rshift = kRelPartitionBits - G.bits;
-          const uint32_t q0 = U.p << rshift, q1 = (U.p + 1) << rshift;
-          uint32_t run = 0;
-          for (int L0 = 0; L0 < m; L0 += 32) {
-            const int L = L0 + lane;
-            uint32_t c = 0;
-            if (L < m) {
-              const uint32_t* off = a.lits[G.lit_begin + L].offsets;
-              const uint32_t e0 = __ldg(off + q0);
-              c = __ldg(off + q1) - e0;
-              s_le0[L] = e0;
-            }
-            uint32_t x = c;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const uint32_t y = __shfl_up_sync(kFullMask, x, o);
-              if (lane >= o) x += y;
-            }
-            if (L < m) s_lstart[L] = run + x - c;
-            run += __shfl_sync(kFullMask, x, 31);
-          }
-          if (lane == 0) s_lstart[m] = run;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-          if (!(j == 0 ? have : (pairs && have && j0 + 1 < U.ecnt))) continue;
-          const uint32_t f = U.f0 + j0 + (uint32_t)j;
-          int lo = 0, hi = m - 1;  // largest L with s_lstart[L] <= f
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_lstart[mid] <= f) lo = mid; else hi = mid - 1;
-          }
-          const LitDesc& d = a.lits[G.lit_begin + lo];
-          const uint32_t e = s_le0[lo] + (f - s_lstart[lo]);
-          const int32_t k0 = __ldg(d.keys + e);
-          int32_t kA = 0, kB = 0;
-          uint32_t nchk = 0, colA = 0, colB = 0, ok0 = 1;
-          for (int q = 1; q < d.nk; ++q) {
-            const int ac = d.atom_col[q];
-            const int32_t kq = __ldg(d.keys + q * d.stride + e);
-            if (ac == 0) {
-              ok0 &= kq == k0 ? 1u : 0u;
-            } else {
-              if (nchk == 0) { kA = kq; colA = (uint32_t)ac; }
-              else if (nchk == 1) { kB = kq; colB = (uint32_t)ac; }
-              ++nchk;
-            }
-          }
-          if (nchk > 2) {
-            nchk = 3;
-            kA = (int32_t)e;
-          }
-          const int32_t mlt = __ldg(d.mult + e);
-          const uint32_t meta = (uint32_t)lo | (nchk << 8) | (ok0 << 10) | (colA << 12) | (colB << 16);
-          if (j == 0) {
-            e_k0.x = k0; e_kA.x = kA; e_kB.x = kB; e_mult.x = mlt; e_meta.x = meta;
-          } else {
-            e_k0.y = k0; e_kA.y = kA; e_kB.y = kB; e_mult.y = mlt; e_meta.y = meta;
-          }
-        }
       }
       {
         // Bounded wait for the bulk copies.  A wait that gives up flags the
@@ -2268,7 +2190,7 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     }
     ecap += 4 * cap;
     ecap = (ecap + 3) & ~int64_t(3);
-    if (mode == kModeStreamed || !kGatherRecords) ecap = 4;  // no entry records
+    if (mode == kModeStreamed) ecap = 4;  // no entry records
     if (cap > (int64_t)UINT32_MAX || ecap > (int64_t)UINT32_MAX)
       return set_error(ctx, QFG_ERR_INVALID, "too many work units");
     caps.push_back(cap);
@@ -2324,11 +2246,9 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     ea.counts = counts;
     ea.piece = piece;
     ea.row_chunk = L.streamed ? 0xffffffffu : 0u;  // streamed: a unit streams all its item's rows
-    // Tiled path: the evaluation kernel reads its entries from the key
-    // tables itself (kGatherRecords = false) or from records a gather
-    // kernel wrote before it.
-    ea.records = (!L.streamed && kGatherRecords) ? 1 : 0;
-    if (!ea.records) ea.entry_cap = 0xffffffffu;
+    // Tiled path: the evaluation kernel reads the entry records the gather
+    // kernel writes (coalesced, one round trip per unit).
+    ea.records = L.streamed ? 0 : 1;
     ea.max_cols = 1;
     for (size_t g = S.gbeg; g < S.gend; ++g) ea.max_cols = std::max(ea.max_cols, gdesc[g].ncols);
     int per_sm = 0;
@@ -2447,7 +2367,7 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
     entries += std::max<int64_t>(kt->num_entries, 1);
   }
   words += units * (int64_t)(sizeof(WorkUnit) / 4) +
-           ((mode == kModeStreamed || !kGatherRecords) ? 20 : 5 * (entries + 4 * units + 8));
+           (mode == kModeStreamed ? 20 : 5 * (entries + 4 * units + 8));
   *bytes = 4 * words + (int64_t)(sizeof(GroupDesc) + sizeof(LitDesc) + sizeof(SigDesc)) * n +
            32 * (int64_t)n;
   return QFG_OK;
@@ -2627,7 +2547,7 @@ extern "C" int qfg_step_traffic(qfg_ctx* c, const qfg_bindings* b, int32_t n,
       const int64_t ne = plan.tables[i]->num_entries;
       const int64_t tab = 4 * ne * (plan.tables[i]->num_keys + 1);
       bytes[QFG_STAGE_UNIT_PLAN] += 8 * ((int64_t)1 << bits);
-      if (mode == kModeStreamed || !kGatherRecords) {
+      if (mode == kModeStreamed) {
         bytes[QFG_STAGE_EVALUATE] += tab + 32;
       } else {
         bytes[QFG_STAGE_UNIT_PLAN] += tab + 20 * ne;
