@@ -726,17 +726,20 @@ bpart_pass2_kernel(const BPartArgs* __restrict__ A) {
 //                two further keys, multiplicity, literal and check columns)
 //                into its block, so the evaluation loads them with one
 //                coalesced round trip;
-//   eval         per unit (its record prefetched while the previous unit
-//                ran): the partition's binding rows arrive by cp.async while
-//                each thread loads its two entry records; a key table of the
+//   eval         per unit (its record loaded while the previous unit ran):
+//                each thread loads its entry records; the partition's
+//                binding rows arrive by cp.async copies of 16-byte chunks
+//                (one aligned run per column and label), shared by all
+//                threads and put in flight as soon as the previous tile had
+//                been probed, completing on an mbarrier; a key table of the
 //                tile is built with one 32-bit atomicCAS per new key, whose
 //                count atomics also give every row its rank within its key
-//                and label; for groups with atom literals a scan of the slot
-//                counts turns those ranks into per-key row lists (positives
-//                first); the entries probe the table and check the key's rows
-//                against their further keys; per-literal sums are combined
-//                with a segmented warp scan into per-CTA int64 accumulators,
-//                flushed to global memory when the CTA retires.
+//                and label; for groups with atom literals each key takes a
+//                run of the row list by a warp-aggregated atomic and its
+//                rows are placed there (positives first); the entries probe the table and check the
+//                key's rows against their further keys; per-literal sums are
+//                combined with a segmented warp scan into per-CTA int64
+//                accumulators, flushed to global memory when the CTA retires.
 
 struct GroupDesc {
   const int32_t* cols;      // ncols SoA partitioned columns, column stride n (a multiple of 4)
@@ -822,30 +825,44 @@ struct EvalArgs {
   int records;               // tiled path: units reserve entry records
 };
 
-// Shared-memory stride of a tile column: room for the alignment shifts of
-// the two segments (bulk copies keep shared and global addresses congruent
-// modulo 16 bytes).
-constexpr int kTileStride = kTile + 8;
+// Shared-memory stride of a tile column.  Each segment (positives,
+// negatives) arrives as the 16-byte chunks of the aligned run of global rows
+// that encloses it, so a segment's rows keep their global offset modulo
+// 4 and the negatives' run starts on the next 16-byte boundary after the
+// positives' run: at most 12 rows of padding per column.
+constexpr int kTileStride = kTile + 16;
 
 size_t eval_smem_bytes(int num_lits, int max_cols) {
-  return sizeof(unsigned long long) * 4 * (size_t)num_lits +
-         sizeof(int32_t) * (size_t)max_cols * kTileStride + sizeof(uint32_t) * 3 * kSlots +
+  return sizeof(unsigned long long) * 4 * (size_t)num_lits + sizeof(uint32_t) * 2 * kSlots +
+         sizeof(int32_t) * (size_t)max_cols * kTileStride + sizeof(uint16_t) * kSlots +
          sizeof(uint16_t) * 4 * kTile;
 }
 
-// One segment of a tile column: global rows [g0, g0 + c) to shared index
-// s0 (s0 = g0 modulo 4).  Its 16-byte aligned body goes by one bulk copy;
-// the unaligned head and tail (at most 3 rows each, or all of a short
-// segment) by plain loads.
-struct SegPiece {
-  uint32_t g0, c, s0;
-  __device__ __forceinline__ uint32_t body_lo() const { return (g0 + 3u) & ~3u; }
-  __device__ __forceinline__ uint32_t body_hi() const { return (g0 + c) & ~3u; }
-  __device__ __forceinline__ bool has_body() const { return c > 0 && body_hi() > body_lo(); }
-  __device__ __forceinline__ uint32_t body_bytes() const {
-    return has_body() ? 4u * (body_hi() - body_lo()) : 0u;
-  }
+// Where one tile of a work unit lies: rows [t0, t0 + nt) of the unit's
+// positives-then-negatives order, npos of them positive.  Global rows
+// [gP, gP + npos) and [gN, gN + nt - npos) of every carried column; in shared
+// memory a positive row i sits at shP + i and a negative row i at
+// baseN + (i - npos).  bytesP / bytesN: the two aligned runs per column,
+// landing at shared index 0 and aN.
+struct TileGeo {
+  uint32_t nt, npos, gP, gN, shP, aN, baseN, bytesP, bytesN;
 };
+
+__device__ __forceinline__ TileGeo tile_geo(const WorkUnit& U, uint32_t t0) {
+  TileGeo g;
+  const uint32_t total = U.Pp + U.Np;
+  g.nt = umin((uint32_t)kTile, total - t0);
+  g.npos = umin(g.nt, U.Pp > t0 ? U.Pp - t0 : 0u);
+  const uint32_t cN = g.nt - g.npos;
+  g.gP = U.ps + t0;
+  g.gN = U.ns + (t0 > U.Pp ? t0 - U.Pp : 0u);
+  g.shP = g.npos > 0u ? (g.gP & 3u) : 0u;
+  g.bytesP = g.npos > 0u ? 4u * (((g.gP + g.npos + 3u) & ~3u) - (g.gP & ~3u)) : 0u;
+  g.aN = g.npos > 0u ? ((g.shP + g.npos + 3u) & ~3u) : 0u;
+  g.baseN = g.aN + (g.gN & 3u);
+  g.bytesN = cN > 0u ? 4u * (((g.gN + cN + 3u) & ~3u) - (g.gN & ~3u)) : 0u;
+  return g;
+}
 
 __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
   const int lane = lane_id();
@@ -1042,51 +1059,84 @@ __device__ __forceinline__ void flush_acc(unsigned long long* dst, long long cp,
 __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem);
-  int32_t* raw = reinterpret_cast<int32_t*>(acc + 4 * a.num_lits);   // max_cols * kTileStride
-  uint32_t* owner = reinterpret_cast<uint32_t*>(raw + a.max_cols * kTileStride);  // kSlots
-  uint32_t* cnt = owner + kSlots;                                     // kSlots
-  uint32_t* sstart = cnt + kSlots;                                    // kSlots
-  uint16_t* rslot = reinterpret_cast<uint16_t*>(sstart + kSlots);     // kTile
-  uint16_t* rrank = rslot + kTile;                                    // kTile
-  uint16_t* rows = rrank + kTile;                                     // kTile: shared positions
+  uint32_t* owner = reinterpret_cast<uint32_t*>(acc + 4 * a.num_lits);   // kSlots
+  uint32_t* cnt = owner + kSlots;                                         // kSlots
+  int32_t* raw = reinterpret_cast<int32_t*>(cnt + kSlots);                // max_cols * kTileStride
+  uint16_t* sstart = reinterpret_cast<uint16_t*>(raw + a.max_cols * kTileStride);  // kSlots
+  uint16_t* rslot = sstart + kSlots;                                      // kTile
+  uint16_t* rrank = rslot + kTile;                                        // kTile
+  uint16_t* rows = rrank + kTile;                                         // kTile: shared positions
   uint16_t* klist = rows + kTile;  // kTile: the slots of the tile's distinct keys, in claim order
   __shared__ __align__(8) uint64_t s_bar;
-  __shared__ WorkUnit s_unit;
-  __shared__ uint32_t s_idx, s_count;
-  __shared__ uint32_t s_nkeys;  // distinct keys of the current tile (entries of klist)
-  __shared__ uint32_t s_warp[32];
-  __shared__ uint32_t s_total;
-  __shared__ uint32_t s_abort;  // a bounded wait gave up: the CTA stops
+  __shared__ WorkUnit s_unit[2];  // the current unit and the next (by unit parity)
+  __shared__ uint32_t s_uidx[2];
+  __shared__ uint32_t s_count;
+  __shared__ uint32_t s_nkeys[2];  // distinct keys of a tile (entries of klist), by tile parity
+  __shared__ uint32_t s_alloc;     // row-list space handed out in the current tile
+  __shared__ uint32_t s_abort;     // a bounded wait gave up: the CTA stops
 
   for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) acc[i] = 0ull;
   for (int i = threadIdx.x; i < kSlots; i += blockDim.x) {
     owner[i] = 0u;
     cnt[i] = 0u;
   }
+
+  // Every thread copies its share of a tile's 16-byte chunks (every
+  // column: the positives' run, then the negatives' run) and arrives on the
+  // tile barrier once its copies have landed.  The caller has passed a
+  // barrier after the last reads of the tile buffer.
+  auto copy_tile = [&](const WorkUnit& V, uint32_t t0) {
+    if (a.withhold_copies) return;  // tests of the bounded wait: no copy, no arrival
+    const TileGeo g = tile_geo(V, t0);
+    const uint32_t cP = g.bytesP >> 4, per = cP + (g.bytesN >> 4);
+    const uint32_t chunks = per * (V.flags & 0xffu);
+    for (uint32_t c = threadIdx.x; c < chunks; c += kEvalThreads) {
+      const uint32_t q = c / per, r = c - q * per;
+      const int32_t* col = V.cols + (int64_t)q * V.stride;
+      int32_t* dst = raw + q * kTileStride;
+      if (r < cP)
+        cp_async16(dst + 4u * r, col + (g.gP & ~3u) + 4u * r);
+      else
+        cp_async16(dst + g.aN + 4u * (r - cP), col + (g.gN & ~3u) + 4u * (r - cP));
+    }
+    cp_async_mbar_arrive_noinc(&s_bar);
+  };
+
+  uint32_t ahead = 0;  // thread 0: the index claimed for the unit after the next
   if (threadIdx.x == 0) {
-    s_nkeys = 0u;
+    s_nkeys[0] = s_nkeys[1] = 0u;
+    s_alloc = 0u;
     s_abort = 0u;
     s_count = umin(a.unit_count[0], a.unit_cap);
-    s_idx = atomicAdd(a.work_counter, 1u);
-    if (s_idx < s_count) s_unit = a.units[s_idx];
-    mbar_init(&s_bar, 1);
+    s_uidx[0] = atomicAdd(a.work_counter, 1u);
+    if (s_uidx[0] < s_count) {
+      s_unit[0] = a.units[s_uidx[0]];
+      ahead = atomicAdd(a.work_counter, 1u);
+    } else {
+      ahead = s_count;
+    }
+    mbar_init(&s_bar, kEvalThreads);
     fence_mbar_init();
   }
   __syncthreads();
-  uint32_t phase = 0;
+  if (s_uidx[0] < s_count) copy_tile(s_unit[0], 0u);
+  uint32_t phase = 0, tp = 0, cur = 0;
 
   for (;;) {
-    const uint32_t idx = s_idx;
-    if (idx >= s_count) break;
-    const WorkUnit U = s_unit;
-    // The next unit's index is claimed now and its record loaded after the
-    // key table is built, so neither wait sits on this unit's path.
+    if (s_uidx[cur] >= s_count) break;
+    const WorkUnit U = s_unit[cur];
+    // Thread 0 loads the next unit's record now (published before the
+    // first key table of this unit is complete) and claims the unit after
+    // it, whose index is first needed one unit later.
     uint32_t nidx = 0;
     WorkUnit nu{};
-    if (threadIdx.x == 0) nidx = atomicAdd(a.work_counter, 1u);
-    const int32_t* __restrict__ gcols = U.cols;
-    const int64_t gn = U.stride;
-    const int ncols = (int)(U.flags & 0xffu);
+    if (threadIdx.x == 0) {
+      nidx = ahead;
+      if (nidx < s_count) {
+        nu = a.units[nidx];
+        ahead = atomicAdd(a.work_counter, 1u);
+      }
+    }
     const int lit_begin = (int)U.lit_begin;
     const bool has_atoms = (U.flags & 0x100u) != 0u;
     const uint32_t total = U.Pp + U.Np;
@@ -1127,57 +1177,16 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     long long bp = 0, bn = 0, cp = 0, cn = 0;
     int Lrun = -1;
     for (uint32_t t0 = 0; t0 < total; t0 += kTile) {
-      const int nt = (int)umin((uint32_t)kTile, total - t0);
-      const int npos = (int)umin((uint32_t)nt, U.Pp > t0 ? U.Pp - t0 : 0u);
-      // The tile's two segments (positives, negatives) of every carried
-      // column: row i sits at shared index i + shP (positives) or baseN +
-      // (i - npos) (negatives), congruent to its global row modulo 4.
-      SegPiece seg[2];
-      seg[0].g0 = U.ps + t0;
-      seg[0].c = (uint32_t)npos;
-      seg[0].s0 = seg[0].g0 & 3u;
-      seg[1].g0 = U.ns + (t0 > U.Pp ? t0 - U.Pp : 0u);
-      seg[1].c = (uint32_t)(nt - npos);
-      seg[1].s0 = seg[0].s0 + (uint32_t)npos + ((seg[1].g0 - (seg[0].s0 + (uint32_t)npos)) & 3u);
-      const uint32_t shP = seg[0].s0, baseN = seg[1].s0;
-      if (threadIdx.x == 0) {
-        fence_proxy_async_smem();  // this tile's copies come after all earlier reads of the buffer
-        const uint32_t tx = (uint32_t)ncols * (seg[0].body_bytes() + seg[1].body_bytes());
-        if (a.withhold_copies) {
-          // Tests of the bounded wait: bytes announced that never arrive.
-          mbar_arrive_expect_tx(&s_bar, tx > 0u ? tx : 16u);
-        } else {
-          mbar_arrive_expect_tx(&s_bar, tx);
-          for (int q = 0; q < ncols; ++q)
-            for (int k = 0; k < 2; ++k)
-              if (seg[k].has_body())
-                bulk_g2s(raw + q * kTileStride + seg[k].s0 + (seg[k].body_lo() - seg[k].g0),
-                         gcols + (int64_t)q * gn + seg[k].body_lo(), seg[k].body_bytes(), &s_bar);
-        }
-      }
-      if ((int)threadIdx.x < 4 * ncols) {
-        // Unaligned heads and tails: (column, segment, head or tail) per thread.
-        const int q = threadIdx.x >> 2, k = (threadIdx.x >> 1) & 1, tail = threadIdx.x & 1;
-        const SegPiece& sp = seg[k];
-        uint32_t lo, hi;
-        if (!sp.has_body()) {
-          lo = tail ? sp.g0 : sp.g0;
-          hi = tail ? sp.g0 : sp.g0 + sp.c;
-        } else {
-          lo = tail ? sp.body_hi() : sp.g0;
-          hi = tail ? sp.g0 + sp.c : sp.body_lo();
-        }
-        const int32_t* src = gcols + (int64_t)q * gn;
-        int32_t* dst = raw + q * kTileStride + sp.s0;
-        for (uint32_t g = lo; g < hi; ++g) dst[g - sp.g0] = __ldg(src + g);
-      }
+      const TileGeo g = tile_geo(U, t0);
+      const int nt = (int)g.nt, npos = (int)g.npos;
+      const uint32_t shP = g.shP, baseN = g.baseN;
       {
-        // Bounded wait for the bulk copies.  A wait that gives up flags the
-        // context, waits once more (bounded) for copies still in flight, so
-        // that none lands after the CTA has stopped, and stops the CTA: all
-        // threads leave the unit loop after the barrier below, nothing is
-        // flushed, and the call reports QFG_ERR_TIMEOUT.  (Should the second
-        // wait give up too, the CTA stops all the same.)
+        // Bounded wait for the tile's copies.  A wait that gives up flags
+        // the context, waits once more (bounded) for copies still in
+        // flight, so that none lands after the CTA has stopped, and stops
+        // the CTA: all threads leave the unit loop after the barrier below,
+        // nothing is flushed, and the call reports QFG_ERR_TIMEOUT.  (Should
+        // the second wait give up too, the CTA stops all the same.)
         int64_t it = 0;
         while (!mbar_try_wait(&s_bar, phase)) {
           if (++it > a.wait_limit) {
@@ -1192,6 +1201,8 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
       }
       __syncthreads();
       if (s_abort != 0u) break;
+      // The other parity's key count was last read before this barrier.
+      if (threadIdx.x == 0) s_nkeys[tp ^ 1u] = 0u;
       // Distinct join keys of the tile: owner = first row + 1, claimed by
       // CAS; the count atomics return each row's rank within its key and
       // label (positive count low half, negative count high half).
@@ -1203,47 +1214,54 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         for (int probe = 0; probe < kSlots; ++probe) {
           const uint32_t o = atomicCAS(&owner[slot], 0u, pos + 1u);
           if (o == 0u) {
-            klist[atomicAdd(&s_nkeys, 1u)] = (uint16_t)slot;
+            klist[atomicAdd(&s_nkeys[tp], 1u)] = (uint16_t)slot;
             break;
           }
           if (raw[o - 1u] == key) break;
           slot = (slot + 1) & (kSlots - 1);
         }
         const uint32_t old = atomicAdd(&cnt[slot], posr ? 1u : 0x10000u);
-        rslot[i] = (uint16_t)slot;
-        rrank[i] = (uint16_t)(posr ? (old & 0xffffu) : (old >> 16));
-      }
-      if (threadIdx.x == 0 && t0 == 0 && nidx < s_count) nu = a.units[nidx];
-      __syncthreads();
-      {
-        // Owners become keys (probes compare keys directly); with atom
-        // literals, slot starts for per-key row lists, positives first.
-        // Only the claimed slots are visited: each thread takes a run of
-        // consecutive entries of the key list.
-        const uint32_t nk = s_nkeys;
-        const uint32_t per = (nk + kEvalThreads - 1u) / kEvalThreads;
-        const uint32_t d0 = umin(nk, threadIdx.x * per), d1 = umin(nk, d0 + per);
         if (has_atoms) {
-          uint32_t sum = 0;
-          for (uint32_t d = d0; d < d1; ++d) {
-            const uint32_t w = cnt[klist[d]];
-            sum += (w & 0xffffu) + (w >> 16);
-          }
-          uint32_t run = block_scan_excl(sum, s_warp, &s_total);
-          for (uint32_t d = d0; d < d1; ++d) {
-            const uint32_t sl = klist[d];
-            const uint32_t w = cnt[sl];
-            sstart[sl] = run;
-            run += (w & 0xffffu) + (w >> 16);
-          }
+          rslot[i] = (uint16_t)slot;
+          rrank[i] = (uint16_t)(posr ? (old & 0xffffu) : (old >> 16));
         }
-        for (uint32_t d = d0; d < d1; ++d) {
-          const uint32_t sl = klist[d];
-          owner[sl] = (uint32_t)raw[owner[sl] - 1u];
+      }
+      if (threadIdx.x == 0 && t0 == 0) {
+        s_uidx[cur ^ 1u] = nidx;
+        if (nidx < s_count) s_unit[cur ^ 1u] = nu;
+      }
+      __syncthreads();
+      const uint32_t nk = s_nkeys[tp];
+      {
+        // Owners become keys (probes compare keys directly).  With atom
+        // literals each key also takes the run of the row list for its
+        // rows by a warp-aggregated atomic (the runs' order is free).
+        for (uint32_t d0 = 0; d0 < nk; d0 += blockDim.x) {
+          const uint32_t d = d0 + threadIdx.x;
+          uint32_t c = 0, sl = 0;
+          if (d < nk) {
+            sl = klist[d];
+            const uint32_t w = cnt[sl];
+            c = (w & 0xffffu) + (w >> 16);
+            owner[sl] = (uint32_t)raw[owner[sl] - 1u];
+          }
+          if (has_atoms) {
+            uint32_t x = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const uint32_t y = __shfl_up_sync(kFullMask, x, o);
+              if (lane_id() >= o) x += y;
+            }
+            uint32_t base = 0;
+            if (lane_id() == 31 && x > 0u) base = atomicAdd(&s_alloc, x);
+            base = __shfl_sync(kFullMask, base, 31);
+            if (d < nk) sstart[sl] = (uint16_t)(base + x - c);
+          }
         }
       }
       __syncthreads();
       if (has_atoms) {
+        if (threadIdx.x == 0) s_alloc = 0u;  // last used above; next used after the next tile's wait
         for (int i = threadIdx.x; i < nt; i += blockDim.x) {
           const int sl = rslot[i];
           const bool posr = i < npos;
@@ -1288,8 +1306,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
           if (nchk == 1) {
             const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
             for (uint32_t x = beg + sub; x < mid; x += tpe) hp += ca[rows[x]] == kA;
-            for (uint32_t x = mid + sub; x < end; x += tpe)
-              hn += ca[rows[x]] == kA;
+            for (uint32_t x = mid + sub; x < end; x += tpe) hn += ca[rows[x]] == kA;
           } else if (nchk == 2) {
             const int32_t kB = j == 0 ? e_kB.x : e_kB.y;
             const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
@@ -1326,16 +1343,20 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         cn += hn;
       }
       __syncthreads();
-      {
-        const uint32_t nk = s_nkeys;
-        for (uint32_t d = threadIdx.x; d < nk; d += blockDim.x) {
-          const uint32_t sl = klist[d];
-          owner[sl] = 0u;
-          cnt[sl] = 0u;
-        }
+      // The tile's slots are cleared and the tile buffer refilled -- the
+      // next tile of this unit, or the first tile of the next unit -- with
+      // no further barrier: the next key table is built after the next
+      // tile's wait and barrier.
+      for (uint32_t d = threadIdx.x; d < nk; d += blockDim.x) {
+        const uint32_t sl = klist[d];
+        owner[sl] = 0u;
+        cnt[sl] = 0u;
       }
-      __syncthreads();
-      if (threadIdx.x == 0) s_nkeys = 0u;  // read by every thread above; next read after a barrier
+      if (t0 + (uint32_t)kTile < total)
+        copy_tile(U, t0 + (uint32_t)kTile);
+      else if (s_uidx[cur ^ 1u] < s_count)
+        copy_tile(s_unit[cur ^ 1u], 0u);
+      tp ^= 1u;
     }
     if (s_abort != 0u) break;  // read after the barrier that follows the wait
     // Threads' entries are contiguous and increasing, so equal literals sit
@@ -1348,11 +1369,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     const bool seg_end = lane_id() == 31 || next_L != Lrun;
     if (seg_end && Lrun >= 0 && (cp | cn | bp | bn) != 0)
       flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
-    if (threadIdx.x == 0) {
-      s_idx = nidx;
-      if (nidx < s_count) s_unit = nu;
-    }
-    __syncthreads();
+    cur ^= 1u;  // the next unit's index and record were published before a barrier of this unit
   }
   __syncthreads();
   if (s_abort != 0u) return;
