@@ -1056,6 +1056,39 @@ __device__ __forceinline__ void flush_acc(unsigned long long* dst, long long cp,
   if (bn) atomicAdd(dst + 3, as_ull(bn));
 }
 
+constexpr int kRowsPerThread = kTile / kEvalThreads;
+constexpr int kInsertBatch = 5;  // rows of a thread whose key-table inserts overlap
+static_assert(kTile % kEvalThreads == 0, "a tile is whole rows per thread");
+
+// Rows x = b, b + step, ... < e of a key's row list whose column value
+// equals k (four rows' loads in flight at a time).
+__device__ __forceinline__ uint32_t count_matches1(const uint16_t* rows, const int32_t* c, int32_t k,
+                                                   uint32_t b, uint32_t e, uint32_t step) {
+  uint32_t h = 0, x = b;
+  for (; x + 3u * step < e; x += 4u * step) {
+    const int r0 = rows[x], r1 = rows[x + step], r2 = rows[x + 2u * step], r3 = rows[x + 3u * step];
+    h += (uint32_t)(c[r0] == k) + (uint32_t)(c[r1] == k) + (uint32_t)(c[r2] == k) + (uint32_t)(c[r3] == k);
+  }
+  for (; x < e; x += step) h += c[rows[x]] == k;
+  return h;
+}
+
+// The same with two columns, both of which must match.
+__device__ __forceinline__ uint32_t count_matches2(const uint16_t* rows, const int32_t* ca,
+                                                   const int32_t* cb, int32_t ka, int32_t kb,
+                                                   uint32_t b, uint32_t e, uint32_t step) {
+  uint32_t h = 0, x = b;
+  for (; x + 1u * step < e; x += 2u * step) {
+    const int r0 = rows[x], r1 = rows[x + step];
+    h += (uint32_t)((ca[r0] == ka) & (cb[r0] == kb)) + (uint32_t)((ca[r1] == ka) & (cb[r1] == kb));
+  }
+  for (; x < e; x += step) {
+    const int r = rows[x];
+    h += (uint32_t)((ca[r] == ka) & (cb[r] == kb));
+  }
+  return h;
+}
+
 __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem);
@@ -1068,7 +1101,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
   uint16_t* rows = rrank + kTile;                                         // kTile: shared positions
   uint16_t* klist = rows + kTile;  // kTile: the slots of the tile's distinct keys, in claim order
   __shared__ __align__(8) uint64_t s_bar;
-  __shared__ WorkUnit s_unit[2];  // the current unit and the next (by unit parity)
+  __shared__ __align__(16) WorkUnit s_unit[2];  // the current unit and the next (by unit parity)
   __shared__ uint32_t s_uidx[2];
   __shared__ uint32_t s_count;
   __shared__ uint32_t s_nkeys[2];  // distinct keys of a tile (entries of klist), by tile parity
@@ -1124,18 +1157,14 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
 
   for (;;) {
     if (s_uidx[cur] >= s_count) break;
-    const WorkUnit U = s_unit[cur];
-    // Thread 0 loads the next unit's record now (published before the
-    // first key table of this unit is complete) and claims the unit after
-    // it, whose index is first needed one unit later.
+    const WorkUnit& U = s_unit[cur];
+    // Thread 0 claims the unit after the next one now (its index is first
+    // needed one unit later); the next unit's record is copied into shared
+    // memory while this unit's first key table is built.
     uint32_t nidx = 0;
-    WorkUnit nu{};
     if (threadIdx.x == 0) {
       nidx = ahead;
-      if (nidx < s_count) {
-        nu = a.units[nidx];
-        ahead = atomicAdd(a.work_counter, 1u);
-      }
+      if (nidx < s_count) ahead = atomicAdd(a.work_counter, 1u);
     }
     const int lit_begin = (int)U.lit_begin;
     const bool has_atoms = (U.flags & 0x100u) != 0u;
@@ -1201,35 +1230,75 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
       }
       __syncthreads();
       if (s_abort != 0u) break;
-      // The other parity's key count was last read before this barrier.
-      if (threadIdx.x == 0) s_nkeys[tp ^ 1u] = 0u;
+      // The other parity's key count and unit record were last read before
+      // this barrier.
+      if (threadIdx.x == 0) {
+        s_nkeys[tp ^ 1u] = 0u;
+        if (t0 == 0) {
+          s_uidx[cur ^ 1u] = nidx;
+          if (nidx < s_count) {
+            const int32_t* src = reinterpret_cast<const int32_t*>(a.units + nidx);
+            int32_t* dst = reinterpret_cast<int32_t*>(&s_unit[cur ^ 1u]);
+#pragma unroll
+            for (int q = 0; q < (int)(sizeof(WorkUnit) / 16); ++q) cp_async16(dst + 4 * q, src + 4 * q);
+          }
+        }
+      }
       // Distinct join keys of the tile: owner = first row + 1, claimed by
       // CAS; the count atomics return each row's rank within its key and
-      // label (positive count low half, negative count high half).
-      for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-        const bool posr = i < npos;
-        const uint32_t pos = posr ? (uint32_t)i + shP : baseN + (uint32_t)(i - npos);
-        const int32_t key = raw[pos];
-        uint32_t slot = mix32((uint32_t)key) & (kSlots - 1);
-        for (int probe = 0; probe < kSlots; ++probe) {
-          const uint32_t o = atomicCAS(&owner[slot], 0u, pos + 1u);
-          if (o == 0u) {
-            klist[atomicAdd(&s_nkeys[tp], 1u)] = (uint16_t)slot;
-            break;
+      // label (positive count low half, negative count high half).  A
+      // thread's rows go through each step in batches of kInsertBatch, so
+      // their shared-memory round trips overlap: keys, the owners of their
+      // home slots, the owners' keys; only a row whose home slot is free or
+      // holds another key takes the probe loop with CAS.
+      for (int k0 = 0; k0 < kRowsPerThread; k0 += kInsertBatch) {
+        int32_t key[kInsertBatch];
+        uint32_t slot[kInsertBatch], own[kInsertBatch];
+#pragma unroll
+        for (int k = 0; k < kInsertBatch; ++k) {
+          const int i = (int)threadIdx.x + (k0 + k) * kEvalThreads;
+          const uint32_t pos = i < npos ? (uint32_t)i + shP : baseN + (uint32_t)(i - npos);
+          key[k] = i < nt ? raw[pos] : 0;
+          slot[k] = mix32((uint32_t)key[k]) & (kSlots - 1);
+        }
+#pragma unroll
+        for (int k = 0; k < kInsertBatch; ++k) own[k] = owner[slot[k]];
+#pragma unroll
+        for (int k = 0; k < kInsertBatch; ++k) {
+          const int i = (int)threadIdx.x + (k0 + k) * kEvalThreads;
+          if (i >= nt) continue;
+          if (own[k] != 0u && raw[own[k] - 1u] == key[k]) continue;  // the key's home slot
+          const uint32_t pos = i < npos ? (uint32_t)i + shP : baseN + (uint32_t)(i - npos);
+          uint32_t sl = slot[k];
+          for (int probe = 0; probe < kSlots; ++probe) {
+            const uint32_t o = atomicCAS(&owner[sl], 0u, pos + 1u);
+            if (o == 0u) {
+              klist[atomicAdd(&s_nkeys[tp], 1u)] = (uint16_t)sl;
+              break;
+            }
+            if (raw[o - 1u] == key[k]) break;
+            sl = (sl + 1) & (kSlots - 1);
           }
-          if (raw[o - 1u] == key) break;
-          slot = (slot + 1) & (kSlots - 1);
+          slot[k] = sl;
         }
-        const uint32_t old = atomicAdd(&cnt[slot], posr ? 1u : 0x10000u);
+        uint32_t old[kInsertBatch];
+#pragma unroll
+        for (int k = 0; k < kInsertBatch; ++k) {
+          const int i = (int)threadIdx.x + (k0 + k) * kEvalThreads;
+          old[k] = i < nt ? atomicAdd(&cnt[slot[k]], i < npos ? 1u : 0x10000u) : 0u;
+        }
         if (has_atoms) {
-          rslot[i] = (uint16_t)slot;
-          rrank[i] = (uint16_t)(posr ? (old & 0xffffu) : (old >> 16));
+#pragma unroll
+          for (int k = 0; k < kInsertBatch; ++k) {
+            const int i = (int)threadIdx.x + (k0 + k) * kEvalThreads;
+            if (i < nt) {
+              rslot[i] = (uint16_t)slot[k];
+              rrank[i] = (uint16_t)(i < npos ? (old[k] & 0xffffu) : (old[k] >> 16));
+            }
+          }
         }
       }
-      if (threadIdx.x == 0 && t0 == 0) {
-        s_uidx[cur ^ 1u] = nidx;
-        if (nidx < s_count) s_unit[cur ^ 1u] = nu;
-      }
+      if (threadIdx.x == 0 && t0 == 0) cp_async_wait_all();  // the next unit's record
       __syncthreads();
       const uint32_t nk = s_nkeys[tp];
       {
@@ -1262,11 +1331,23 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
       __syncthreads();
       if (has_atoms) {
         if (threadIdx.x == 0) s_alloc = 0u;  // last used above; next used after the next tile's wait
-        for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-          const int sl = rslot[i];
-          const bool posr = i < npos;
-          const uint32_t off = posr ? rrank[i] : (cnt[sl] & 0xffffu) + rrank[i];
-          rows[sstart[sl] + off] = (uint16_t)(posr ? (uint32_t)i + shP : baseN + (uint32_t)(i - npos));
+        // All of a thread's loads first, then its stores (the shared arrays
+        // may alias as far as the compiler knows).
+        uint32_t dst[kRowsPerThread];
+#pragma unroll
+        for (int k = 0; k < kRowsPerThread; ++k) {
+          const int i = (int)threadIdx.x + k * kEvalThreads;
+          dst[k] = 0u;
+          if (i < nt) {
+            const int sl = rslot[i];
+            const uint32_t rk = rrank[i];
+            dst[k] = (uint32_t)sstart[sl] + (i < npos ? rk : (cnt[sl] & 0xffffu) + rk);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < kRowsPerThread; ++k) {
+          const int i = (int)threadIdx.x + k * kEvalThreads;
+          if (i < nt) rows[dst[k]] = (uint16_t)(i < npos ? (uint32_t)i + shP : baseN + (uint32_t)(i - npos));
         }
         __syncthreads();
       }
@@ -1305,20 +1386,14 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
           const int32_t kA = j == 0 ? e_kA.x : e_kA.y;
           if (nchk == 1) {
             const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
-            for (uint32_t x = beg + sub; x < mid; x += tpe) hp += ca[rows[x]] == kA;
-            for (uint32_t x = mid + sub; x < end; x += tpe) hn += ca[rows[x]] == kA;
+            hp = count_matches1(rows, ca, kA, beg + sub, mid, tpe);
+            hn = count_matches1(rows, ca, kA, mid + sub, end, tpe);
           } else if (nchk == 2) {
             const int32_t kB = j == 0 ? e_kB.x : e_kB.y;
             const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
             const int32_t* cb = raw + ((meta >> 16) & 7u) * kTileStride;
-            for (uint32_t x = beg + sub; x < mid; x += tpe) {
-              const int r = rows[x];
-              hp += (ca[r] == kA) & (cb[r] == kB);
-            }
-            for (uint32_t x = mid + sub; x < end; x += tpe) {
-              const int r = rows[x];
-              hn += (ca[r] == kA) & (cb[r] == kB);
-            }
+            hp = count_matches2(rows, ca, cb, kA, kB, beg + sub, mid, tpe);
+            hn = count_matches2(rows, ca, cb, kA, kB, mid + sub, end, tpe);
           } else {
             // More than two checked columns: keys from the key table.
             const LitDesc& d = a.lits[lit_begin + L];
