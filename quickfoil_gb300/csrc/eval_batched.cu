@@ -43,11 +43,12 @@ namespace {
 constexpr int kTile = 1280;            // binding rows per shared-memory tile
 constexpr int kTargetRows = 1024;      // partition bits keep the mean partition below this
 constexpr int kSlots = 2048;           // key-table slots (power of two > kTile)
-constexpr int kEvalThreads = 256;
+constexpr int kEvalThreads = 288;     // evaluation block: eight consumer warps and one producer warp
+constexpr int kConsumers = kEvalThreads - 32;
 constexpr int kGroupCols = QFG_MAX_ARITY;  // join column + up to 7 atom columns
 constexpr int kMaxLitsPerLaunch = 512;
-constexpr int kChunk = 2 * kEvalThreads;     // relation entries per work unit: two per thread
-constexpr int kMaxGroupLits = kEvalThreads;  // one thread per literal in the per-item prefix
+constexpr int kChunk = 2 * kConsumers;       // relation entries per work unit: two per consumer
+constexpr int kMaxGroupLits = 256;  // literals of one group (one thread each in a per-item prefix)
 constexpr int kPartThreads = 1024;
 constexpr int kDefaultCoarseBits = 7;  // pass 1 fan-out: 2 << 7 = 256 bins (hash prefix, label)
 constexpr int kMaxCoarseBits = 8;      // at most 512 pass-1 bins
@@ -56,7 +57,7 @@ constexpr int kMaxSinglePassBits = 8;  // one pass up to 2 << 8 = 512 bins
 constexpr int kMaxPartitionBits = 16;
 static_assert(kMaxPartitionBits <= kRelPartitionBits, "relation bins must refine binding bins");
 static_assert(kMaxPartitionBits <= kMaxCoarseBits + kMaxSubBits, "two passes reach every bit count");
-static_assert(kSlots % kEvalThreads == 0 && kSlots > kTile, "slot table shape");
+static_assert(kSlots > kTile, "slot table shape");
 
 // ----------------------------------------------------------------------------
 // Relation key tables.
@@ -1056,9 +1057,14 @@ __device__ __forceinline__ void flush_acc(unsigned long long* dst, long long cp,
   if (bn) atomicAdd(dst + 3, as_ull(bn));
 }
 
-constexpr int kRowsPerThread = kTile / kEvalThreads;
+constexpr int kRowsPerThread = kTile / kConsumers;
 constexpr int kInsertBatch = 5;  // rows of a thread whose key-table inserts overlap
-static_assert(kTile % kEvalThreads == 0, "a tile is whole rows per thread");
+static_assert(kTile % kConsumers == 0, "a tile is whole rows per consumer thread");
+
+// Barrier of the consumer warps only (the producer warp never joins it).
+__device__ __forceinline__ void consumer_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
+}
 
 // Rows x = b, b + step, ... < e of a key's row list whose column value
 // equals k (four rows' loads in flight at a time).
@@ -1100,9 +1106,11 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
   uint16_t* rrank = rslot + kTile;                                        // kTile
   uint16_t* rows = rrank + kTile;                                         // kTile: shared positions
   uint16_t* klist = rows + kTile;  // kTile: the slots of the tile's distinct keys, in claim order
-  __shared__ __align__(8) uint64_t s_bar;
-  __shared__ __align__(16) WorkUnit s_unit[2];  // the current unit and the next (by unit parity)
-  __shared__ uint32_t s_uidx[2];
+  __shared__ __align__(8) uint64_t s_full;    // a tile (or the end mark) is in the buffer
+  __shared__ __align__(8) uint64_t s_empty;   // the consumers are done with the buffer
+  __shared__ __align__(8) uint64_t s_rec[3];  // a unit record (or the end mark) is published
+  __shared__ __align__(16) WorkUnit s_unit[3];  // unit records, by unit index modulo 3
+  __shared__ uint32_t s_uidx[3];
   __shared__ uint32_t s_count;
   __shared__ uint32_t s_nkeys[2];  // distinct keys of a tile (entries of klist), by tile parity
   __shared__ uint32_t s_alloc;     // row-list space handed out in the current tile
@@ -1113,80 +1121,146 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     owner[i] = 0u;
     cnt[i] = 0u;
   }
-
-  // Every thread copies its share of a tile's 16-byte chunks (every
-  // column: the positives' run, then the negatives' run) and arrives on the
-  // tile barrier once its copies have landed.  The caller has passed a
-  // barrier after the last reads of the tile buffer.
-  auto copy_tile = [&](const WorkUnit& V, uint32_t t0) {
-    if (a.withhold_copies) return;  // tests of the bounded wait: no copy, no arrival
-    const TileGeo g = tile_geo(V, t0);
-    const uint32_t cP = g.bytesP >> 4, per = cP + (g.bytesN >> 4);
-    const uint32_t chunks = per * (V.flags & 0xffu);
-    for (uint32_t c = threadIdx.x; c < chunks; c += kEvalThreads) {
-      const uint32_t q = c / per, r = c - q * per;
-      const int32_t* col = V.cols + (int64_t)q * V.stride;
-      int32_t* dst = raw + q * kTileStride;
-      if (r < cP)
-        cp_async16(dst + 4u * r, col + (g.gP & ~3u) + 4u * r);
-      else
-        cp_async16(dst + g.aN + 4u * (r - cP), col + (g.gN & ~3u) + 4u * (r - cP));
-    }
-    cp_async_mbar_arrive_noinc(&s_bar);
-  };
-
-  uint32_t ahead = 0;  // thread 0: the index claimed for the unit after the next
   if (threadIdx.x == 0) {
     s_nkeys[0] = s_nkeys[1] = 0u;
     s_alloc = 0u;
     s_abort = 0u;
     s_count = umin(a.unit_count[0], a.unit_cap);
-    s_uidx[0] = atomicAdd(a.work_counter, 1u);
-    if (s_uidx[0] < s_count) {
-      s_unit[0] = a.units[s_uidx[0]];
-      ahead = atomicAdd(a.work_counter, 1u);
-    } else {
-      ahead = s_count;
-    }
-    mbar_init(&s_bar, kEvalThreads);
+    mbar_init(&s_full, 1);
+    mbar_init(&s_empty, 1);
+    for (int k = 0; k < 3; ++k) mbar_init(&s_rec[k], 1);
     fence_mbar_init();
   }
-  __syncthreads();
-  if (s_uidx[0] < s_count) copy_tile(s_unit[0], 0u);
-  uint32_t phase = 0, tp = 0, cur = 0;
+  __syncthreads();  // the last barrier of the whole block: the roles split here
 
-  for (;;) {
-    if (s_uidx[cur] >= s_count) break;
-    const WorkUnit& U = s_unit[cur];
-    // Thread 0 claims the unit after the next one now (its index is first
-    // needed one unit later); the next unit's record is copied into shared
-    // memory while this unit's first key table is built.
-    uint32_t nidx = 0;
-    if (threadIdx.x == 0) {
-      nidx = ahead;
-      if (nidx < s_count) ahead = atomicAdd(a.work_counter, 1u);
+  if (threadIdx.x >= kConsumers) {
+    // Producer: one thread claims the units and publishes each unit's
+    // record one unit ahead (record slot u mod 3: its last reader finished
+    // with unit u - 3 before this unit's predecessor released the buffer),
+    // and puts every tile in flight (bulk copies of each column's positive
+    // and negative runs) as soon as the consumers release the buffer.  After
+    // the last unit it publishes an index past the end, as a record and as
+    // an empty tile.
+    if (threadIdx.x != kConsumers) return;
+    const uint32_t count = s_count;
+    auto claim = [&](uint32_t slot, WorkUnit& V) -> uint32_t {
+      const uint32_t idx = atomicAdd(a.work_counter, 1u);
+      if (idx < count) {
+        V = a.units[idx];
+        s_unit[slot] = V;
+      }
+      s_uidx[slot] = idx;
+      mbar_arrive(&s_rec[slot]);
+      return idx;
+    };
+    uint32_t ephase = 0, slot = 0;
+    bool first = true;
+    WorkUnit V{};
+    uint32_t idx = claim(0u, V);
+    for (;;) {
+      const uint32_t total = idx < count ? V.Pp + V.Np : 0u;
+      const uint32_t nslot = slot == 2u ? 0u : slot + 1u;
+      WorkUnit NV{};
+      uint32_t nidx = count;
+      uint32_t t0 = 0;
+      do {
+        if (!first) {
+          int64_t it = 0;
+          while (!mbar_try_wait(&s_empty, ephase)) {
+            if (++it > a.wait_limit) {
+              atomicExch(a.error_flag, 1);  // the consumers' own bounded waits stop them
+              return;
+            }
+          }
+          ephase ^= 1u;
+        }
+        first = false;
+        if (idx >= count) {
+          mbar_arrive(&s_full);  // the end mark: no tile
+          return;
+        }
+        const TileGeo g = tile_geo(V, t0);
+        const int nc = (int)(V.flags & 0xffu);
+        fence_proxy_async_smem();  // the copies come after the consumers' reads of the buffer
+        const uint32_t tx = (uint32_t)nc * (g.bytesP + g.bytesN);
+        if (a.withhold_copies) {
+          mbar_arrive_expect_tx(&s_full, tx > 0u ? tx : 16u);  // tests: bytes that never arrive
+        } else {
+          mbar_arrive_expect_tx(&s_full, tx);
+          for (int q = 0; q < nc; ++q) {
+            const int32_t* col = V.cols + (int64_t)q * V.stride;
+            if (g.bytesP) bulk_g2s(raw + q * kTileStride, col + (g.gP & ~3u), g.bytesP, &s_full);
+            if (g.bytesN) bulk_g2s(raw + q * kTileStride + g.aN, col + (g.gN & ~3u), g.bytesN, &s_full);
+          }
+        }
+        if (t0 == 0) nidx = claim(nslot, NV);  // the next unit, while this tile is in flight
+        t0 += (uint32_t)kTile;
+      } while (t0 < total);
+      idx = nidx;
+      V = NV;
+      slot = nslot;
     }
-    const int lit_begin = (int)U.lit_begin;
-    const bool has_atoms = (U.flags & 0x100u) != 0u;
-    const uint32_t total = U.Pp + U.Np;
+  }
 
-    // This thread's entry records.  More entries than threads: a pair of
-    // consecutive records per thread.  At most half as many: `tpe` (2 to
-    // 8) neighbouring threads share one entry and split its row checks
-    // (thread `sub` takes rows sub, sub + tpe, ...).  Otherwise one each.
-    uint32_t tpe = 1, sub = 0;
-    const bool pairs = U.ecnt > (uint32_t)kEvalThreads;
-    if (!pairs && 2u * U.ecnt <= (uint32_t)kEvalThreads) {
-      const uint32_t q = (uint32_t)kEvalThreads / (U.ecnt > 0u ? U.ecnt : 1u);
+  // Consumers.  Bounded wait for the next tile: a wait that gives up flags
+  // the context, waits once more (bounded) for copies still in flight, so
+  // that none lands after the CTA has stopped, and stops the CTA: all
+  // consumers leave the unit loop after the barrier that follows, nothing is
+  // flushed, and the call reports QFG_ERR_TIMEOUT.  (Should the second wait
+  // give up too, the CTA stops all the same.)
+  uint32_t phase = 0, tp = 0, cur = 0;
+  auto wait_tile = [&]() -> bool {
+    int64_t it = 0;
+    while (!mbar_try_wait(&s_full, phase)) {
+      if (++it > a.wait_limit) {
+        atomicExch(a.error_flag, 1);
+        s_abort = 1u;
+        for (int64_t k2 = 0; k2 < a.wait_limit && !mbar_try_wait(&s_full, phase); ++k2) {
+        }
+        break;
+      }
+    }
+    phase ^= 1u;
+    consumer_sync();
+    return s_abort != 0u;
+  };
+
+  // This thread's entry records of a unit.  More entries than consumers:
+  // a pair of consecutive records per thread.  At most half as many: `tpe`
+  // (2 to 8) neighbouring threads share one entry and split its row checks
+  // (thread `sub` takes rows sub, sub + tpe, ...).  Otherwise one each.
+  // They are loaded as soon as the unit's record is published, so the loads
+  // are in flight while the previous unit's sums are reduced.
+  uint32_t tpe = 1, sub = 0;
+  bool have = false, have1 = false;
+  int2 e_k0 = make_int2(0, 0), e_kA = e_k0, e_kB = e_k0, e_mult = e_k0;
+  uint2 e_meta = make_uint2(0u, 0u);
+  uint32_t rphase = 0;  // bit k: parity of record slot k's next phase
+  auto load_entries = [&](uint32_t rslot_i) -> bool {
+    int64_t it = 0;
+    while (!mbar_try_wait(&s_rec[rslot_i], (rphase >> rslot_i) & 1u)) {
+      if (++it > a.wait_limit) {
+        atomicExch(a.error_flag, 1);
+        s_abort = 1u;  // seen after the next wait's barrier
+        return false;
+      }
+    }
+    rphase ^= 1u << rslot_i;
+    if (s_uidx[rslot_i] >= s_count) return false;
+    const WorkUnit& V = s_unit[rslot_i];
+    tpe = 1;
+    sub = 0;
+    const bool pairs = V.ecnt > (uint32_t)kConsumers;
+    if (!pairs && 2u * V.ecnt <= (uint32_t)kConsumers) {
+      const uint32_t q = (uint32_t)kConsumers / (V.ecnt > 0u ? V.ecnt : 1u);
       tpe = q >= 8u ? 8u : q >= 4u ? 4u : 2u;
       sub = threadIdx.x & (tpe - 1u);
     }
     const uint32_t j0 = pairs ? 2u * threadIdx.x : threadIdx.x / tpe;
-    const bool have = j0 < U.ecnt && U.eoff + U.ecnt <= a.entry_cap;
-    int2 e_k0 = make_int2(0, 0), e_kA = e_k0, e_kB = e_k0, e_mult = e_k0;
-    uint2 e_meta = make_uint2(0u, 0u);
+    have = j0 < V.ecnt && V.eoff + V.ecnt <= a.entry_cap;
+    have1 = pairs && have && j0 + 1 < V.ecnt;
     if (have) {
-      const uint32_t r = U.eoff + j0;  // pairs: even, and the block is padded to a multiple of 4
+      const uint32_t r = V.eoff + j0;  // pairs: even, and the block is padded to a multiple of 4
       if (pairs) {
         e_k0 = __ldg(reinterpret_cast<const int2*>(a.rec.k0 + r));
         e_kA = __ldg(reinterpret_cast<const int2*>(a.rec.kA + r));
@@ -1201,49 +1275,27 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         e_meta.x = __ldg(a.rec.meta + r);
       }
     }
-    const bool have1 = pairs && have && j0 + 1 < U.ecnt;
+    return true;
+  };
+
+  load_entries(0u);
+  for (;;) {
+    if (wait_tile()) break;
+    if (s_uidx[cur] >= s_count) break;  // the producer's end mark
+    const WorkUnit& U = s_unit[cur];
+    const int lit_begin = (int)U.lit_begin;
+    const bool has_atoms = (U.flags & 0x100u) != 0u;
+    const uint32_t total = U.Pp + U.Np;
 
     long long bp = 0, bn = 0, cp = 0, cn = 0;
     int Lrun = -1;
     for (uint32_t t0 = 0; t0 < total; t0 += kTile) {
+      if (t0 > 0 && wait_tile()) break;
       const TileGeo g = tile_geo(U, t0);
       const int nt = (int)g.nt, npos = (int)g.npos;
       const uint32_t shP = g.shP, baseN = g.baseN;
-      {
-        // Bounded wait for the tile's copies.  A wait that gives up flags
-        // the context, waits once more (bounded) for copies still in
-        // flight, so that none lands after the CTA has stopped, and stops
-        // the CTA: all threads leave the unit loop after the barrier below,
-        // nothing is flushed, and the call reports QFG_ERR_TIMEOUT.  (Should
-        // the second wait give up too, the CTA stops all the same.)
-        int64_t it = 0;
-        while (!mbar_try_wait(&s_bar, phase)) {
-          if (++it > a.wait_limit) {
-            atomicExch(a.error_flag, 1);
-            s_abort = 1u;
-            for (int64_t k2 = 0; k2 < a.wait_limit && !mbar_try_wait(&s_bar, phase); ++k2) {
-            }
-            break;
-          }
-        }
-        phase ^= 1u;
-      }
-      __syncthreads();
-      if (s_abort != 0u) break;
-      // The other parity's key count and unit record were last read before
-      // this barrier.
-      if (threadIdx.x == 0) {
-        s_nkeys[tp ^ 1u] = 0u;
-        if (t0 == 0) {
-          s_uidx[cur ^ 1u] = nidx;
-          if (nidx < s_count) {
-            const int32_t* src = reinterpret_cast<const int32_t*>(a.units + nidx);
-            int32_t* dst = reinterpret_cast<int32_t*>(&s_unit[cur ^ 1u]);
-#pragma unroll
-            for (int q = 0; q < (int)(sizeof(WorkUnit) / 16); ++q) cp_async16(dst + 4 * q, src + 4 * q);
-          }
-        }
-      }
+      // The other parity's key count was last read before the wait's barrier.
+      if (threadIdx.x == 0) s_nkeys[tp ^ 1u] = 0u;
       // Distinct join keys of the tile: owner = first row + 1, claimed by
       // CAS; the count atomics return each row's rank within its key and
       // label (positive count low half, negative count high half).  A
@@ -1256,7 +1308,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         uint32_t slot[kInsertBatch], own[kInsertBatch];
 #pragma unroll
         for (int k = 0; k < kInsertBatch; ++k) {
-          const int i = (int)threadIdx.x + (k0 + k) * kEvalThreads;
+          const int i = (int)threadIdx.x + (k0 + k) * kConsumers;
           const uint32_t pos = i < npos ? (uint32_t)i + shP : baseN + (uint32_t)(i - npos);
           key[k] = i < nt ? raw[pos] : 0;
           slot[k] = mix32((uint32_t)key[k]) & (kSlots - 1);
@@ -1265,7 +1317,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         for (int k = 0; k < kInsertBatch; ++k) own[k] = owner[slot[k]];
 #pragma unroll
         for (int k = 0; k < kInsertBatch; ++k) {
-          const int i = (int)threadIdx.x + (k0 + k) * kEvalThreads;
+          const int i = (int)threadIdx.x + (k0 + k) * kConsumers;
           if (i >= nt) continue;
           if (own[k] != 0u && raw[own[k] - 1u] == key[k]) continue;  // the key's home slot
           const uint32_t pos = i < npos ? (uint32_t)i + shP : baseN + (uint32_t)(i - npos);
@@ -1284,13 +1336,13 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         uint32_t old[kInsertBatch];
 #pragma unroll
         for (int k = 0; k < kInsertBatch; ++k) {
-          const int i = (int)threadIdx.x + (k0 + k) * kEvalThreads;
+          const int i = (int)threadIdx.x + (k0 + k) * kConsumers;
           old[k] = i < nt ? atomicAdd(&cnt[slot[k]], i < npos ? 1u : 0x10000u) : 0u;
         }
         if (has_atoms) {
 #pragma unroll
           for (int k = 0; k < kInsertBatch; ++k) {
-            const int i = (int)threadIdx.x + (k0 + k) * kEvalThreads;
+            const int i = (int)threadIdx.x + (k0 + k) * kConsumers;
             if (i < nt) {
               rslot[i] = (uint16_t)slot[k];
               rrank[i] = (uint16_t)(i < npos ? (old[k] & 0xffffu) : (old[k] >> 16));
@@ -1298,14 +1350,13 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
           }
         }
       }
-      if (threadIdx.x == 0 && t0 == 0) cp_async_wait_all();  // the next unit's record
-      __syncthreads();
+      consumer_sync();
       const uint32_t nk = s_nkeys[tp];
       {
         // Owners become keys (probes compare keys directly).  With atom
         // literals each key also takes the run of the row list for its
         // rows by a warp-aggregated atomic (the runs' order is free).
-        for (uint32_t d0 = 0; d0 < nk; d0 += blockDim.x) {
+        for (uint32_t d0 = 0; d0 < nk; d0 += kConsumers) {
           const uint32_t d = d0 + threadIdx.x;
           uint32_t c = 0, sl = 0;
           if (d < nk) {
@@ -1328,7 +1379,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
           }
         }
       }
-      __syncthreads();
+      consumer_sync();
       if (has_atoms) {
         if (threadIdx.x == 0) s_alloc = 0u;  // last used above; next used after the next tile's wait
         // All of a thread's loads first, then its stores (the shared arrays
@@ -1336,7 +1387,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         uint32_t dst[kRowsPerThread];
 #pragma unroll
         for (int k = 0; k < kRowsPerThread; ++k) {
-          const int i = (int)threadIdx.x + k * kEvalThreads;
+          const int i = (int)threadIdx.x + k * kConsumers;
           dst[k] = 0u;
           if (i < nt) {
             const int sl = rslot[i];
@@ -1346,10 +1397,10 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         }
 #pragma unroll
         for (int k = 0; k < kRowsPerThread; ++k) {
-          const int i = (int)threadIdx.x + k * kEvalThreads;
+          const int i = (int)threadIdx.x + k * kConsumers;
           if (i < nt) rows[dst[k]] = (uint16_t)(i < npos ? (uint32_t)i + shP : baseN + (uint32_t)(i - npos));
         }
-        __syncthreads();
+        consumer_sync();
       }
       // This thread's entries against the tile.
 #pragma unroll
@@ -1417,23 +1468,20 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         cp += hp;
         cn += hn;
       }
-      __syncthreads();
-      // The tile's slots are cleared and the tile buffer refilled -- the
-      // next tile of this unit, or the first tile of the next unit -- with
-      // no further barrier: the next key table is built after the next
-      // tile's wait and barrier.
-      for (uint32_t d = threadIdx.x; d < nk; d += blockDim.x) {
+      consumer_sync();
+      // The tile's slots are cleared (the next key table is built after the
+      // next wait's barrier) and the buffer goes back to the producer.
+      for (uint32_t d = threadIdx.x; d < nk; d += kConsumers) {
         const uint32_t sl = klist[d];
         owner[sl] = 0u;
         cnt[sl] = 0u;
       }
-      if (t0 + (uint32_t)kTile < total)
-        copy_tile(U, t0 + (uint32_t)kTile);
-      else if (s_uidx[cur ^ 1u] < s_count)
-        copy_tile(s_unit[cur ^ 1u], 0u);
+      if (threadIdx.x == 0) mbar_arrive(&s_empty);
       tp ^= 1u;
     }
     if (s_abort != 0u) break;  // read after the barrier that follows the wait
+    const uint32_t next = cur == 2u ? 0u : cur + 1u;
+    load_entries(next);
     // Threads' entries are contiguous and increasing, so equal literals sit
     // on consecutive lanes; idle lanes (Lrun = -1) trail.
     cp = seg_scan(cp, Lrun);
@@ -1444,11 +1492,11 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     const bool seg_end = lane_id() == 31 || next_L != Lrun;
     if (seg_end && Lrun >= 0 && (cp | cn | bp | bn) != 0)
       flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
-    cur ^= 1u;  // the next unit's index and record were published before a barrier of this unit
+    cur = next;
   }
-  __syncthreads();
+  consumer_sync();
   if (s_abort != 0u) return;
-  for (int i = threadIdx.x; i < 4 * a.num_lits; i += blockDim.x) {
+  for (int i = threadIdx.x; i < 4 * a.num_lits; i += kConsumers) {
     const unsigned long long v = acc[i];
     if (v != 0ull) atomicAdd(&a.counts[4 * a.lits[i >> 2].out + (i & 3)], v);
   }
