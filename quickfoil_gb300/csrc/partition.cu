@@ -133,7 +133,7 @@ __global__ void stable_scatter_kernel(IO io, int64_t n, int shift, int bits, int
 // warp w owns rows [w * kRTPerWarp, (w + 1) * kRTPerWarp) and walks them 32
 // at a time: a row's rank among the warp's rows of its digit is the warp's
 // running count of the digit plus its rank among the equal-digit lanes below
-// it (__match_any_sync), with no block barrier between the steps.  One scan
+// it (one ballot per digit bit), with no block barrier between the steps.  One scan
 // over the warps of every digit then turns the warps' counts into offsets,
 // so each row's rank within the round is stable; the round's keys, staged in
 // shared memory, are written in digit order, consecutive threads on
@@ -202,10 +202,19 @@ __global__ void __launch_bounds__(kRTThreads) round_scatter_kernel(IO io, int64_
       }
       const uint32_t d = (k >> shift) & mask;
       const unsigned act = __ballot_sync(kFullMask, valid);
+      // The lanes holding the same digit: one ballot per digit bit.
+      unsigned peers = act;
+#pragma unroll
+      for (int b = 0; b < kRTMaxBits; ++b) {
+        if (b < bits) {
+          const bool bit = ((d >> b) & 1u) != 0u;
+          const unsigned bb = __ballot_sync(kFullMask, bit);
+          peers &= bit ? bb : ~bb;
+        }
+      }
       dj[j] = d;
       rk[j] = 0;
       if (valid) {
-        const unsigned peers = __match_any_sync(act, d);
         rk[j] = my[d] + __popc(peers & lt);
         __syncwarp(act);
         if (lane == __ffs(peers) - 1) my[d] += __popc(peers);
