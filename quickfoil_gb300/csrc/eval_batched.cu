@@ -48,6 +48,7 @@ constexpr int kConsumers = kEvalThreads - 32;
 constexpr int kGroupCols = QFG_MAX_ARITY;  // join column + up to 7 atom columns
 constexpr int kMaxLitsPerLaunch = 512;
 constexpr int kChunk = 2 * kConsumers;       // relation entries per work unit: two per consumer
+constexpr int kUnitEntries = 4 * kChunk;     // relation entries per evaluation unit (one key table)
 constexpr int kMaxGroupLits = 256;  // literals of one group (one thread each in a per-item prefix)
 constexpr int kPartThreads = 1024;
 constexpr int kDefaultCoarseBits = 7;  // pass 1 fan-out: 2 << 7 = 256 bins (hash prefix, label)
@@ -714,12 +715,12 @@ bpart_pass2_kernel(const BPartArgs* __restrict__ A) {
 // ----------------------------------------------------------------------------
 // Persistent evaluation kernel.
 //
-// Work unit = a range of at most kChunk relation entries of one (group,
+// Work unit = a range of at most kUnitEntries relation entries of one (group,
 // partition) item.  Three launches per literal batch:
 //   plan_units   lists the units: each item's segment bounds and the number
 //                of relation entries its literals hold in the item's key
 //                range; items without rows or entries are dropped, items
-//                with more than kChunk entries (hot join keys of skewed
+//                with more than kUnitEntries entries (hot join keys of skewed
 //                relations) are split so no CTA is left with a long tail,
 //                and every unit gets a block of entry records;
 //   gather       one warp per unit forms the item's literal-major entry
@@ -811,8 +812,9 @@ struct EvalArgs {
   int max_cols;
   int64_t total_items;
   WorkUnit* units;
-  uint32_t* unit_count;      // [units, entry records]
-  uint32_t unit_cap;
+  WorkUnit* eunits;          // tiled path: evaluation units, up to kUnitEntries entries each
+  uint32_t* unit_count;      // [units, entry records, evaluation units]
+  uint32_t unit_cap;         // of units, and of evaluation units
   uint32_t entry_cap;
   EntryRecs rec;
   unsigned int* work_counter;
@@ -906,24 +908,34 @@ __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
           espace = (nch - 1) * a.piece + ((E - (nch - 1) * a.piece + 3u) & ~3u);
       }
     }
-    // Warp-aggregated reservation of unit slots and entry records.
-    uint32_t x = nch, y = espace;
+    // Evaluation units (tiled path): runs of up to kUnitEntries / piece
+    // consecutive units of the item, whose entry blocks are consecutive.
+    const uint32_t per_eu = (uint32_t)kUnitEntries / a.piece;
+    const uint32_t neu = a.eunits != nullptr ? (nch + per_eu - 1u) / per_eu : 0u;
+    // Warp-aggregated reservation of unit slots, entry records and
+    // evaluation units.
+    uint32_t x = nch, y = espace, z = neu;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t xu = __shfl_up_sync(kFullMask, x, o), yu = __shfl_up_sync(kFullMask, y, o);
+      const uint32_t zu = __shfl_up_sync(kFullMask, z, o);
       if (lane >= o) {
         x += xu;
         y += yu;
+        z += zu;
       }
     }
     const uint32_t tu = __shfl_sync(kFullMask, x, 31), te = __shfl_sync(kFullMask, y, 31);
-    uint32_t ub = 0, eb = 0;
+    const uint32_t tv = __shfl_sync(kFullMask, z, 31);
+    uint32_t ub = 0, eb = 0, vb = 0;
     if (lane == 31 && tu > 0) {
       ub = atomicAdd(&a.unit_count[0], tu);
       eb = atomicAdd(&a.unit_count[1], te);
+      if (tv > 0) vb = atomicAdd(&a.unit_count[2], tv);
     }
     ub = __shfl_sync(kFullMask, ub, 31) + x - nch;
     eb = __shfl_sync(kFullMask, eb, 31) + y - espace;
+    vb = __shfl_sync(kFullMask, vb, 31) + z - neu;
     if (a.row_chunk > 0) {
       // Streamed path: (entry piece, row chunk) pairs; a unit's rows are
       // [pad, pad + ecnt2) of the item's positives-then-negatives order,
@@ -954,6 +966,18 @@ __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
         u.Pp = u.Np = 0;
       }
       a.units[ub + k] = u;
+    }
+    for (uint32_t k = 0; k < neu; ++k) {
+      if (vb + k >= a.unit_cap) break;  // never read: the evaluation stops at unit_cap
+      WorkUnit v = u;
+      v.f0 = k * (uint32_t)kUnitEntries;
+      v.ecnt = umin(E - v.f0, (uint32_t)kUnitEntries);
+      v.eoff = eb + v.f0;
+      if ((uint64_t)v.eoff + ((v.ecnt + 3u) & ~3u) > a.entry_cap) {
+        v.ecnt = 0;  // as above: never happens
+        v.Pp = v.Np = 0;
+      }
+      a.eunits[vb + k] = v;
     }
   }
 }
@@ -1125,7 +1149,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     s_nkeys[0] = s_nkeys[1] = 0u;
     s_alloc = 0u;
     s_abort = 0u;
-    s_count = umin(a.unit_count[0], a.unit_cap);
+    s_count = umin(a.unit_count[2], a.unit_cap);
     mbar_init(&s_full, 1);
     mbar_init(&s_empty, 1);
     for (int k = 0; k < 3; ++k) mbar_init(&s_rec[k], 1);
@@ -1146,7 +1170,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     auto claim = [&](uint32_t slot, WorkUnit& V) -> uint32_t {
       const uint32_t idx = atomicAdd(a.work_counter, 1u);
       if (idx < count) {
-        V = a.units[idx];
+        V = a.eunits[idx];
         s_unit[slot] = V;
       }
       s_uidx[slot] = idx;
@@ -1236,31 +1260,23 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
   int2 e_k0 = make_int2(0, 0), e_kA = e_k0, e_kB = e_k0, e_mult = e_k0;
   uint2 e_meta = make_uint2(0u, 0u);
   uint32_t rphase = 0;  // bit k: parity of record slot k's next phase
-  auto load_entries = [&](uint32_t rslot_i) -> bool {
-    int64_t it = 0;
-    while (!mbar_try_wait(&s_rec[rslot_i], (rphase >> rslot_i) & 1u)) {
-      if (++it > a.wait_limit) {
-        atomicExch(a.error_flag, 1);
-        s_abort = 1u;  // seen after the next wait's barrier
-        return false;
-      }
-    }
-    rphase ^= 1u << rslot_i;
-    if (s_uidx[rslot_i] >= s_count) return false;
-    const WorkUnit& V = s_unit[rslot_i];
+  // Entries [c0, c0 + kChunk) of unit V into this thread's registers.
+  auto setup_chunk = [&](const WorkUnit& V, uint32_t c0) {
+    const uint32_t cnt = umin((uint32_t)kChunk, V.ecnt - c0);
     tpe = 1;
     sub = 0;
-    const bool pairs = V.ecnt > (uint32_t)kConsumers;
-    if (!pairs && 2u * V.ecnt <= (uint32_t)kConsumers) {
-      const uint32_t q = (uint32_t)kConsumers / (V.ecnt > 0u ? V.ecnt : 1u);
+    const bool pairs = cnt > (uint32_t)kConsumers;
+    if (!pairs && 2u * cnt <= (uint32_t)kConsumers) {
+      const uint32_t q = (uint32_t)kConsumers / (cnt > 0u ? cnt : 1u);
       tpe = q >= 8u ? 8u : q >= 4u ? 4u : 2u;
       sub = threadIdx.x & (tpe - 1u);
     }
     const uint32_t j0 = pairs ? 2u * threadIdx.x : threadIdx.x / tpe;
-    have = j0 < V.ecnt && V.eoff + V.ecnt <= a.entry_cap;
-    have1 = pairs && have && j0 + 1 < V.ecnt;
+    have = j0 < cnt && V.eoff + V.ecnt <= a.entry_cap;
+    have1 = pairs && have && j0 + 1 < cnt;
     if (have) {
-      const uint32_t r = V.eoff + j0;  // pairs: even, and the block is padded to a multiple of 4
+      // pairs: even (c0 and the block start are multiples of 4)
+      const uint32_t r = V.eoff + c0 + j0;
       if (pairs) {
         e_k0 = __ldg(reinterpret_cast<const int2*>(a.rec.k0 + r));
         e_kA = __ldg(reinterpret_cast<const int2*>(a.rec.kA + r));
@@ -1275,7 +1291,42 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         e_meta.x = __ldg(a.rec.meta + r);
       }
     }
+  };
+  // The first chunk of the unit in record slot rslot_i, once published.
+  auto load_entries = [&](uint32_t rslot_i) -> bool {
+    int64_t it = 0;
+    while (!mbar_try_wait(&s_rec[rslot_i], (rphase >> rslot_i) & 1u)) {
+      if (++it > a.wait_limit) {
+        atomicExch(a.error_flag, 1);
+        s_abort = 1u;  // seen after the next wait's barrier
+        return false;
+      }
+    }
+    rphase ^= 1u << rslot_i;
+    if (s_uidx[rslot_i] >= s_count) return false;
+    setup_chunk(s_unit[rslot_i], 0u);
     return true;
+  };
+
+  // Per-literal sums of the warp's lanes into the CTA's accumulators.  A
+  // thread's entries are contiguous and increasing within a chunk, so equal
+  // literals sit on consecutive lanes (the segmented scan needs that); idle
+  // lanes (Lrun = -1) trail.  A thread with no entry in a later chunk
+  // flushes its sums on its own, so every lane's literal at the unit's end
+  // comes from the unit's last chunk.
+  long long bp = 0, bn = 0, cp = 0, cn = 0;
+  int Lrun = -1;
+  auto reduce_sums = [&](int lit_begin) {
+    cp = seg_scan(cp, Lrun);
+    cn = seg_scan(cn, Lrun);
+    bp = seg_scan(bp, Lrun);
+    bn = seg_scan(bn, Lrun);
+    const int next_L = __shfl_down_sync(kFullMask, Lrun, 1);
+    const bool seg_end = lane_id() == 31 || next_L != Lrun;
+    if (seg_end && Lrun >= 0 && (cp | cn | bp | bn) != 0)
+      flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
+    bp = bn = cp = cn = 0;
+    Lrun = -1;
   };
 
   load_entries(0u);
@@ -1287,9 +1338,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     const bool has_atoms = (U.flags & 0x100u) != 0u;
     const uint32_t total = U.Pp + U.Np;
 
-    long long bp = 0, bn = 0, cp = 0, cn = 0;
-    int Lrun = -1;
-    for (uint32_t t0 = 0; t0 < total; t0 += kTile) {
+    for (uint32_t t0 = 0; t0 < total || t0 == 0; t0 += kTile) {  // an empty unit: one empty tile
       if (t0 > 0 && wait_tile()) break;
       const TileGeo g = tile_geo(U, t0);
       const int nt = (int)g.nt, npos = (int)g.npos;
@@ -1402,71 +1451,85 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
         }
         consumer_sync();
       }
-      // This thread's entries against the tile.
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        if (!(j == 0 ? have : have1)) continue;
-        const int32_t k0 = j == 0 ? e_k0.x : e_k0.y;
-        const uint32_t meta = j == 0 ? e_meta.x : e_meta.y;
-        const int L = (int)(meta & 0xffu);
-        if (L != Lrun) {
-          if (Lrun >= 0 && (cp | cn | bp | bn) != 0)
-            flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
-          bp = bn = cp = cn = 0;
-          Lrun = L;
-        }
-        if (!((meta >> 10) & 1u)) continue;
-        uint32_t slot = mix32((uint32_t)k0) & (kSlots - 1);
-        uint32_t w = 0;
-        for (int probe = 0; probe < kSlots; ++probe) {
-          w = cnt[slot];
-          if (w == 0u || (int32_t)owner[slot] == k0) break;
-          slot = (slot + 1) & (kSlots - 1);
-        }
-        if (w == 0u) continue;
-        const uint32_t P = w & 0xffffu, N = w >> 16;
-        const uint32_t nchk = (meta >> 8) & 3u;
-        uint32_t hp = 0, hn = 0;
-        if (nchk == 0) {
-          if (sub == 0u) {
-            hp = P;
-            hn = N;
+      // This thread's entries against the tile, a chunk of the unit's
+      // entries at a time (the first chunk's records were loaded when the
+      // unit's record was published; a later tile reloads it).
+      for (uint32_t c0 = 0; c0 < U.ecnt || c0 == 0; c0 += kChunk) {
+        if (c0 > 0 || t0 > 0) {
+          setup_chunk(U, c0);
+          if (!have && Lrun >= 0) {
+            // No entry in this chunk: the thread's sums go now, so at the
+            // unit's end every lane's literal is from the last chunk.
+            if ((cp | cn | bp | bn) != 0) flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
+            bp = bn = cp = cn = 0;
+            Lrun = -1;
           }
-        } else {
-          const uint32_t beg = sstart[slot], mid = beg + P, end = mid + N;
-          const int32_t kA = j == 0 ? e_kA.x : e_kA.y;
-          if (nchk == 1) {
-            const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
-            hp = count_matches1(rows, ca, kA, beg + sub, mid, tpe);
-            hn = count_matches1(rows, ca, kA, mid + sub, end, tpe);
-          } else if (nchk == 2) {
-            const int32_t kB = j == 0 ? e_kB.x : e_kB.y;
-            const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
-            const int32_t* cb = raw + ((meta >> 16) & 7u) * kTileStride;
-            hp = count_matches2(rows, ca, cb, kA, kB, beg + sub, mid, tpe);
-            hn = count_matches2(rows, ca, cb, kA, kB, mid + sub, end, tpe);
+        }
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          if (!(j == 0 ? have : have1)) continue;
+          const int32_t k0 = j == 0 ? e_k0.x : e_k0.y;
+          const uint32_t meta = j == 0 ? e_meta.x : e_meta.y;
+          const int L = (int)(meta & 0xffu);
+          if (L != Lrun) {
+            if (Lrun >= 0 && (cp | cn | bp | bn) != 0)
+              flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
+            bp = bn = cp = cn = 0;
+            Lrun = L;
+          }
+          if (!((meta >> 10) & 1u)) continue;
+          uint32_t slot = mix32((uint32_t)k0) & (kSlots - 1);
+          uint32_t w = 0;
+          for (int probe = 0; probe < kSlots; ++probe) {
+            w = cnt[slot];
+            if (w == 0u || (int32_t)owner[slot] == k0) break;
+            slot = (slot + 1) & (kSlots - 1);
+          }
+          if (w == 0u) continue;
+          const uint32_t P = w & 0xffffu, N = w >> 16;
+          const uint32_t nchk = (meta >> 8) & 3u;
+          uint32_t hp = 0, hn = 0;
+          if (nchk == 0) {
+            if (sub == 0u) {
+              hp = P;
+              hn = N;
+            }
           } else {
-            // More than two checked columns: keys from the key table.
-            const LitDesc& d = a.lits[lit_begin + L];
-            const uint32_t e = (uint32_t)kA;
-            for (uint32_t x = beg + sub; x < end; x += tpe) {
-              const int r = rows[x];
-              bool pass = true;
-              for (int q = 1; q < d.nk && pass; ++q) {
-                const int ac = d.atom_col[q];
-                if (ac != 0) pass = raw[ac * kTileStride + r] == __ldg(d.keys + q * d.stride + e);
-              }
-              if (pass) {
-                if (x < mid) ++hp; else ++hn;
+            const uint32_t beg = sstart[slot], mid = beg + P, end = mid + N;
+            const int32_t kA = j == 0 ? e_kA.x : e_kA.y;
+            if (nchk == 1) {
+              const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
+              hp = count_matches1(rows, ca, kA, beg + sub, mid, tpe);
+              hn = count_matches1(rows, ca, kA, mid + sub, end, tpe);
+            } else if (nchk == 2) {
+              const int32_t kB = j == 0 ? e_kB.x : e_kB.y;
+              const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
+              const int32_t* cb = raw + ((meta >> 16) & 7u) * kTileStride;
+              hp = count_matches2(rows, ca, cb, kA, kB, beg + sub, mid, tpe);
+              hn = count_matches2(rows, ca, cb, kA, kB, mid + sub, end, tpe);
+            } else {
+              // More than two checked columns: keys from the key table.
+              const LitDesc& d = a.lits[lit_begin + L];
+              const uint32_t e = (uint32_t)kA;
+              for (uint32_t x = beg + sub; x < end; x += tpe) {
+                const int r = rows[x];
+                bool pass = true;
+                for (int q = 1; q < d.nk && pass; ++q) {
+                  const int ac = d.atom_col[q];
+                  if (ac != 0) pass = raw[ac * kTileStride + r] == __ldg(d.keys + q * d.stride + e);
+                }
+                if (pass) {
+                  if (x < mid) ++hp; else ++hn;
+                }
               }
             }
           }
+          const long long mlt = j == 0 ? e_mult.x : e_mult.y;
+          bp += mlt * hp;
+          bn += mlt * hn;
+          cp += hp;
+          cn += hn;
         }
-        const long long mlt = j == 0 ? e_mult.x : e_mult.y;
-        bp += mlt * hp;
-        bn += mlt * hn;
-        cp += hp;
-        cn += hn;
       }
       consumer_sync();
       // The tile's slots are cleared (the next key table is built after the
@@ -1482,16 +1545,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     if (s_abort != 0u) break;  // read after the barrier that follows the wait
     const uint32_t next = cur == 2u ? 0u : cur + 1u;
     load_entries(next);
-    // Threads' entries are contiguous and increasing, so equal literals sit
-    // on consecutive lanes; idle lanes (Lrun = -1) trail.
-    cp = seg_scan(cp, Lrun);
-    cn = seg_scan(cn, Lrun);
-    bp = seg_scan(bp, Lrun);
-    bn = seg_scan(bn, Lrun);
-    const int next_L = __shfl_down_sync(kFullMask, Lrun, 1);
-    const bool seg_end = lane_id() == 31 || next_L != Lrun;
-    if (seg_end && Lrun >= 0 && (cp | cn | bp | bn) != 0)
-      flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
+    reduce_sums(lit_begin);
     cur = next;
   }
   consumer_sync();
@@ -2338,7 +2392,8 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     max_cap = std::max(max_cap, cap);
     max_ecap = std::max(max_ecap, ecap);
   }
-  QFG_TRY(ctx->scratch[kScrWork].reserve(ctx, sizeof(WorkUnit) * (size_t)max_cap));
+  // Units, then (tiled path) as many evaluation units at most.
+  QFG_TRY(ctx->scratch[kScrWork].reserve(ctx, sizeof(WorkUnit) * 2 * (size_t)max_cap));
   QFG_TRY(ctx->scratch[kScrEntries].reserve(ctx, sizeof(int32_t) * 5 * (size_t)max_ecap));
   EntryRecs recs;
   {
@@ -2376,6 +2431,7 @@ int prepare_step(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_literal* 
     ea.total_items = total;
     ea.work_counter = ps->counter;
     ea.units = ctx->scratch[kScrWork].as<WorkUnit>();
+    ea.eunits = L.streamed ? nullptr : ea.units + max_cap;
     ea.unit_count = ps->counter + 1;
     ea.unit_cap = (uint32_t)caps[si];
     ea.entry_cap = (uint32_t)ecaps[si];
@@ -2445,7 +2501,7 @@ int enqueue_step(Ctx* ctx, const PreparedStep* pps) {
   QFG_TRY(stage_end(ctx, QFG_STAGE_BIND_PARTITION));
   for (const LaunchJob& L : ps.launches) {
     QFG_TRY(stage_begin(ctx, QFG_STAGE_UNIT_PLAN));
-    QFG_CUDA(ctx, cudaMemsetAsync(ps.counter, 0, 3 * sizeof(unsigned int), ctx->stream));
+    QFG_CUDA(ctx, cudaMemsetAsync(ps.counter, 0, 4 * sizeof(unsigned int), ctx->stream));
     plan_units_kernel<<<L.plan_grid, 256, 0, ctx->stream>>>(L.ea);
     QFG_LAUNCHED(ctx);
     if (L.ea.records) {
@@ -2506,7 +2562,7 @@ int step_scratch_bytes(Ctx* ctx, const qfg_bindings* b, int32_t n, const qfg_lit
     units += kt->num_entries / piece + 1;
     entries += std::max<int64_t>(kt->num_entries, 1);
   }
-  words += units * (int64_t)(sizeof(WorkUnit) / 4) +
+  words += (mode == kModeStreamed ? 1 : 2) * units * (int64_t)(sizeof(WorkUnit) / 4) +
            (mode == kModeStreamed ? 20 : 5 * (entries + 4 * units + 8));
   *bytes = 4 * words + (int64_t)(sizeof(GroupDesc) + sizeof(LitDesc) + sizeof(SigDesc)) * n +
            32 * (int64_t)n;
