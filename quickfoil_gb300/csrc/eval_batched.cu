@@ -48,7 +48,7 @@ constexpr int kConsumers = kEvalThreads - 32;
 constexpr int kGroupCols = QFG_MAX_ARITY;  // join column + up to 7 atom columns
 constexpr int kMaxLitsPerLaunch = 512;
 constexpr int kChunk = 2 * kConsumers;       // relation entries per work unit: two per consumer
-constexpr int kUnitEntries = 4 * kChunk;     // relation entries per evaluation unit (one key table)
+constexpr int kUnitEntries = 8 * kChunk;     // relation entries per evaluation unit (one key table)
 constexpr int kMaxGroupLits = 256;  // literals of one group (one thread each in a per-item prefix)
 constexpr int kPartThreads = 1024;
 constexpr int kDefaultCoarseBits = 7;  // pass 1 fan-out: 2 << 7 = 256 bins (hash prefix, label)
