@@ -1090,31 +1090,39 @@ __device__ __forceinline__ void consumer_sync() {
   asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
 }
 
-// Rows x = b, b + step, ... < e of a key's row list whose column value
-// equals k (four rows' loads in flight at a time).
+// Rows x = b, b + step, ... < e of a key's row list (its positive rows
+// before mid) whose column value equals k: positive matches in the low 16
+// bits, negative matches in the high 16 (four rows' loads in flight at a
+// time).
 __device__ __forceinline__ uint32_t count_matches1(const uint16_t* rows, const int32_t* c, int32_t k,
-                                                   uint32_t b, uint32_t e, uint32_t step) {
+                                                   uint32_t b, uint32_t mid, uint32_t e,
+                                                   uint32_t step) {
   uint32_t h = 0, x = b;
   for (; x + 3u * step < e; x += 4u * step) {
     const int r0 = rows[x], r1 = rows[x + step], r2 = rows[x + 2u * step], r3 = rows[x + 3u * step];
-    h += (uint32_t)(c[r0] == k) + (uint32_t)(c[r1] == k) + (uint32_t)(c[r2] == k) + (uint32_t)(c[r3] == k);
+    h += (uint32_t)(c[r0] == k) << (x >= mid ? 16 : 0);
+    h += (uint32_t)(c[r1] == k) << (x + step >= mid ? 16 : 0);
+    h += (uint32_t)(c[r2] == k) << (x + 2u * step >= mid ? 16 : 0);
+    h += (uint32_t)(c[r3] == k) << (x + 3u * step >= mid ? 16 : 0);
   }
-  for (; x < e; x += step) h += c[rows[x]] == k;
+  for (; x < e; x += step) h += (uint32_t)(c[rows[x]] == k) << (x >= mid ? 16 : 0);
   return h;
 }
 
 // The same with two columns, both of which must match.
 __device__ __forceinline__ uint32_t count_matches2(const uint16_t* rows, const int32_t* ca,
                                                    const int32_t* cb, int32_t ka, int32_t kb,
-                                                   uint32_t b, uint32_t e, uint32_t step) {
+                                                   uint32_t b, uint32_t mid, uint32_t e,
+                                                   uint32_t step) {
   uint32_t h = 0, x = b;
   for (; x + 1u * step < e; x += 2u * step) {
     const int r0 = rows[x], r1 = rows[x + step];
-    h += (uint32_t)((ca[r0] == ka) & (cb[r0] == kb)) + (uint32_t)((ca[r1] == ka) & (cb[r1] == kb));
+    h += (uint32_t)((ca[r0] == ka) & (cb[r0] == kb)) << (x >= mid ? 16 : 0);
+    h += (uint32_t)((ca[r1] == ka) & (cb[r1] == kb)) << (x + step >= mid ? 16 : 0);
   }
   for (; x < e; x += step) {
     const int r = rows[x];
-    h += (uint32_t)((ca[r] == ka) & (cb[r] == kb));
+    h += (uint32_t)((ca[r] == ka) & (cb[r] == kb)) << (x >= mid ? 16 : 0);
   }
   return h;
 }
@@ -1499,14 +1507,16 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
             const int32_t kA = j == 0 ? e_kA.x : e_kA.y;
             if (nchk == 1) {
               const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
-              hp = count_matches1(rows, ca, kA, beg + sub, mid, tpe);
-              hn = count_matches1(rows, ca, kA, mid + sub, end, tpe);
+              const uint32_t h = count_matches1(rows, ca, kA, beg + sub, mid, end, tpe);
+              hp = h & 0xffffu;
+              hn = h >> 16;
             } else if (nchk == 2) {
               const int32_t kB = j == 0 ? e_kB.x : e_kB.y;
               const int32_t* ca = raw + ((meta >> 12) & 7u) * kTileStride;
               const int32_t* cb = raw + ((meta >> 16) & 7u) * kTileStride;
-              hp = count_matches2(rows, ca, cb, kA, kB, beg + sub, mid, tpe);
-              hn = count_matches2(rows, ca, cb, kA, kB, mid + sub, end, tpe);
+              const uint32_t h = count_matches2(rows, ca, cb, kA, kB, beg + sub, mid, end, tpe);
+              hp = h & 0xffffu;
+              hn = h >> 16;
             } else {
               // More than two checked columns: keys from the key table.
               const LitDesc& d = a.lits[lit_begin + L];
