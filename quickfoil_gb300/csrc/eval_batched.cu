@@ -1473,6 +1473,17 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
             Lrun = -1;
           }
         }
+        // Both entries' home slots first, so their shared-memory round trips
+        // overlap; a key that is not in its home slot probes onwards.
+        uint32_t hslot[2], hw[2], hown[2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+          hslot[j] = mix32((uint32_t)(j == 0 ? e_k0.x : e_k0.y)) & (kSlots - 1);
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          hw[j] = cnt[hslot[j]];
+          hown[j] = owner[hslot[j]];
+        }
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
           if (!(j == 0 ? have : have1)) continue;
@@ -1486,12 +1497,14 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
             Lrun = L;
           }
           if (!((meta >> 10) & 1u)) continue;
-          uint32_t slot = mix32((uint32_t)k0) & (kSlots - 1);
-          uint32_t w = 0;
-          for (int probe = 0; probe < kSlots; ++probe) {
-            w = cnt[slot];
-            if (w == 0u || (int32_t)owner[slot] == k0) break;
-            slot = (slot + 1) & (kSlots - 1);
+          uint32_t slot = hslot[j];
+          uint32_t w = hw[j];
+          if (w != 0u && (int32_t)hown[j] != k0) {
+            for (int probe = 1; probe < kSlots; ++probe) {
+              slot = (slot + 1) & (kSlots - 1);
+              w = cnt[slot];
+              if (w == 0u || (int32_t)owner[slot] == k0) break;
+            }
           }
           if (w == 0u) continue;
           const uint32_t P = w & 0xffffu, N = w >> 16;
