@@ -1021,41 +1021,74 @@ __global__ void __launch_bounds__(32 * kGatherWarps) gather_entries_kernel(EvalA
     }
     if (lane == 0) lstart[m] = run;
     __syncwarp();
-    for (uint32_t j = lane; j < U.ecnt; j += 32) {
-      const uint32_t f = U.f0 + j;
-      int lo = 0, hi = m - 1;  // largest L with lstart[L] <= f
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (lstart[mid] <= f) lo = mid; else hi = mid - 1;
+    // Four entries a lane at a time, each step for all four together so
+    // their round trips overlap: the literal (a branch-free binary search of
+    // the literal starts), its descriptor, the key columns, the record.
+    int top = 1;
+    while (top * 2 <= m) top *= 2;
+    for (uint32_t jb = 0; jb < U.ecnt; jb += 4 * 32) {
+      uint32_t f[4], e[4];
+      int lo[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        f[q] = U.f0 + jb + (uint32_t)(lane + 32 * q);
+        lo[q] = 0;  // largest L with lstart[L] <= f
       }
-      const LitDesc& d = a.lits[G.lit_begin + lo];
-      const uint32_t e = le0[lo] + (f - lstart[lo]);
-      const int32_t* kp = d.keys;
-      const int nk = d.nk;
-      const int32_t k0 = __ldg(kp + e);
-      int32_t kA = 0, kB = 0;
-      uint32_t nchk = 0, colA = 0, colB = 0, ok0 = 1;
-      for (int q = 1; q < nk; ++q) {
-        const int ac = d.atom_col[q];
-        const int32_t kq = __ldg(kp + q * d.stride + e);
-        if (ac == 0) {
-          ok0 &= kq == k0 ? 1u : 0u;
-        } else {
-          if (nchk == 0) { kA = kq; colA = (uint32_t)ac; }
-          else if (nchk == 1) { kB = kq; colB = (uint32_t)ac; }
-          ++nchk;
+      for (int step = top; step > 0; step >>= 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (lo[q] + step < m && lstart[lo[q] + step] <= f[q]) lo[q] += step;
+      }
+      const LitDesc* d[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        d[q] = a.lits + G.lit_begin + lo[q];
+        e[q] = le0[lo[q]] + (f[q] - lstart[lo[q]]);
+      }
+      int32_t k[4][3];
+      int nk[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool valid = jb + (uint32_t)(lane + 32 * q) < U.ecnt;
+        nk[q] = valid ? d[q]->nk : 0;
+        const int32_t* kp = d[q]->keys;
+        const int64_t st = d[q]->stride;
+        k[q][0] = nk[q] > 0 ? __ldg(kp + e[q]) : 0;
+        k[q][1] = nk[q] > 1 ? __ldg(kp + st + e[q]) : 0;
+        k[q][2] = nk[q] > 2 ? __ldg(kp + 2 * st + e[q]) : 0;
+      }
+      int32_t mlt[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) mlt[q] = nk[q] > 0 ? __ldg(d[q]->mult + e[q]) : 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (nk[q] == 0) continue;
+        const LitDesc& dd = *d[q];
+        const int32_t k0 = k[q][0];
+        int32_t kA = 0, kB = 0;
+        uint32_t nchk = 0, colA = 0, colB = 0, ok0 = 1;
+        for (int c = 1; c < nk[q]; ++c) {
+          const int ac = dd.atom_col[c];
+          const int32_t kc = c == 1 ? k[q][1] : c == 2 ? k[q][2] : __ldg(dd.keys + c * dd.stride + e[q]);
+          if (ac == 0) {
+            ok0 &= kc == k0 ? 1u : 0u;
+          } else {
+            if (nchk == 0) { kA = kc; colA = (uint32_t)ac; }
+            else if (nchk == 1) { kB = kc; colB = (uint32_t)ac; }
+            ++nchk;
+          }
         }
+        if (nchk > 2) {
+          nchk = 3;
+          kA = (int32_t)e[q];
+        }
+        const uint32_t r = U.eoff + jb + (uint32_t)(lane + 32 * q);
+        a.rec.k0[r] = k0;
+        a.rec.kA[r] = kA;
+        a.rec.kB[r] = kB;
+        a.rec.mult[r] = mlt[q];
+        a.rec.meta[r] = (uint32_t)lo[q] | (nchk << 8) | (ok0 << 10) | (colA << 12) | (colB << 16);
       }
-      if (nchk > 2) {
-        nchk = 3;
-        kA = (int32_t)e;
-      }
-      const uint32_t r = U.eoff + j;
-      a.rec.k0[r] = k0;
-      a.rec.kA[r] = kA;
-      a.rec.kB[r] = kB;
-      a.rec.mult[r] = __ldg(d.mult + e);
-      a.rec.meta[r] = (uint32_t)lo | (nchk << 8) | (ok0 << 10) | (colA << 12) | (colB << 16);
     }
     __syncwarp();
   }
