@@ -222,11 +222,14 @@ __device__ __forceinline__ int lane_of(const int4& v, int k) {
   return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
 }
 
+constexpr int kHistCopies = 8;  // histogram copies of a CTA (warp w counts into copy w mod 8)
+
 template <bool kVec>
-__device__ __forceinline__ void bpart_hist_body(const BPartArgs& a, uint32_t* p1) {
+__device__ __forceinline__ void bpart_hist_body(const BPartArgs& a, uint32_t (*hc)[2 << kMaxCoarseBits]) {
   const int np1 = 2 << a.cbits;
-  for (int i = threadIdx.x; i < np1; i += blockDim.x) p1[i] = 0;
+  for (int i = threadIdx.x; i < kHistCopies * np1; i += blockDim.x) hc[i / np1][i % np1] = 0;
   __syncthreads();
+  uint32_t* p1 = hc[warp_id() % kHistCopies];
   int64_t r0, r1;
   cta_range4(a.n, &r0, &r1);
   const int32_t* __restrict__ key = a.cols[0];
@@ -240,6 +243,16 @@ __device__ __forceinline__ void bpart_hist_body(const BPartArgs& a, uint32_t* p1
     const int4* __restrict__ kv = reinterpret_cast<const int4*>(key + r0);
     const int64_t step = blockDim.x;
     int64_t v = threadIdx.x;
+    for (; v + 3 * step < nv; v += 4 * step) {
+      int4 kk[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) kk[u] = __ldg(kv + v + u * step);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) count(lane_of(kk[u], k), r0 + 4 * (v + u * step) + k);
+      }
+    }
     for (; v + step < nv; v += 2 * step) {
       const int4 k0 = __ldg(kv + v), k1 = __ldg(kv + v + step);
 #pragma unroll
@@ -257,18 +270,20 @@ __device__ __forceinline__ void bpart_hist_body(const BPartArgs& a, uint32_t* p1
   for (int64_t r = rs + threadIdx.x; r < r1; r += blockDim.x) count(key[r], r);
   __syncthreads();
   for (int i = threadIdx.x; i < np1; i += blockDim.x) {
-    const uint32_t c = p1[i];
+    uint32_t c = 0;
+#pragma unroll
+    for (int h = 0; h < kHistCopies; ++h) c += hc[h][i];
     a.p1_base[(int64_t)blockIdx.x * np1 + i] = c ? atomicAdd(&a.p1_tot[i], c) : 0u;
   }
 }
 
 __global__ void __launch_bounds__(kPartThreads, 1) bpart_hist_kernel(const BPartArgs* __restrict__ A) {
-  __shared__ uint32_t p1[2 << (kMaxCoarseBits + 1)];
+  __shared__ uint32_t hc[kHistCopies][2 << kMaxCoarseBits];
   const BPartArgs& a = A[blockIdx.y];
   if (a.vec)
-    bpart_hist_body<true>(a, p1);
+    bpart_hist_body<true>(a, hc);
   else
-    bpart_hist_body<false>(a, p1);
+    bpart_hist_body<false>(a, hc);
 }
 
 // Round processing.  A round is up to kPassRows consecutive rows of one
@@ -898,6 +913,7 @@ __global__ void __launch_bounds__(256) plan_units_kernel(EvalArgs a) {
       if (u.Pp + u.Np > 0) {
         const int rshift = kRelPartitionBits - G.bits;
         const uint32_t q0 = p << rshift, q1 = (p + 1) << rshift;
+#pragma unroll 4
         for (int L = G.lit_begin; L < G.lit_end; ++L) {
           const uint32_t* off = a.lits[L].offsets;
           E += __ldg(off + q1) - __ldg(off + q0);
