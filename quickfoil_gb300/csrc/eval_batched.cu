@@ -1122,6 +1122,27 @@ __device__ __forceinline__ long long seg_scan(long long v, int seg) {
   return v;
 }
 
+// Per-CTA int64 accumulators updated as (low, high) 32-bit word pairs: the
+// low word's atomic tells whether it wrapped, and the carry goes into the
+// high word with the value's high half.  Concurrent adds each carry their
+// own wrap, so the pair always sums exactly (shared-memory 32-bit atomics
+// are native; 64-bit adds are not).
+__device__ __forceinline__ void acc_add32(uint32_t* p, unsigned long long v) {
+  const uint32_t lo = (uint32_t)v, hi = (uint32_t)(v >> 32);
+  const uint32_t old = atomicAdd(p, lo);
+  const uint32_t c = hi + ((old + lo < old) ? 1u : 0u);
+  if (c != 0u) atomicAdd(p + 1, c);
+}
+
+__device__ __forceinline__ void flush_acc32(unsigned long long* dst, long long cp, long long cn,
+                                            long long bp, long long bn) {
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  if (cp) acc_add32(d + 0, (unsigned long long)cp);
+  if (cn) acc_add32(d + 2, (unsigned long long)cn);
+  if (bp) acc_add32(d + 4, (unsigned long long)bp);
+  if (bn) acc_add32(d + 6, (unsigned long long)bn);
+}
+
 __device__ __forceinline__ void flush_acc(unsigned long long* dst, long long cp, long long cn,
                                           long long bp, long long bn) {
   if (cp) atomicAdd(dst + 0, as_ull(cp));
@@ -1373,15 +1394,24 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
   // comes from the unit's last chunk.
   long long bp = 0, bn = 0, cp = 0, cn = 0;
   int Lrun = -1;
-  auto reduce_sums = [&](int lit_begin) {
-    cp = seg_scan(cp, Lrun);
-    cn = seg_scan(cn, Lrun);
+  auto reduce_sums = [&](int lit_begin, bool small) {
+    if (small) {
+      // Fewer than 2^20 rows in the unit: a lane's covered counts stay below
+      // 2^24 (at most 16 entries), their 32-lane sums below 2^29, so both
+      // counts travel in one 64-bit scan.
+      const long long c2 = seg_scan(cp | (cn << 32), Lrun);
+      cp = c2 & 0xffffffffll;
+      cn = (long long)((unsigned long long)c2 >> 32);
+    } else {
+      cp = seg_scan(cp, Lrun);
+      cn = seg_scan(cn, Lrun);
+    }
     bp = seg_scan(bp, Lrun);
     bn = seg_scan(bn, Lrun);
     const int next_L = __shfl_down_sync(kFullMask, Lrun, 1);
     const bool seg_end = lane_id() == 31 || next_L != Lrun;
     if (seg_end && Lrun >= 0 && (cp | cn | bp | bn) != 0)
-      flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
+      flush_acc32(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
     bp = bn = cp = cn = 0;
     Lrun = -1;
   };
@@ -1517,7 +1547,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
           if (!have && Lrun >= 0) {
             // No entry in this chunk: the thread's sums go now, so at the
             // unit's end every lane's literal is from the last chunk.
-            if ((cp | cn | bp | bn) != 0) flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
+            if ((cp | cn | bp | bn) != 0) flush_acc32(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
             bp = bn = cp = cn = 0;
             Lrun = -1;
           }
@@ -1541,7 +1571,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
           const int L = (int)(meta & 0xffu);
           if (L != Lrun) {
             if (Lrun >= 0 && (cp | cn | bp | bn) != 0)
-              flush_acc(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
+              flush_acc32(acc + 4 * (lit_begin + Lrun), cp, cn, bp, bn);
             bp = bn = cp = cn = 0;
             Lrun = L;
           }
@@ -1617,7 +1647,7 @@ __global__ void __launch_bounds__(kEvalThreads, 3) eval_batched_kernel(EvalArgs 
     if (s_abort != 0u) break;  // read after the barrier that follows the wait
     const uint32_t next = cur == 2u ? 0u : cur + 1u;
     load_entries(next);
-    reduce_sums(lit_begin);
+    reduce_sums(lit_begin, total < (1u << 20));
     cur = next;
   }
   consumer_sync();
