@@ -22,12 +22,13 @@
 // top_bits(mix32(B[j])) and label (positives first), carrying the join
 // column and the atom columns the group's literals test.  The evaluation
 // kernel is persistent: each CTA repeatedly takes a (group, partition) work
-// item, loads that binding partition into shared memory, builds a
-// shared-memory table of its distinct join keys (atomicCAS on slot owners)
-// with per-label row counts and per-key row lists, and then streams, for
-// every literal of the group, the relation key tuples of the same partition
-// range through it.  Counts are reduced with warp shuffles into per-CTA
-// int64 accumulators and flushed to global memory once per CTA.
+// item, loads that binding partition into shared memory (a producer warp
+// feeding TMA bulk copies), builds a shared-memory table of its distinct
+// join keys (atomicCAS on slot owners) with per-label row counts and per-key
+// row lists, and then streams, for every literal of the group, the relation
+// key tuples of the same partition range through it.  Counts are reduced
+// with warp shuffles into per-CTA int64 accumulators and flushed to global
+// memory once per CTA.
 #include <algorithm>
 #include <cstring>
 #include <set>
@@ -730,32 +731,35 @@ bpart_pass2_kernel(const BPartArgs* __restrict__ A) {
 // ----------------------------------------------------------------------------
 // Persistent evaluation kernel.
 //
-// Work unit = a range of at most kUnitEntries relation entries of one (group,
-// partition) item.  Three launches per literal batch:
+// Work unit = a range of at most kChunk relation entries of one (group,
+// partition) item; evaluation unit = up to kUnitEntries / kChunk consecutive
+// units of one item.  Three launches per literal batch:
 //   plan_units   lists the units: each item's segment bounds and the number
 //                of relation entries its literals hold in the item's key
-//                range; items without rows or entries are dropped, items
+//                range; items without rows or entries are dropped, the
+//                entries of an item are cut into units of kChunk (one gather
+//                warp each) with a block of entry records apiece, and items
 //                with more than kUnitEntries entries (hot join keys of skewed
-//                relations) are split so no CTA is left with a long tail,
-//                and every unit gets a block of entry records;
+//                relations) into several evaluation units, so no CTA is left
+//                with a long tail;
 //   gather       one warp per unit forms the item's literal-major entry
 //                space and writes the unit's entry records (join key, up to
 //                two further keys, multiplicity, literal and check columns)
 //                into its block, so the evaluation loads them with one
 //                coalesced round trip;
-//   eval         per unit (its record loaded while the previous unit ran):
-//                each thread loads its entry records; the partition's
-//                binding rows arrive by cp.async copies of 16-byte chunks
-//                (one aligned run per column and label), shared by all
-//                threads and put in flight as soon as the previous tile had
-//                been probed, completing on an mbarrier; a key table of the
-//                tile is built with one 32-bit atomicCAS per new key, whose
-//                count atomics also give every row its rank within its key
-//                and label; for groups with atom literals each key takes a
-//                run of the row list by a warp-aggregated atomic and its
-//                rows are placed there (positives first); the entries probe the table and check the
-//                key's rows against their further keys; per-literal sums are
-//                combined with a segmented warp scan into per-CTA int64
+//   eval         a producer warp claims evaluation units, publishes each
+//                record one unit ahead and feeds the tiles (the partition's
+//                binding rows, one 16-byte aligned run per column and label)
+//                by TMA bulk copies on full/empty mbarriers; eight consumer
+//                warps load a unit's first entry records as soon as its
+//                record is published, build a key table of the tile (one
+//                32-bit atomicCAS per new key, whose count atomics also give
+//                every row its rank within its key and label), give each key
+//                a run of the row list by a warp-aggregated atomic and place
+//                its rows there (positives first), then probe the table with
+//                the unit's entries kChunk at a time and check each key's
+//                rows against the entries' further keys; per-literal sums
+//                are combined with a segmented warp scan into per-CTA int64
 //                accumulators, flushed to global memory when the CTA retires.
 
 struct GroupDesc {
