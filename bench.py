@@ -69,6 +69,8 @@ def parse_args():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop leg")
     ap.add_argument("--no-coverage", action="store_true",
                     help="skip the coverage, test-runner and loader legs")
+    ap.add_argument("--no-operators", action="store_true",
+                    help="skip the leg timing the reference's operators kept at the C ABI")
     ap.add_argument("--no-learn", action="store_true",
                     help="skip the full-scale learn-loop (config 4) leg")
     return ap.parse_args()
@@ -383,9 +385,12 @@ def run_gb300(args):
 
     # The API-kept RadixPartition (qfg_radix_partition, the reference layout)
     # on one binding column at 15 radix bits, against 12 bytes a row.
-    radix = None
+    radix = operators = None
     if args.workload == "batched_step" and rank == 0:
         radix = run_radix_partition(eng, dev_cols[0], stream, torch, measured_peak_hbm()[0])
+        if not args.no_operators:
+            operators = run_operators(eng, w, b, dev_cols, stream, torch, measured_peak_hbm()[0],
+                                      batched_counts)
 
     # End to end through the C ABI from pinned host buffers.
     pinned = [torch.from_numpy(c).pin_memory() for c in w.binding_columns]
@@ -514,6 +519,8 @@ def run_gb300(args):
             line["serving"] = serving
         if radix is not None:
             line["radix_partition"] = radix
+        if operators is not None:
+            line["operators"] = operators
         if learn is not None:
             line["learn_loop"] = learn
         if coverage is not None:
@@ -570,6 +577,82 @@ def run_radix_partition(eng, values, stream, torch, peak, bits: int = 15, reps: 
     return {"kernel": "qfg_radix_partition (two stable 7/8-bit passes)", "rows": n, "bits": bits,
             "ms": ms, "algorithmic_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9,
             "frac": alg / (ms * 1e-3) / 1e9 / peak, "peak": peak, "stable_partition": ok}
+
+
+def run_operators(eng, w, b, dev_cols, stream, torch, peak, counts, reps: int = 3):
+    """The reference's operators kept at the C ABI, each timed with CUDA events
+    on the context stream over `reps` calls, at the batched step's sizes:
+    BuildHashTableOnPartitions over the 15-bit RadixPartition of one 32M-row
+    binding column, BuildHashTableOnTable over the largest relation's first
+    column, LeftSemiJoin and RightSemiJoin of that binding column against the
+    relation's column, and the label-aware extension of the binding set by
+    one of the step's literals.  Bytes are the arrays each call reads and
+    writes, once each; the fraction is against the measured copy peak."""
+    from quickfoil_gb300 import _capi as C
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(reps):
+            out = fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps, out
+
+    def entry(name, ms, nbytes, **extra):
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        return dict(name=name, ms=round(ms, 4), bytes=int(nbytes), achieved_gbs=round(gbs, 1),
+                    frac=round(gbs / peak, 4), **extra)
+
+    out = []
+    col = dev_cols[0]
+    n = col.numel()
+    bits = 15
+    tuples, offsets = eng.radix_partition(col, bits)
+    ms, res = timed(lambda: eng.build_hash_table_on_partitions(tuples, offsets, bits))
+    buckets, bucket_offsets, masks, nxt = res
+    io = 8 * n + 8 * offsets.numel() + 4 * buckets.numel() + 8 * bucket_offsets.numel() + \
+        4 * masks.numel() + 4 * nxt.numel()
+    out.append(entry("qfg_build_hash_table_on_partitions", ms, io, rows=n, bits=bits))
+    rel = max(w.relations, key=lambda r: len(r[0]))
+    rkey = torch.from_numpy(rel[0]).to(col.device)
+    m = rkey.numel()
+    ms, res = timed(lambda: eng.build_hash_table_on_table([rkey]))
+    io = 4 * m + 4 * res[0].numel() + 4 * res[1].numel()
+    out.append(entry("qfg_build_hash_table_on_table", ms, io, rows=m))
+    ms, res = timed(lambda: eng.left_semijoin([col], [rkey]))
+    out.append(entry("qfg_left_semijoin", ms, 4 * n + 4 * m + 8 * res[0].numel(), probe_rows=n,
+                     build_rows=m, ones=int(res[1])))
+    ms, res = timed(lambda: eng.right_semijoin([col], [rkey]))
+    out.append(entry("qfg_right_semijoin", ms, 4 * n + 4 * m + 8 * res[0].numel(), probe_rows=n,
+                     build_rows=m, ones=int(res[1])))
+    # Extension by the step literal with the fewest binding pairs above 1M.
+    pairs = counts[:, 2] + counts[:, 3]
+    pick = [i for i in np.argsort(pairs) if pairs[i] >= 1_000_000]
+    if pick:
+        i = int(pick[0])
+        lit = w.literals[i]
+        npos, nneg = int(counts[i, 2]), int(counts[i, 3])
+        nb = eng.extend_bindings(b, lit, npos, nneg)
+        nb.close()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        total = 0.0
+        for _ in range(reps):
+            ev0.record(stream)
+            nb = eng.extend_bindings(b, lit, npos, nneg)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            total += ev0.elapsed_time(ev1)
+            ncols_out = nb.num_columns
+            nb.close()
+        ms = total / reps
+        io = 4 * b.num_columns * b.num_tuples + 4 * ncols_out * (npos + nneg)
+        out.append(entry("qfg_extend_bindings", ms, io, rows_in=b.num_tuples,
+                         rows_out=npos + nneg, columns_out=ncols_out))
+    return out
 
 
 def run_learn_loop(torch):
