@@ -292,6 +292,9 @@ int qfg_server_wait(qfg_server* server, int64_t request_id);
 int qfg_server_drain(qfg_server* server);
 int qfg_server_stats(qfg_server* server, double* p50_ms, double* p99_ms, int64_t* completed,
                      int64_t* peak_in_flight);
+/* Starts the statistics afresh (latencies, completed count, peak in flight),
+ * e.g. after a warm-up that allocated the slots' scratch. */
+int qfg_server_reset_stats(qfg_server* server);
 int qfg_server_destroy(qfg_server* server);
 
 /* ---- API-kept operators (device pointers, context stream) -------------- */

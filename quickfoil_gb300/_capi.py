@@ -122,6 +122,7 @@ SIGNATURES = [
     ("qfg_server_drain", ctypes.c_int, [c_vp]),
     ("qfg_server_stats", ctypes.c_int,
      [c_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), c_i64p, c_i64p]),
+    ("qfg_server_reset_stats", ctypes.c_int, [c_vp]),
     ("qfg_server_destroy", ctypes.c_int, [c_vp]),
     ("qfg_radix_partition", ctypes.c_int,
      [c_vp, c_vp, ctypes.c_int64, ctypes.c_int, c_vp, c_vp]),

@@ -522,6 +522,15 @@ extern "C" int qfg_server_stats(qfg_server* s, double* p50_ms, double* p99_ms, i
   return QFG_OK;
 }
 
+extern "C" int qfg_server_reset_stats(qfg_server* s) {
+  if (s == nullptr) return QFG_ERR_INVALID;
+  s->latencies_ms.clear();
+  int64_t running = 0;
+  for (const Slot& slot : s->slots) running += (int64_t)slot.running.size();
+  s->peak_in_flight = running;
+  return QFG_OK;
+}
+
 extern "C" int qfg_server_destroy(qfg_server* s) {
   if (s == nullptr) return QFG_ERR_INVALID;
   qfg_server_drain(s);

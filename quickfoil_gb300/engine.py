@@ -668,6 +668,10 @@ class StepServer:
         return {"p50_ms": p50.value, "p99_ms": p99.value, "completed": done.value,
                 "peak_in_flight": peak.value}
 
+    def reset_stats(self):
+        C.check(self.engine.lib.qfg_server_reset_stats(self.handle), self.engine.ctx,
+                "qfg_server_reset_stats")
+
     def close(self):
         if self.handle:
             self.engine.lib.qfg_server_destroy(self.handle)
