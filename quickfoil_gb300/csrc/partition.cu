@@ -313,34 +313,6 @@ PassShape pass_shape(int64_t n, int bits) {
   return s;
 }
 
-template <class IO>
-int stable_pass(Ctx* ctx, IO io, int64_t n, int shift, int bits, int64_t* digit_offsets) {
-  const PassShape s = pass_shape(n, bits);
-  const int64_t entries = s.num_chunks * (int64_t(1) << bits);
-  QFG_TRY(ctx->scratch[kScrHist].reserve(ctx, sizeof(uint32_t) * (size_t)entries));
-  uint32_t* hist = ctx->scratch[kScrHist].as<uint32_t>();
-  if (s.smem > 48 * 1024) {
-    QFG_CUDA(ctx, cudaFuncSetAttribute(stable_hist_kernel<IO>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem));
-    QFG_CUDA(ctx, cudaFuncSetAttribute(stable_scatter_kernel<IO>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem));
-  }
-  stable_hist_kernel<IO><<<s.grid, 32 * s.warps, s.smem, ctx->stream>>>(io, n, shift, bits, s.chunk,
-                                                                        s.num_chunks, hist);
-  QFG_LAUNCHED(ctx);
-  QFG_TRY(exclusive_scan_u32(ctx, hist, hist, entries, nullptr));
-  if (digit_offsets != nullptr) {
-    const uint32_t P = 1u << bits;
-    digit_offsets_kernel<<<(P + 256) / 256, 256, 0, ctx->stream>>>(hist, s.num_chunks, bits, n,
-                                                                   digit_offsets);
-    QFG_LAUNCHED(ctx);
-  }
-  stable_scatter_kernel<IO><<<s.grid, 32 * s.warps, s.smem, ctx->stream>>>(
-      io, n, shift, bits, s.chunk, s.num_chunks, hist);
-  QFG_LAUNCHED(ctx);
-  return QFG_OK;
-}
-
 // One stable partition pass with the round kernels (bits <= kRTMaxBits):
 // per-CTA digit counts, a digit-major scan, the staged scatter.
 template <class IO>
@@ -383,13 +355,19 @@ int stable_sort_pairs(Ctx* ctx, uint32_t* k0, int32_t* p0, uint32_t* k1, int32_t
   int32_t* pin = p0;
   uint32_t* kout = k1;
   int32_t* pout = p1;
-  const int passes = std::max(1, (key_bits + 11) / 12);
+  if (n <= 0) {
+    *k_out = kin;
+    *p_out = pin;
+    return QFG_OK;
+  }
+  // Passes of at most kRTMaxBits bits through the staged round kernels.
+  const int passes = std::max(1, (key_bits + kRTMaxBits - 1) / kRTMaxBits);
   const int step = (key_bits + passes - 1) / passes;
   int shift = 0;
   for (int pass = 0; pass < passes; ++pass) {
     const int bits = std::max(1, std::min(step, key_bits - shift));
     SortIO io{kin, pass == 0 ? nullptr : pin, kout, pout};
-    QFG_TRY(stable_pass(ctx, io, n, shift, bits, nullptr));
+    QFG_TRY(round_pass(ctx, io, n, shift, bits, nullptr));
     shift += bits;
     std::swap(kin, kout);
     std::swap(pin, pout);
