@@ -278,6 +278,7 @@ __global__ void asj_probe_kernel(const int32_t* __restrict__ buckets, const int3
   const int64_t nw = (n_ex + 31) >> 5;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  unsigned long long c = 0;
   for (int64_t w = warp; w < nw; w += nwarps) {
     const int64_t e = (w << 5) + lane_id();
     bool hit = false;
@@ -294,9 +295,11 @@ __global__ void asj_probe_kernel(const int32_t* __restrict__ buckets, const int3
     const unsigned word = __ballot_sync(kFullMask, hit);
     if (lane_id() == 0) {
       if (words != nullptr) words[w] = word;
-      if (word != 0u) atomicAdd(count, (unsigned long long)__popc(word));
+      c += (unsigned long long)__popc(word);
     }
   }
+  // One count a warp, not one a word: the words' atomics would share one address.
+  if (lane_id() == 0 && c != 0) atomicAdd(count, c);
 }
 
 }  // namespace

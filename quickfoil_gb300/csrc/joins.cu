@@ -6,8 +6,9 @@
 //
 // LeftSemiJoin / RightSemiJoin (operations/LeftSemiJoin.hpp:55-141,
 // operations/RightSemiJoin.hpp:44-82) only need membership: the rows of the
-// other side look their tuple up and a warp turns 32 answers into one 32-bit
-// word with __ballot_sync.  Two consecutive words form one 64-bit block of
+// other side check a bit filter of the set side's key tuples, look up the
+// tuples that pass, and a warp turns 32 answers into one 32-bit word with
+// __ballot_sync.  Two consecutive words form one 64-bit block of
 // the reference's BitVector (dynamic_bitset<unsigned long>, little-endian
 // bit order), so the output is byte-identical; bits past the last row stay
 // zero as the reference requires (utility/BitVectorBuilder.hpp:46-54).
@@ -33,21 +34,73 @@ namespace qfg {
 
 namespace {
 
+// Set side's filter: bit (hash >> (32 - fbits)) of every set row's key tuple
+// (the key set's slots use the hash's low bits).  A probe row whose bit is
+// clear has no match, so most misses never touch the key set.  Built only
+// when the probed side is at least twice the set side: otherwise building it
+// costs about what it saves.
+__global__ void semijoin_filter_kernel(KeyCols set, int64_t n, uint32_t* __restrict__ filter,
+                                       int fbits) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t b = keys_hash<0>(set, r) >> (32 - fbits);
+    // Repeated keys find their bit set and spare the word's atomics.
+    if (!((filter[b >> 5] >> (b & 31)) & 1u)) atomicOr(&filter[b >> 5], 1u << (b & 31));
+  }
+}
+
+template <int NK>
 __global__ void semijoin_bits_kernel(KeyCols build, const int32_t* __restrict__ owner, uint32_t mask,
+                                     const uint32_t* __restrict__ filter, int fbits,
                                      KeyCols probe, int64_t n, uint32_t* __restrict__ words,
                                      int64_t nwords, unsigned long long* __restrict__ ones) {
   const int64_t warps_total = (int64_t)gridDim.x * blockDim.x / 32;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = lane_id();
-  for (int64_t w = gw; w < nwords; w += warps_total) {
-    const int64_t i = w * 32 + lane;
-    const bool hit = i < n && keyset_find(build, owner, mask, probe, i) >= 0;
-    const unsigned ball = __ballot_sync(kFullMask, hit);
-    if (lane == 0) {
-      if (words != nullptr) words[w] = ball;
-      if (ball != 0u) atomicAdd(ones, (unsigned long long)__popc(ball));
+  constexpr int W = 4;  // words a warp keeps in flight: the lookups are latency-bound
+  unsigned long long c = 0;
+  for (int64_t w0 = gw; w0 < nwords; w0 += warps_total * W) {
+    uint32_t h[W];
+    bool live[W];
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      const int64_t i = (w0 + u * warps_total) * 32 + lane;
+      live[u] = i < n;
+      h[u] = live[u] ? keys_hash<NK>(probe, i) : 0u;
+    }
+    if (fbits > 0) {
+#pragma unroll
+      for (int u = 0; u < W; ++u) {
+        const uint32_t b = h[u] >> (32 - fbits);
+        if (live[u]) live[u] = (__ldg(filter + (b >> 5)) >> (b & 31)) & 1u;
+      }
+    }
+    int32_t o[W];
+#pragma unroll
+    for (int u = 0; u < W; ++u) o[u] = live[u] ? owner[h[u] & mask] : -1;
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      const int64_t i = (w0 + u * warps_total) * 32 + lane;
+      bool hit = false;
+      uint32_t slot = h[u] & mask;
+      for (uint32_t p = 0; p <= mask && o[u] >= 0; ++p) {
+        if (keys_eq<NK>(build, o[u], probe, i)) {
+          hit = true;
+          break;
+        }
+        slot = (slot + 1) & mask;
+        o[u] = owner[slot];
+      }
+      const int64_t w = w0 + u * warps_total;
+      const unsigned ball = __ballot_sync(kFullMask, hit);
+      if (lane == 0 && w < nwords) {
+        if (words != nullptr) words[w] = ball;
+        c += (unsigned long long)__popc(ball);
+      }
     }
   }
+  // One count a warp: a count a word serialises a million atomics on one address.
+  if (lane == 0 && c != 0) atomicAdd(ones, c);
 }
 
 // After a stable sort of build rows by representative: first and last
@@ -138,11 +191,38 @@ int semijoin(Ctx* ctx, const KeyCols& set_side, int64_t n_set, const KeyCols& bi
     keyset_insert_kernel<0><<<rows_grid(ctx, n_set), 256, 0, ctx->stream>>>(set_side, n_set, owner,
                                                                          mask, nullptr);
     QFG_LAUNCHED(ctx);
+    // About 8 filter bits a set row (2^16 to 2^28 bits); fbits 0 = no filter.
+    int fbits = 0;
+    const uint32_t* filter = nullptr;
+    if (n_bits >= 2 * n_set) {
+      fbits = 16;
+      while (fbits < 28 && ((int64_t)1 << fbits) < 8 * n_set) ++fbits;
+      const size_t fwords = (size_t)1 << (fbits - 5);
+      QFG_TRY(ctx->scratch[kScrTmpB].reserve(ctx, sizeof(uint32_t) * fwords));
+      uint32_t* f = ctx->scratch[kScrTmpB].as<uint32_t>();
+      QFG_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(uint32_t) * fwords, ctx->stream));
+      semijoin_filter_kernel<<<rows_grid(ctx, n_set), 256, 0, ctx->stream>>>(set_side, n_set, f,
+                                                                            fbits);
+      QFG_LAUNCHED(ctx);
+      filter = f;
+    }
     const unsigned grid = (unsigned)std::max<int64_t>(
         1, std::min<int64_t>((nwords + 7) / 8, (int64_t)ctx->num_sms * 8));
-    semijoin_bits_kernel<<<grid, 256, 0, ctx->stream>>>(set_side, owner, mask, bit_side, n_bits,
-                                                        reinterpret_cast<uint32_t*>(d_bits), nwords,
-                                                        ones);
+    uint32_t* words = reinterpret_cast<uint32_t*>(d_bits);
+    switch (set_side.nk) {
+      case 1:
+        semijoin_bits_kernel<1><<<grid, 256, 0, ctx->stream>>>(set_side, owner, mask, filter, fbits,
+                                                               bit_side, n_bits, words, nwords, ones);
+        break;
+      case 2:
+        semijoin_bits_kernel<2><<<grid, 256, 0, ctx->stream>>>(set_side, owner, mask, filter, fbits,
+                                                               bit_side, n_bits, words, nwords, ones);
+        break;
+      default:
+        semijoin_bits_kernel<0><<<grid, 256, 0, ctx->stream>>>(set_side, owner, mask, filter, fbits,
+                                                               bit_side, n_bits, words, nwords, ones);
+        break;
+    }
     QFG_LAUNCHED(ctx);
   }
   unsigned long long h = 0;
