@@ -49,11 +49,15 @@ __global__ void semijoin_filter_kernel(KeyCols set, int64_t n, uint32_t* __restr
   }
 }
 
+// Probes the key set of `build` with the rows of `probe`.  flag == nullptr:
+// the answers go to 32-row words (and their count to *ones).  Otherwise each
+// matched representative row o gets flag[o] = 1.
 template <int NK>
 __global__ void semijoin_bits_kernel(KeyCols build, const int32_t* __restrict__ owner, uint32_t mask,
                                      const uint32_t* __restrict__ filter, int fbits,
                                      KeyCols probe, int64_t n, uint32_t* __restrict__ words,
-                                     int64_t nwords, unsigned long long* __restrict__ ones) {
+                                     int64_t nwords, unsigned long long* __restrict__ ones,
+                                     uint8_t* __restrict__ flag) {
   const int64_t warps_total = (int64_t)gridDim.x * blockDim.x / 32;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = lane_id();
@@ -91,6 +95,10 @@ __global__ void semijoin_bits_kernel(KeyCols build, const int32_t* __restrict__ 
         slot = (slot + 1) & mask;
         o[u] = owner[slot];
       }
+      if (flag != nullptr) {
+        if (hit && flag[o[u]] == 0) flag[o[u]] = 1;
+        continue;
+      }
       const int64_t w = w0 + u * warps_total;
       const unsigned ball = __ballot_sync(kFullMask, hit);
       if (lane == 0 && w < nwords) {
@@ -100,6 +108,28 @@ __global__ void semijoin_bits_kernel(KeyCols build, const int32_t* __restrict__ 
     }
   }
   // One count a warp: a count a word serialises a million atomics on one address.
+  if (lane == 0 && c != 0) atomicAdd(ones, c);
+}
+
+// Bits of the rows of a key set's own table: row i is in when its
+// representative was marked.
+__global__ void semijoin_rep_bits_kernel(const int32_t* __restrict__ rep,
+                                         const uint8_t* __restrict__ flag, int64_t n,
+                                         uint32_t* __restrict__ words, int64_t nwords,
+                                         unsigned long long* __restrict__ ones) {
+  const int64_t warps_total = (int64_t)gridDim.x * blockDim.x / 32;
+  const int lane = lane_id();
+  unsigned long long c = 0;
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; w < nwords;
+       w += warps_total) {
+    const int64_t i = w * 32 + lane;
+    const int32_t r = i < n ? rep[i] : -1;
+    const unsigned ball = __ballot_sync(kFullMask, r >= 0 && flag[r] != 0);
+    if (lane == 0) {
+      words[w] = ball;
+      c += (unsigned long long)__popc(ball);
+    }
+  }
   if (lane == 0 && c != 0) atomicAdd(ones, c);
 }
 
@@ -184,46 +214,75 @@ int semijoin(Ctx* ctx, const KeyCols& set_side, int64_t n_set, const KeyCols& bi
     if (nwords > 0)
       QFG_CUDA(ctx, cudaMemsetAsync(d_bits, 0, sizeof(uint32_t) * nwords, ctx->stream));
   } else {
-    const uint32_t mask = table_mask(n_set);
+    // The key set holds the smaller side and the larger side probes it.  When
+    // the smaller side is the one that gets bits, the probes mark its
+    // representatives and its rows read their bit through their representative.
+    const bool mark = n_set > n_bits;
+    const KeyCols& small = mark ? bit_side : set_side;
+    const KeyCols& large = mark ? set_side : bit_side;
+    const int64_t n_small = mark ? n_bits : n_set;
+    const int64_t n_large = mark ? n_set : n_bits;
+    const uint32_t mask = table_mask(n_small);
     QFG_TRY(ctx->scratch[kScrJoin].reserve(ctx, sizeof(int32_t) * ((size_t)mask + 1)));
     int32_t* owner = ctx->scratch[kScrJoin].as<int32_t>();
+    int32_t* rep = nullptr;
+    uint8_t* flag = nullptr;
+    if (mark) {
+      QFG_TRY(ctx->scratch[kScrJoin2].reserve(ctx, (sizeof(int32_t) + 1) * (size_t)n_small));
+      rep = ctx->scratch[kScrJoin2].as<int32_t>();
+      flag = reinterpret_cast<uint8_t*>(rep + n_small);
+      QFG_CUDA(ctx, cudaMemsetAsync(flag, 0, (size_t)n_small, ctx->stream));
+    }
     QFG_CUDA(ctx, cudaMemsetAsync(owner, 0xff, sizeof(int32_t) * ((size_t)mask + 1), ctx->stream));
-    keyset_insert_kernel<0><<<rows_grid(ctx, n_set), 256, 0, ctx->stream>>>(set_side, n_set, owner,
-                                                                         mask, nullptr);
+    keyset_insert_kernel<0><<<rows_grid(ctx, n_small), 256, 0, ctx->stream>>>(small, n_small,
+                                                                           owner, mask, rep);
     QFG_LAUNCHED(ctx);
-    // About 8 filter bits a set row (2^16 to 2^28 bits); fbits 0 = no filter.
+    // About 8 filter bits a key-set row (2^16 to 2^28 bits); fbits 0 = no filter.
     int fbits = 0;
     const uint32_t* filter = nullptr;
-    if (n_bits >= 2 * n_set) {
+    if (n_large >= 2 * n_small) {
       fbits = 16;
-      while (fbits < 28 && ((int64_t)1 << fbits) < 8 * n_set) ++fbits;
+      while (fbits < 28 && ((int64_t)1 << fbits) < 8 * n_small) ++fbits;
       const size_t fwords = (size_t)1 << (fbits - 5);
       QFG_TRY(ctx->scratch[kScrTmpB].reserve(ctx, sizeof(uint32_t) * fwords));
       uint32_t* f = ctx->scratch[kScrTmpB].as<uint32_t>();
       QFG_CUDA(ctx, cudaMemsetAsync(f, 0, sizeof(uint32_t) * fwords, ctx->stream));
-      semijoin_filter_kernel<<<rows_grid(ctx, n_set), 256, 0, ctx->stream>>>(set_side, n_set, f,
-                                                                            fbits);
+      semijoin_filter_kernel<<<rows_grid(ctx, n_small), 256, 0, ctx->stream>>>(small, n_small, f,
+                                                                              fbits);
       QFG_LAUNCHED(ctx);
       filter = f;
     }
-    const unsigned grid = (unsigned)std::max<int64_t>(
-        1, std::min<int64_t>((nwords + 7) / 8, (int64_t)ctx->num_sms * 8));
+    // 32-row words of the probing side (the output's words when not marking).
+    const int64_t pwords = mark ? (n_large + 31) / 32 : nwords;
     uint32_t* words = reinterpret_cast<uint32_t*>(d_bits);
-    switch (set_side.nk) {
+    uint32_t* pout = mark ? nullptr : words;
+    const unsigned grid = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((pwords + 7) / 8, (int64_t)ctx->num_sms * 8));
+    switch (small.nk) {
       case 1:
-        semijoin_bits_kernel<1><<<grid, 256, 0, ctx->stream>>>(set_side, owner, mask, filter, fbits,
-                                                               bit_side, n_bits, words, nwords, ones);
+        semijoin_bits_kernel<1><<<grid, 256, 0, ctx->stream>>>(small, owner, mask, filter, fbits,
+                                                               large, n_large, pout, pwords, ones,
+                                                               flag);
         break;
       case 2:
-        semijoin_bits_kernel<2><<<grid, 256, 0, ctx->stream>>>(set_side, owner, mask, filter, fbits,
-                                                               bit_side, n_bits, words, nwords, ones);
+        semijoin_bits_kernel<2><<<grid, 256, 0, ctx->stream>>>(small, owner, mask, filter, fbits,
+                                                               large, n_large, pout, pwords, ones,
+                                                               flag);
         break;
       default:
-        semijoin_bits_kernel<0><<<grid, 256, 0, ctx->stream>>>(set_side, owner, mask, filter, fbits,
-                                                               bit_side, n_bits, words, nwords, ones);
+        semijoin_bits_kernel<0><<<grid, 256, 0, ctx->stream>>>(small, owner, mask, filter, fbits,
+                                                               large, n_large, pout, pwords, ones,
+                                                               flag);
         break;
     }
     QFG_LAUNCHED(ctx);
+    if (mark) {
+      semijoin_rep_bits_kernel<<<(unsigned)std::max<int64_t>(
+                                     1, std::min<int64_t>((nwords + 7) / 8,
+                                                          (int64_t)ctx->num_sms * 8)),
+                                 256, 0, ctx->stream>>>(rep, flag, n_bits, words, nwords, ones);
+      QFG_LAUNCHED(ctx);
+    }
   }
   unsigned long long h = 0;
   QFG_CUDA(ctx, cudaMemcpyAsync(&h, ones, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));

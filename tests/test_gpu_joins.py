@@ -37,6 +37,27 @@ def test_semijoins_exact(engine, k, n_probe, n_build):
         np.testing.assert_array_equal(bits.cpu().numpy().view(np.uint64), wbits)
 
 
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("n_probe,n_build", [(300000, 9000), (9000, 300000), (40000, 30000),
+                                             (30000, 40000)])
+def test_semijoins_wide_domain(engine, k, n_probe, n_build):
+    """Mostly missing keys (the bit filter rejects most probes) and repeated
+    keys, with either side the larger one (the key set is built on the
+    smaller side, whichever side gets the bits)."""
+    rng = np.random.default_rng(1000 * k + n_probe)
+    dom = {1: 60000, 2: 300, 3: 40}[k]
+    probe = [rng.integers(-dom, dom, n_probe).astype(np.int32) for _ in range(k)]
+    build = [rng.integers(-dom, dom, n_build).astype(np.int32) for _ in range(k)]
+    for name in ("left", "right"):
+        fn = engine.left_semijoin if name == "left" else engine.right_semijoin
+        ofn = oracle.left_semijoin if name == "left" else oracle.right_semijoin
+        bits, ones = fn([dev(c) for c in probe], [dev(c) for c in build])
+        wbits, wones = ofn(probe, build)
+        assert 0 < wones < (n_probe if name == "left" else n_build)
+        assert ones == wones
+        np.testing.assert_array_equal(bits.cpu().numpy().view(np.uint64), wbits)
+
+
 def _extension_case(engine, B, P, R, lit):
     rid = _ids[0]
     _ids[0] += 1
