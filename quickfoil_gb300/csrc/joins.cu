@@ -49,10 +49,11 @@ __global__ void semijoin_filter_kernel(KeyCols set, int64_t n, uint32_t* __restr
   }
 }
 
-// Probes the key set of `build` with the rows of `probe`.  flag == nullptr:
-// the answers go to 32-row words (and their count to *ones).  Otherwise each
-// matched representative row o gets flag[o] = 1.
-template <int NK>
+// Probes the key set of `build` with the rows of `probe`.  MARK false: the
+// answers go to 32-row words (and their count to *ones).  MARK true: each
+// matched representative row o gets flag[o] = 1.  The mode is a template
+// argument so that the word form keeps its 32 registers (8 CTAs an SM).
+template <int NK, bool MARK>
 __global__ void semijoin_bits_kernel(KeyCols build, const int32_t* __restrict__ owner, uint32_t mask,
                                      const uint32_t* __restrict__ filter, int fbits,
                                      KeyCols probe, int64_t n, uint32_t* __restrict__ words,
@@ -95,7 +96,7 @@ __global__ void semijoin_bits_kernel(KeyCols build, const int32_t* __restrict__ 
         slot = (slot + 1) & mask;
         o[u] = owner[slot];
       }
-      if (flag != nullptr) {
+      if constexpr (MARK) {
         if (hit && flag[o[u]] == 0) flag[o[u]] = 1;
         continue;
       }
@@ -204,6 +205,33 @@ int make_keycols(Ctx* ctx, const int32_t* const* host_ptrs, int nk, KeyCols* out
   return QFG_OK;
 }
 
+// A grid of as many 256-thread CTAs as fit on the GPU at once (or fewer, 8
+// words a CTA): the probe loop is grid-strided, so a second partial wave
+// would only add a tail.
+template <typename Kernel>
+unsigned resident_grid(Ctx* ctx, Kernel k, int64_t words) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, 0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  return (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>((words + 7) / 8, (int64_t)ctx->num_sms * per_sm));
+}
+
+template <bool MARK>
+int launch_semijoin_probe(Ctx* ctx, int nk, const KeyCols& small, const int32_t* owner,
+                          uint32_t mask, const uint32_t* filter, int fbits, const KeyCols& large,
+                          int64_t n_large, uint32_t* pout, int64_t pwords,
+                          unsigned long long* ones, uint8_t* flag) {
+  auto k = nk == 1 ? semijoin_bits_kernel<1, MARK>
+                   : nk == 2 ? semijoin_bits_kernel<2, MARK> : semijoin_bits_kernel<0, MARK>;
+  k<<<resident_grid(ctx, k, pwords), 256, 0, ctx->stream>>>(small, owner, mask, filter, fbits,
+                                                            large, n_large, pout, pwords, ones,
+                                                            flag);
+  QFG_LAUNCHED(ctx);
+  return QFG_OK;
+}
+
 int semijoin(Ctx* ctx, const KeyCols& set_side, int64_t n_set, const KeyCols& bit_side,
              int64_t n_bits, uint64_t* d_bits, int64_t* num_ones) {
   const int64_t nwords = 2 * ((n_bits + 63) / 64);
@@ -256,31 +284,16 @@ int semijoin(Ctx* ctx, const KeyCols& set_side, int64_t n_set, const KeyCols& bi
     const int64_t pwords = mark ? (n_large + 31) / 32 : nwords;
     uint32_t* words = reinterpret_cast<uint32_t*>(d_bits);
     uint32_t* pout = mark ? nullptr : words;
-    const unsigned grid = (unsigned)std::max<int64_t>(
-        1, std::min<int64_t>((pwords + 7) / 8, (int64_t)ctx->num_sms * 8));
-    switch (small.nk) {
-      case 1:
-        semijoin_bits_kernel<1><<<grid, 256, 0, ctx->stream>>>(small, owner, mask, filter, fbits,
-                                                               large, n_large, pout, pwords, ones,
-                                                               flag);
-        break;
-      case 2:
-        semijoin_bits_kernel<2><<<grid, 256, 0, ctx->stream>>>(small, owner, mask, filter, fbits,
-                                                               large, n_large, pout, pwords, ones,
-                                                               flag);
-        break;
-      default:
-        semijoin_bits_kernel<0><<<grid, 256, 0, ctx->stream>>>(small, owner, mask, filter, fbits,
-                                                               large, n_large, pout, pwords, ones,
-                                                               flag);
-        break;
-    }
-    QFG_LAUNCHED(ctx);
     if (mark) {
-      semijoin_rep_bits_kernel<<<(unsigned)std::max<int64_t>(
-                                     1, std::min<int64_t>((nwords + 7) / 8,
-                                                          (int64_t)ctx->num_sms * 8)),
-                                 256, 0, ctx->stream>>>(rep, flag, n_bits, words, nwords, ones);
+      QFG_TRY(launch_semijoin_probe<true>(ctx, small.nk, small, owner, mask, filter, fbits, large,
+                                          n_large, pout, pwords, ones, flag));
+    } else {
+      QFG_TRY(launch_semijoin_probe<false>(ctx, small.nk, small, owner, mask, filter, fbits, large,
+                                           n_large, pout, pwords, ones, flag));
+    }
+    if (mark) {
+      semijoin_rep_bits_kernel<<<resident_grid(ctx, semijoin_rep_bits_kernel, nwords), 256, 0,
+                                 ctx->stream>>>(rep, flag, n_bits, words, nwords, ones);
       QFG_LAUNCHED(ctx);
     }
   }
