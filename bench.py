@@ -557,7 +557,8 @@ def run_radix_partition(eng, values, stream, torch, peak, bits: int = 15, reps: 
     """qfg_radix_partition (RadixPartition, stable, PartitionTuple output) of
     one 32M-row binding column at 15 radix bits, timed with CUDA events on
     the context stream; checked for a stable partition; HBM fraction on the
-    12 bytes a row of the benchmark spec's partition figure (4 read, 8 written)."""
+    12 bytes a row of a partition's I/O (the key and the row index read, the
+    index written)."""
     n = values.numel()
     tuples, offsets = eng.radix_partition(values, bits)
     torch.cuda.synchronize()
